@@ -1,0 +1,350 @@
+#!/usr/bin/env python
+"""Benchmark of the Chain hot path: TEBD gate+SVD steps/s at chi=1024.
+
+One step = one ``evolve!`` of a Haar-random two-site gate on a bond whose neighbours both have
+chi = 1024: theta (2048 x 2048 complex) = A_l diag(Lambda) A_r, gate, thin SVD, truncate! to
+maxdim = 1024 with the 1e-10 cutoff.  The chain is n = 24 random isometric sites (bonds
+min(1024, 2^i) mirrored), so bonds 10..14 carry chi = 1024; steps cycle over the three bonds whose
+neighbours are both full.  Every step touches > 129 MB (sites 64 MB, theta 64 MB, SVD buffers
+several x 64 MB), so inputs are larger than L2.
+
+Prints one JSON line (driver contract): ``value`` = gate-steps/s of the mixed path with the state
+resident in HBM; ``e2e`` = the same through the C ABI with pinned host buffers copied in and out
+every step; ``fp64`` = the plain all-FP64 path; ``roofline`` for the dominant kernel;
+``cpu_baseline`` = the oracle (NumPy/LAPACK) on the host cores.
+
+``--impl reference`` times the CPU restatement (the reference itself is Julia and is not
+installed), on the same workload, with all host threads.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "qrochet.jl_gb300")
+sys.path.insert(0, PKG)
+sys.path.insert(0, ROOT)
+
+METRIC = "TEBD gate+SVD steps/s at χ=1024; batched solves/s, p50/p99; mixed vs FP64 path"
+N_SITES, CHI, MAXDIM, CUTOFF = 24, 1024, 1024, 1e-10
+BONDS = (11, 12, 13)  # 1-based left sites of the gate bonds with chi=1024 on both sides
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=6)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--fp64-steps", type=int, default=2)
+    p.add_argument("--cpu-steps", type=int, default=2)
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--quick", action="store_true", help="small chi for a fast functional run")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    return rank, world, local
+
+
+class Dist:
+    """Barrier and max-reduce across replicas (gloo; no data-path collective)."""
+
+    def __init__(self, world):
+        self.world = world
+        if world > 1:
+            import torch.distributed as td
+
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, x):
+        if self.world == 1:
+            return x
+        import torch
+
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+
+def workload(chi):
+    from qrochet import random as R
+
+    g = R.rng(2024)
+    arrays = R.rand_chain_state_arrays(g, N_SITES, chi, p=2)
+    gates = [R.haar_unitary(g, 4) for _ in range(64)]
+    return arrays, gates
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out = ""
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def gate_flops(chi):
+    """Algorithmic flops of one gate step (theta GEMM + gate + R-SVD count of an m x n SVD,
+    m = n = 2 chi, 4 (4 m^2 n + 8 m n^2 + 9 n^3) real flops for complex)."""
+    m = n = 2 * chi
+    gemm = 8.0 * (2 * chi) * (2 * chi) * chi
+    gate = 8.0 * chi * chi * 16
+    svd = 4.0 * (4 * m * m * n + 8 * m * n * n + 9 * n ** 3)
+    return gemm + gate + svd
+
+
+def cpu_gate_step(al, ar, lam, u, maxdim):
+    """Oracle gate step (NumPy/LAPACK): the same arithmetic as evolve_2site! + truncate!."""
+    from oracle import chain_oracle as O
+
+    ch = O.OChain([np.ones((1, 2, al.shape[0]), dtype=complex)] + [al, ar] +
+                  [np.ones((ar.shape[2], 2, 1), dtype=complex)])
+    ch.lam[1] = lam
+    O.evolve_2site_(ch, 1, u, threshold=CUTOFF, maxdim=maxdim)
+    return ch
+
+
+def run_reference(args, chi):
+    """CPU restatement on all host threads (the Julia reference is not installed)."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    arrays, gates = workload(chi)
+    from oracle import chain_oracle as O
+
+    ch = O.from_reference_arrays(arrays)
+    steps = max(1, min(args.steps, 3))
+    warm = min(args.warmup, 1)
+    b = BONDS[0] - 1
+    al, ar = ch.sites[b], ch.sites[b + 1]
+    lam = np.ones(al.shape[2])
+    for i in range(warm):
+        cpu_gate_step(al, ar, lam, gates[i], MAXDIM if chi == CHI else chi)
+    t0 = time.perf_counter()
+    for i in range(steps):
+        cpu_gate_step(al, ar, lam, gates[i], MAXDIM if chi == CHI else chi)
+    dt = time.perf_counter() - t0
+    v = steps / dt
+    cores = os.cpu_count()
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "gate-steps/s", "n_gpus": args.gpus,
+            "steps": steps, "warmup": warm, "ms_per_step": 1e3 * dt / steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "complex128", "data": "synthetic",
+            "config": {"workload": f"tebd_gate_step_chi{chi}", "chi": chi, "theta": f"{2 * chi}x{2 * chi}",
+                       "maxdim": MAXDIM if chi == CHI else chi, "threshold": CUTOFF, "n_sites": N_SITES},
+            "cpu_baseline": {"value": v, "unit": "gate-steps/s", "cores": cores, "kind": "port",
+                             "sample": f"{steps} gate-steps of the {args.steps} requested (NumPy/LAPACK "
+                                       f"restatement of Chain.jl evolve_2site!+truncate!; Qrochet.jl is Julia "
+                                       f"and is not installed)"},
+            "e2e": {"value": v, "unit": "gate-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, chi):
+    import qrochet as Q
+
+    rank, world, local = dist_env()
+    dist = Dist(world)
+    Q.set_device(local)
+    arrays, gates = workload(chi)
+    maxdim = MAXDIM if chi == CHI else chi
+
+    def make(prec):
+        psi = Q.MPS(arrays)
+        psi.set_precision(prec)
+        return psi
+
+    def step(psi, i):
+        b = BONDS[i % len(BONDS)]
+        Q.evolve_(psi, Q.gate_from_matrix(gates[i % len(gates)], [b, b + 1]), threshold=CUTOFF, maxdim=maxdim)
+
+    # ---- mixed path, state resident in HBM -------------------------------------------------------
+    psi = make("mixed")
+    for i in range(args.warmup):
+        step(psi, i)
+    psi.sync()
+    clocks = Clocks(local)
+    clocks.start()
+    l0 = Q.launch_count()
+    dist.barrier()
+    psi.sync()
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        step(psi, args.warmup + i)
+    psi.sync()
+    dt = time.perf_counter() - t0
+    launches = Q.launch_count() - l0
+    dist.barrier()
+    clk = clocks.stop()
+    dt_max = dist.max(dt)
+    value = world * args.steps / dt_max
+
+    # ---- plain FP64 path ---------------------------------------------------------------------------
+    fp64 = None
+    if args.fp64_steps > 0:
+        p64 = make("fp64")
+        step(p64, 0)
+        p64.sync()
+        t1 = time.perf_counter()
+        for i in range(args.fp64_steps):
+            step(p64, 1 + i)
+        p64.sync()
+        d64 = dist.max(time.perf_counter() - t1)
+        fp64 = {"value": world * args.fp64_steps / d64, "unit": "gate-steps/s",
+                "ms_per_step": 1e3 * d64 / args.fp64_steps, "steps": args.fp64_steps}
+        del p64
+
+    # ---- e2e through the C ABI with pinned host buffers --------------------------------------------
+    pin = {}
+    for b in sorted({x for bb in BONDS for x in (bb, bb + 1)}):
+        pa = Q.PinnedArray(arrays[b - 1].shape)
+        pa.array[...] = arrays[b - 1]
+        po = Q.PinnedArray(arrays[b - 1].shape)
+        pin[b] = (pa, po)
+    pe = make("mixed")
+    h2d = d2h = 0
+    pe.sync()
+    t2 = time.perf_counter()
+    for i in range(args.steps):
+        b = BONDS[i % len(BONDS)]
+        for s in (b, b + 1):
+            pe.upload_site(s, pin[s][0].array)
+        step(pe, i)
+        for s in (b, b + 1):
+            pe.download_site(s, pin[s][1].array)
+        lam = pe.lambda_between(b, b + 1)
+        if i == 0:
+            h2d = 2 * pin[b][0].array.nbytes + 16 * 16
+            d2h = 2 * pin[b][1].array.nbytes + lam.nbytes
+    pe.sync()
+    de = dist.max(time.perf_counter() - t2)
+    e2e = {"value": world * args.steps / de, "unit": "gate-steps/s", "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * de / args.steps}
+    del pe
+
+    # ---- roofline of the dominant kernel (separate instrumented pass) -------------------------------
+    Q.prof_enable(True)
+    pr = make("mixed")
+    for i in range(min(3, args.steps)):
+        step(pr, i)
+    pr.sync()
+    stats = {k: Q.prof_read(k) for k in Q.PROF_KINDS}
+    Q.prof_enable(False)
+    del pr
+    dom = max(stats, key=lambda k: stats[k]["ms"])
+    peaks = {"zgemm_dmma": ("dmma", "tensor"), "jacobi_fp32": ("ffma", "fp32"), "jacobi_fp64": ("dfma", "fp64"),
+             "householder_qr": ("dfma", "fp64"), "env_mix": ("dfma", "fp64")}
+    pk_kind, bound = peaks[dom]
+    peak = Q.probe_peak(pk_kind)
+    st = stats[dom]
+    achieved = st["flops"] / (st["ms"] * 1e-3) / 1e12 if st["ms"] > 0 else 0.0
+    shares = {k: round(v["ms"] / max(1e-9, sum(x["ms"] for x in stats.values())), 4) for k, v in stats.items()}
+    roofline = {"bound": bound, "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak if peak else None, "traffic": None,
+                "peak_source": f"measured in-process ({pk_kind} loop kernel, best of 3)",
+                "launches": st["launches"], "avg_launch_ms": st["ms"] / max(1, st["launches"]),
+                "time_share": shares}
+    try:
+        mp = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        roofline["measured_peaks_json"] = {"hbm_gbs": mp.get("hbm_gbs"), "bf16_tflops": mp.get("bf16_tflops")}
+    except Exception:
+        pass
+
+    # ---- CPU baseline (rank 0, bounded sample) ------------------------------------------------------
+    cpu = None
+    if rank == 0 and not args.no_cpu and args.cpu_steps > 0:
+        from oracle import chain_oracle as O
+
+        ch = O.from_reference_arrays(arrays)
+        b = BONDS[0] - 1
+        al, ar = ch.sites[b], ch.sites[b + 1]
+        lam = np.ones(al.shape[2])
+        t3 = time.perf_counter()
+        for i in range(args.cpu_steps):
+            cpu_gate_step(al, ar, lam, gates[i], maxdim)
+        dc = time.perf_counter() - t3
+        cpu = {"value": args.cpu_steps / dc, "unit": "gate-steps/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"{args.cpu_steps} gate-steps at chi={chi} (NumPy/LAPACK zgesdd restatement, all host "
+                         f"threads)"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "gate-steps/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1e3 * dt_max / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None,
+                "dtype": "complex64 Jacobi preconditioner + complex128 (FP64 DMMA) refinement; FP64 theta",
+                "data": "synthetic",
+                "config": {"workload": f"tebd_gate_step_chi{chi}", "chi": chi, "theta": f"{2 * chi}x{2 * chi}",
+                           "maxdim": maxdim, "threshold": CUTOFF, "n_sites": N_SITES, "precision": "mixed",
+                           "parallelism": "replicas" if world > 1 else "single",
+                           "l2": "inputs larger than L2 (>129 MB touched per step)"},
+                "fp64": fp64, "mixed_over_fp64": (value / fp64["value"]) if fp64 else None,
+                "gflop_per_step": gate_flops(chi) / 1e9, "e2e": e2e, "gpu_launches": launches,
+                "roofline": roofline, "cpu_baseline": cpu, "clocks": clk}
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    chi = 128 if args.quick else CHI
+    if args.impl == "reference":
+        run_reference(args, chi)
+    else:
+        run_ours(args, chi)
+
+
+if __name__ == "__main__":
+    main()

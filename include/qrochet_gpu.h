@@ -1,0 +1,137 @@
+/*
+ * qrochet_gpu.h -- C ABI of the GB300 (sm_103a) implementation of Qrochet.jl's Chain (MPS/MPO)
+ * hot path.  Plain pointers and sizes only; every call returns a status code (QR_OK == 0) and
+ * leaves a message for qr_last_error_string() on failure.
+ *
+ * Layout conventions at the boundary (what a Julia `ccall` passes from `Array{ComplexF64}`):
+ *   - complex numbers are interleaved (re, im) doubles;
+ *   - site arrays are column-major with dims named by a 3-letter `order` string over
+ *     {'o','l','r'} (states) or a 4-letter string over {'o','i','l','r'} (operators); the open
+ *     ends omit 'l' (site 1) and 'r' (site n) exactly like Chain(State(), Open(), arrays; order);
+ *   - sites and bonds are 0-based here; bond b joins sites b and b+1;
+ *   - gates are row-major matrices M[(o_1..o_k),(i_1..i_k)] with the left lane slowest.
+ *
+ * Reference interfaces replaced (paths inside Qrochet.jl v0.1.2):
+ *   Chain(State(), Open(), arrays; order)   src/Ansatz/Chain.jl:64-100
+ *   Chain(Operator(), Open(), arrays)       src/Ansatz/Chain.jl:133-172
+ *   copy(::Chain)                           src/Ansatz/Chain.jl:11
+ *   canonize_site!                          src/Ansatz/Chain.jl:339-376
+ *   truncate!                               src/Ansatz/Chain.jl:390-422
+ *   canonize!                               src/Ansatz/Chain.jl:469-497
+ *   mixed_canonize!                         src/Ansatz/Chain.jl:509-524
+ *   normalize!(::Chain, ::Site)             src/Ansatz/Chain.jl:532-536
+ *   contract!(::Chain, Val(:between))       src/Ansatz/Chain.jl:309-333
+ *   evolve! / evolve_1site! / evolve_2site! src/Ansatz/Chain.jl:543-661 (+669-722 Vidal path)
+ *   expect                                  src/Ansatz/Chain.jl:724-735
+ *   overlap(::State, ::Chain, ::State, ::Chain)  src/Ansatz/Chain.jl:740-748
+ *   LinearAlgebra.norm(::Ansatz)            src/Ansatz.jl:101-109
+ *   isleftcanonical / isrightcanonical      src/Ansatz/Chain.jl:424-458
+ */
+#ifndef QROCHET_GPU_H
+#define QROCHET_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct qr_chain qr_chain; /* one open-boundary MPS resident in device memory */
+typedef struct qr_mpo qr_mpo;     /* one open-boundary MPO resident in device memory */
+
+/* Status codes; the Julia shim maps them to the reference's exceptions. */
+#define QR_OK 0
+#define QR_EINVAL 1       /* ArgumentError */
+#define QR_EASSERT 2      /* AssertionError (@assert) */
+#define QR_ENO_SCHMIDT 3  /* MissingSchmidtCoefficientsException (src/Ansatz.jl:91-99) */
+#define QR_EDIM 4         /* DimensionMismatch */
+#define QR_ENOMEM 5       /* device allocation failed */
+#define QR_ECUDA 6        /* CUDA runtime error */
+#define QR_ENODEV 7       /* no CUDA device */
+#define QR_ENOCONV 8      /* SVD sweeps did not converge */
+
+/* Precision of a chain's arithmetic (qr_chain_set_precision). */
+#define QR_FP64 0  /* plain: all ComplexF64 */
+#define QR_MIXED 1 /* FP32 Jacobi preconditioner + FP64 refinement for SVD; split-precision
+                      tensor-core contractions for environment sweeps */
+
+#define QR_DIR_LEFT 0
+#define QR_DIR_RIGHT 1
+#define QR_METHOD_QR 0
+#define QR_METHOD_SVD 1
+
+/* ---- library ---------------------------------------------------------------------------- */
+const char* qr_last_error_string(void);
+int qr_version(int* major, int* minor);
+int qr_device_count(int* count);
+int qr_set_device(int device);
+/* number of kernels this library has launched in this process (for launch accounting) */
+int qr_launch_count(uint64_t* count);
+
+/* per-kernel-class CUDA-event timing, for benchmarks: kinds 0 zgemm (FP64 DMMA), 1 Jacobi FP64,
+   2 Jacobi FP32, 3 Householder QR, 4 environment mixing.  No reference counterpart. */
+int qr_prof_enable(int on);
+int qr_prof_read(int kind, double* ms, uint64_t* launches, double* flops, double* bytes);
+/* peak of one pipe measured now: 0 FP64 tensor (DMMA), 1 FP32 FFMA, 2 FP64 DFMA (TFLOP/s) */
+int qr_probe_peak(int kind, double* tflops);
+/* page-locked host buffers for host<->device copies (cudaHostAlloc). */
+int qr_host_alloc(uint64_t bytes, void** ptr);
+int qr_host_free(void* ptr);
+
+/* ---- chain lifecycle (Chain.jl:64-100, :11) --------------------------------------------- */
+int qr_chain_create(int n, int d, const int* bond_dims /* n-1 */, qr_chain** out);
+int qr_chain_free(qr_chain* h);
+int qr_chain_copy(const qr_chain* src, qr_chain** out);
+int qr_chain_upload_site(qr_chain* h, int site, const double* host, const char* order);
+int qr_chain_download_site(const qr_chain* h, int site, double* host, const char* order);
+int qr_chain_site_dims(const qr_chain* h, int site, int* chi_l, int* d, int* chi_r);
+int qr_chain_bond_dims(const qr_chain* h, int* out /* n-1 */);
+int qr_chain_has_lambda(const qr_chain* h, int bond, int* flag);
+int qr_chain_get_lambda(const qr_chain* h, int bond, double* out, int* len);
+int qr_chain_set_lambda(qr_chain* h, int bond, const double* lam, int len);
+int qr_chain_ntensors(const qr_chain* h, int* out);
+int qr_chain_nsites(const qr_chain* h, int* out);
+int qr_chain_set_precision(qr_chain* h, int mode);
+int qr_chain_get_precision(const qr_chain* h, int* mode);
+/* the cudaStream_t this chain's work is ordered on (for caller-side CUDA events) */
+int qr_chain_stream(const qr_chain* h, void** stream);
+int qr_chain_sync(const qr_chain* h);
+
+/* ---- canonical forms (Chain.jl:339-376, 469-536, 309-333) ------------------------------- */
+int qr_canonize_site(qr_chain* h, int site, int direction, int method);
+int qr_canonize(qr_chain* h);
+int qr_mixed_canonize(qr_chain* h, int center);
+int qr_normalize(qr_chain* h, int root);
+int qr_contract_between(qr_chain* h, int site1, int site2, int direction, int delete_lambda);
+/* ||A^dagger A - I||_F of a site viewed [(l,o) x r] (left) or A A^dagger over [l x (o,r)] */
+int qr_canonicality_error(const qr_chain* h, int site, int direction, double* err);
+
+/* ---- truncation (Chain.jl:390-422): threshold NaN -> 1e-16 default; maxdim < 0 -> none -- */
+int qr_truncate(qr_chain* h, int site1, int site2, double threshold, int maxdim);
+
+/* ---- gates (Chain.jl:543-661, 669-722) --------------------------------------------------- */
+int qr_evolve_1site(qr_chain* h, int site, const double* gate /* d x d */);
+/* threshold NaN and maxdim < 0 together mean: no truncate! call */
+int qr_evolve_2site(qr_chain* h, int site_l, const double* gate /* d^2 x d^2 */,
+                    double threshold, int maxdim, int iscanonical, int renormalize);
+
+/* ---- contractions (Chain.jl:724-748, Ansatz.jl:101-109) ---------------------------------- */
+/* <b|a> (b conjugated), written as (re, im) */
+int qr_overlap(const qr_chain* a, const qr_chain* b, double* out);
+int qr_norm(const qr_chain* h, double* out);
+/* unnormalised <psi| O_{k-1} ... O_0 |psi>; observable j acts on lanes first[j]..first[j]+nl[j]-1
+   (nl in {1,2}) with the row-major matrix starting at mats + 2*offset_j (complex entries,
+   offsets packed in order) */
+int qr_expect(const qr_chain* h, int nobs, const int* first, const int* nlanes,
+              const double* mats, double* out);
+
+/* ---- MPO (Chain.jl:133-172) and <psi|H|psi> (merge, src/Quantum.jl:330-348) -------------- */
+int qr_mpo_create(int n, int d, const int* bond_dims /* n-1 */, qr_mpo** out);
+int qr_mpo_free(qr_mpo* w);
+int qr_mpo_upload_site(qr_mpo* w, int site, const double* host, const char* order);
+int qr_mpo_expect(const qr_chain* h, const qr_mpo* w, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QROCHET_GPU_H */

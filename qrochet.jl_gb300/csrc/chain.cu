@@ -1,0 +1,946 @@
+// C ABI of the GB300 Chain path: a device-resident open-boundary MPS (qr_chain) and MPO
+// (qr_mpo), and the drivers of the reference's methods on them.
+//
+// Device layout: site i is a column-major (chi_l, d, chi_r) array with chi_l fastest, so both
+// groupings the reference factorises are plain column-major matrices: [(l,o) x r] (ld chi_l*d)
+// for direction=:right and [l x (o,r)] (ld chi_l) for direction=:left.  The two-site block
+// theta[(l,o1) x (o2,r)] is then one GEMM of neighbouring sites, and its SVD factors U and Vh
+// are directly the new site tensors.  The open ends carry bonds of size 1.  Lambda vectors live
+// in their own device buffers, one per bond that holds one (the reference keeps them as
+// separate hyperindex tensors on the bond, src/Ansatz/Chain.jl:338).
+#include <vector>
+#include <string>
+#include <complex>
+#include <cstring>
+#include <cmath>
+#include <mutex>
+#include "kernels.cuh"
+
+namespace qr {
+
+static thread_local std::string t_err;
+std::atomic<uint64_t> g_launches{0};
+
+void set_error(const std::string& msg) { t_err = msg; }
+int fail(int code, const std::string& msg) {
+  t_err = msg;
+  return code;
+}
+int cuda_fail(cudaError_t e, const char* what) {
+  t_err = std::string(what) + ": " + cudaGetErrorString(e);
+  return (e == cudaErrorMemoryAllocation) ? QR_ENOMEM
+         : (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) ? QR_ENODEV
+                                                                        : QR_ECUDA;
+}
+
+static std::once_flag g_pool_once;
+static void init_pool() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    uint64_t thr = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+}
+
+}  // namespace qr
+
+using namespace qr;
+
+struct qr_chain {
+  int n = 0, d = 0, precision = QR_FP64;
+  cudaStream_t stream = nullptr;
+  std::vector<int> bd;            // n-1 bond sizes
+  std::vector<double2*> site;     // n site tensors
+  std::vector<double*> lam;       // n-1 Lambda vectors or nullptr
+  std::vector<int> lamlen;
+  SvdWork* svd = nullptr;
+  double2* gate = nullptr;        // d^4 complex scratch for gate matrices
+  double2* ws = nullptr;          // theta / factorisation workspace
+  size_t ws_cap = 0;
+  double* scal = nullptr;         // small device scalars
+  int cl(int i) const { return i == 0 ? 1 : bd[i - 1]; }
+  int cr(int i) const { return i == n - 1 ? 1 : bd[i]; }
+  size_t elems(int i) const { return (size_t)cl(i) * d * cr(i); }
+};
+
+struct qr_mpo {
+  int n = 0, d = 0;
+  std::vector<int> bd;
+  std::vector<double2*> site;  // (wl, o, i, wr), wl fastest
+  int wl(int i) const { return i == 0 ? 1 : bd[i - 1]; }
+  int wr(int i) const { return i == n - 1 ? 1 : bd[i]; }
+};
+
+namespace {
+
+int cuda_ok(cudaError_t e, const char* what) { return e == cudaSuccess ? QR_OK : cuda_fail(e, what); }
+
+int dalloc(void** p, size_t bytes, cudaStream_t s) {
+  if (bytes == 0) bytes = 16;
+  cudaError_t e = cudaMallocAsync(p, bytes, s);
+  if (e != cudaSuccess) return fail(QR_ENOMEM, std::string("device allocation: ") + cudaGetErrorString(e));
+  return QR_OK;
+}
+
+int ensure_ws(qr_chain* h, size_t elems) {
+  if (elems <= h->ws_cap) return QR_OK;
+  if (h->ws) cudaFreeAsync(h->ws, h->stream);
+  h->ws = nullptr;
+  h->ws_cap = 0;
+  size_t want = elems + elems / 4 + 64;
+  QR_TRY(dalloc((void**)&h->ws, want * sizeof(double2), h->stream));
+  h->ws_cap = want;
+  return QR_OK;
+}
+
+// replace site i's buffer (frees the old one on the chain's stream)
+void set_site(qr_chain* h, int i, double2* p) {
+  if (h->site[i] && h->site[i] != p) cudaFreeAsync(h->site[i], h->stream);
+  h->site[i] = p;
+}
+
+void drop_lambda(qr_chain* h, int b) {
+  if (h->lam[b]) cudaFreeAsync(h->lam[b], h->stream);
+  h->lam[b] = nullptr;
+  h->lamlen[b] = 0;
+}
+
+// Bond b gets Lambda = the first len entries of src (device); src is copied.
+int put_lambda(qr_chain* h, int b, const double* src, int len) {
+  double* p = nullptr;
+  QR_TRY(dalloc((void**)&p, sizeof(double) * len, h->stream));
+  QR_CUDA(cudaMemcpyAsync(p, src, sizeof(double) * len, cudaMemcpyDeviceToDevice, h->stream));
+  drop_lambda(h, b);
+  h->lam[b] = p;
+  h->lamlen[b] = len;
+  return QR_OK;
+}
+
+int upload_gate(qr_chain* h, const double* g, int dim) {
+  QR_CUDA(cudaMemcpyAsync(h->gate, g, sizeof(double2) * dim * dim, cudaMemcpyHostToDevice, h->stream));
+  return QR_OK;
+}
+
+// filter the 3/4-letter order like the reference does for open ends
+std::string filtered(const char* order, bool first, bool last) {
+  std::string o(order ? order : "");
+  std::string out;
+  for (char c : o) {
+    if (first && c == 'l') continue;
+    if (last && c == 'r') continue;
+    out.push_back(c);
+  }
+  return out;
+}
+
+bool is_perm(const std::string& o, const char* letters) {
+  std::string a = o, b = letters;
+  if (a.size() != b.size()) return false;
+  for (char c : b)
+    if (a.find(c) == std::string::npos) return false;
+  return true;
+}
+
+// Perm that maps a host column-major array with dims named by `hord` into the internal layout
+// `iord` (dims `idims` by letter).
+Perm make_perm(const std::string& hord, const std::string& iord, const long* idims_by_iord) {
+  // host strides by letter
+  long stride[8] = {0};
+  char letters[8];
+  int nl = 0;
+  long acc = 1;
+  for (char c : hord) {
+    long dim = 1;
+    for (size_t k = 0; k < iord.size(); k++)
+      if (iord[k] == c) dim = idims_by_iord[k];
+    letters[nl] = c;
+    stride[nl++] = acc;
+    acc *= dim;
+  }
+  Perm p;
+  p.nd = (int)iord.size();
+  for (size_t k = 0; k < iord.size(); k++) {
+    p.dims[k] = idims_by_iord[k];
+    p.src_stride[k] = 0;
+    for (int q = 0; q < nl; q++)
+      if (letters[q] == iord[k]) p.src_stride[k] = stride[q];
+  }
+  return p;
+}
+
+int check_site(const qr_chain* h, int i) {
+  if (!h) return fail(QR_EINVAL, "null chain");
+  if (i < 0 || i >= h->n) return fail(QR_EINVAL, "site out of range");
+  return QR_OK;
+}
+
+// ---- canonize_site! (Chain.jl:339-376) ---------------------------------------------------------
+int canonize_site_impl(qr_chain* h, int i, int dir, int method) {
+  QR_TRY(check_site(h, i));
+  if (dir == QR_DIR_LEFT) {
+    if (i == 0) return fail(QR_EINVAL, "Cannot right-canonize left-most tensor");
+  } else if (dir == QR_DIR_RIGHT) {
+    if (i == h->n - 1) return fail(QR_EINVAL, "Cannot left-canonize right-most tensor");
+  } else {
+    return fail(QR_EINVAL, "Unknown direction");
+  }
+  if (method != QR_METHOD_QR && method != QR_METHOD_SVD) return fail(QR_EINVAL, "Unknown factorization method");
+  cudaStream_t s = h->stream;
+  const int d = h->d, cl = h->cl(i), cr = h->cr(i);
+  const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
+  if (dir == QR_DIR_RIGHT) {
+    const int m = cl * d, nn = cr, k = m < nn ? m : nn;
+    const int cr2 = h->cr(i + 1);
+    // ws: [M copy (m*nn)] [R or Vh (k*nn)] [S (k doubles)] [tau (k)]
+    QR_TRY(ensure_ws(h, (size_t)m * nn + (size_t)k * nn + k + k));
+    double2* W = h->ws;
+    double2* Rr = W + (size_t)m * nn;
+    double* S = (double*)(Rr + (size_t)k * nn);
+    double2* tau = Rr + (size_t)k * nn + k;
+    double2* Q = nullptr;
+    QR_TRY(dalloc((void**)&Q, sizeof(double2) * (size_t)m * k, s));
+    if (method == QR_METHOD_QR) {
+      QR_CUDA(cudaMemcpyAsync(W, h->site[i], sizeof(double2) * (size_t)m * nn, cudaMemcpyDeviceToDevice, s));
+      QR_TRY(zqr_thin(s, W, m, nn, m, Q, m, Rr, k, tau));
+    } else {
+      QR_TRY(zsvd_thin(s, h->svd, h->precision, h->site[i], m, nn, m, Q, m, S, Rr, k));
+    }
+    // next site <- R diag(Lambda_i) A_{i+1}
+    double2* nxt = nullptr;
+    QR_TRY(dalloc((void**)&nxt, sizeof(double2) * (size_t)k * d * cr2, s));
+    QR_TRY(zgemm(s, OP_N, OP_N, k, d * cr2, cr, one, Rr, k, 0, h->site[i + 1], cr, 0, zero, nxt, k, 0, 1,
+                 h->lam[i]));
+    set_site(h, i, Q);
+    set_site(h, i + 1, nxt);
+    h->bd[i] = k;
+    drop_lambda(h, i);
+    if (method == QR_METHOD_SVD) QR_TRY(put_lambda(h, i, S, k));
+  } else {
+    const int m = d * cr, nn = cl, k = m < nn ? m : nn;
+    const int cl0 = h->cl(i - 1);
+    // ws: [M = A^T (m*nn)] [Q (m*k)] [R or Vh (k*nn)] [S] [tau]
+    QR_TRY(ensure_ws(h, (size_t)m * nn + (size_t)m * k + (size_t)k * nn + k + k));
+    double2* W = h->ws;
+    double2* Q = W + (size_t)m * nn;
+    double2* Rr = Q + (size_t)m * k;
+    double* S = (double*)(Rr + (size_t)k * nn);
+    double2* tau = Rr + (size_t)k * nn + k;
+    QR_TRY(ztranspose(s, h->site[i], cl, cl, d * cr, W, m, 0));  // M[(o,r), l] = A[l, (o,r)]
+    if (method == QR_METHOD_QR) {
+      QR_TRY(zqr_thin(s, W, m, nn, m, Q, m, Rr, k, tau));
+    } else {
+      QR_TRY(zsvd_thin(s, h->svd, h->precision, W, m, nn, m, Q, m, S, Rr, k));
+    }
+    double2* cur = nullptr;
+    QR_TRY(dalloc((void**)&cur, sizeof(double2) * (size_t)k * m, s));
+    QR_TRY(ztranspose(s, Q, m, m, k, cur, k, 0));  // new site [k x (o,r)] = Q^T
+    double2* prv = nullptr;
+    QR_TRY(dalloc((void**)&prv, sizeof(double2) * (size_t)cl0 * d * k, s));
+    // prev <- A_{i-1} diag(Lambda_{i-1}) R^T
+    QR_TRY(zgemm(s, OP_N, OP_T, cl0 * d, k, cl, one, h->site[i - 1], cl0 * d, 0, Rr, k, 0, zero, prv, cl0 * d,
+                 0, 1, h->lam[i - 1]));
+    set_site(h, i, cur);
+    set_site(h, i - 1, prv);
+    h->bd[i - 1] = k;
+    drop_lambda(h, i - 1);
+    if (method == QR_METHOD_SVD) QR_TRY(put_lambda(h, i - 1, S, k));
+  }
+  return QR_OK;
+}
+
+int scale_site_by_lambda(qr_chain* h, int i, int side, const double* lam, int inv, double atol) {
+  return zscale_bond(h->stream, h->site[i], h->cl(i), h->d, h->cr(i), lam, side, inv, atol);
+}
+
+// ---- truncate! (Chain.jl:390-422) -------------------------------------------------------------
+int truncate_impl(qr_chain* h, int s1, int s2, double threshold, int maxdim) {
+  if (!h) return fail(QR_EINVAL, "null chain");
+  if (s2 != s1 + 1 || s1 < 0 || s2 >= h->n) return fail(QR_EINVAL, "Invalid bond");
+  const int b = s1;
+  if (!h->lam[b]) return fail(QR_ENO_SCHMIDT, "Can't access the spectrum on bond");
+  const int dim = h->lamlen[b];
+  std::vector<double> lam(dim);
+  QR_CUDA(cudaMemcpyAsync(lam.data(), h->lam[b], sizeof(double) * dim, cudaMemcpyDeviceToHost, h->stream));
+  QR_CUDA(cudaStreamSynchronize(h->stream));
+  int upto = (maxdim >= 0) ? (maxdim < dim ? maxdim : dim) : dim;
+  if (std::isnan(threshold)) threshold = 1e-16;
+  std::vector<int> keep;
+  for (int k = 0; k < upto; k++)
+    if (std::fabs(lam[k]) > threshold) keep.push_back(k);
+  const int nk = (int)keep.size();
+  if (nk == 0) return fail(QR_EINVAL, "truncation would leave an empty bond");
+  bool prefix = true;
+  for (int k = 0; k < nk; k++) prefix = prefix && (keep[k] == k);
+  if (nk == dim) return QR_OK;
+  cudaStream_t s = h->stream;
+  const int d = h->d, cl = h->cl(s1), cr2 = h->cr(s2);
+  double2 *a = nullptr, *c = nullptr;
+  QR_TRY(dalloc((void**)&a, sizeof(double2) * (size_t)cl * d * nk, s));
+  QR_TRY(dalloc((void**)&c, sizeof(double2) * (size_t)nk * d * cr2, s));
+  double* nl = nullptr;
+  QR_TRY(dalloc((void**)&nl, sizeof(double) * nk, s));
+  if (prefix) {
+    QR_CUDA(cudaMemcpyAsync(a, h->site[s1], sizeof(double2) * (size_t)cl * d * nk, cudaMemcpyDeviceToDevice, s));
+    QR_CUDA(cudaMemcpy2DAsync(c, sizeof(double2) * nk, h->site[s2], sizeof(double2) * dim, sizeof(double2) * nk,
+                              (size_t)d * cr2, cudaMemcpyDeviceToDevice, s));
+    QR_CUDA(cudaMemcpyAsync(nl, h->lam[b], sizeof(double) * nk, cudaMemcpyDeviceToDevice, s));
+  } else {
+    for (int k = 0; k < nk; k++) {
+      int src = keep[k];
+      QR_CUDA(cudaMemcpyAsync(a + (size_t)cl * d * k, h->site[s1] + (size_t)cl * d * src,
+                              sizeof(double2) * (size_t)cl * d, cudaMemcpyDeviceToDevice, s));
+      QR_CUDA(cudaMemcpy2DAsync(c + k, sizeof(double2) * nk, h->site[s2] + src, sizeof(double2) * dim,
+                                sizeof(double2), (size_t)d * cr2, cudaMemcpyDeviceToDevice, s));
+      QR_CUDA(cudaMemcpyAsync(nl + k, h->lam[b] + src, sizeof(double), cudaMemcpyDeviceToDevice, s));
+    }
+  }
+  set_site(h, s1, a);
+  set_site(h, s2, c);
+  drop_lambda(h, b);
+  h->lam[b] = nl;
+  h->lamlen[b] = nk;
+  h->bd[b] = nk;
+  return QR_OK;
+}
+
+int mixed_canonize_impl(qr_chain* h, int center) {
+  QR_TRY(check_site(h, center));
+  for (int i = 0; i < center; i++) QR_TRY(canonize_site_impl(h, i, QR_DIR_RIGHT, QR_METHOD_QR));
+  for (int i = h->n - 1; i > center; i--) QR_TRY(canonize_site_impl(h, i, QR_DIR_LEFT, QR_METHOD_QR));
+  return canonize_site_impl(h, center, QR_DIR_LEFT, QR_METHOD_SVD);
+}
+
+int normalize_impl(qr_chain* h, int root) {
+  QR_TRY(mixed_canonize_impl(h, root));
+  return dnormalize(h->stream, h->lam[root - 1], h->lamlen[root - 1]);
+}
+
+// ---- evolve_2site! (Chain.jl:606-661) + Vidal helpers (Chain.jl:669-722) ------------------------
+int evolve2_impl(qr_chain* h, int sl, const double* g, double threshold, int maxdim, int iscanonical,
+                 int renormalize) {
+  if (!h) return fail(QR_EINVAL, "null chain");
+  if (sl < 0 || sl + 1 >= h->n) return fail(QR_EINVAL, "The sites in the bond must be between 1 and n");
+  const int sr = sl + 1, n = h->n, d = h->d;
+  cudaStream_t s = h->stream;
+  QR_TRY(upload_gate(h, g, d * d));
+  const double* lam_prev = nullptr;
+  const double* lam_next = nullptr;
+  if (iscanonical) {
+    lam_prev = (sl == 0) ? nullptr : h->lam[sl - 1];
+    lam_next = (sl == n - 2) ? nullptr : h->lam[sr];
+    if (lam_prev) QR_TRY(scale_site_by_lambda(h, sl, 0, lam_prev, 0, 0.0));
+    if (lam_next) QR_TRY(scale_site_by_lambda(h, sr, 2, lam_next, 0, 0.0));
+  }
+  const int cl = h->cl(sl), cb = h->bd[sl], cr = h->cr(sr);
+  const int m = cl * d, nn = d * cr, k = m < nn ? m : nn;
+  QR_TRY(ensure_ws(h, (size_t)m * nn + k));
+  double2* th = h->ws;
+  double* S = (double*)(th + (size_t)m * nn);
+  const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
+  // theta = A_l diag(Lambda) A_r  [(l,o1) x (o2,r)]
+  QR_TRY(zgemm(s, OP_N, OP_N, m, nn, cb, one, h->site[sl], m, 0, h->site[sr], cb, 0, zero, th, m, 0, 1, h->lam[sl]));
+  QR_TRY(zgate2(s, th, cl, d, cr, h->gate));
+  double2 *U = nullptr, *Vh = nullptr;
+  QR_TRY(dalloc((void**)&U, sizeof(double2) * (size_t)m * k, s));
+  QR_TRY(dalloc((void**)&Vh, sizeof(double2) * (size_t)k * nn, s));
+  QR_TRY(zsvd_thin(s, h->svd, h->precision, th, m, nn, m, U, m, S, Vh, k));
+  set_site(h, sl, U);
+  set_site(h, sr, Vh);
+  h->bd[sl] = k;
+  if (iscanonical) {
+    if (lam_prev) QR_TRY(scale_site_by_lambda(h, sl, 0, lam_prev, 1, 1e-32));
+    if (lam_next) QR_TRY(scale_site_by_lambda(h, sr, 2, lam_next, 1, 1e-32));
+  }
+  QR_TRY(put_lambda(h, sl, S, k));
+  const bool trunc = !std::isnan(threshold) || maxdim >= 0;
+  if (trunc) {
+    QR_TRY(truncate_impl(h, sl, sr, threshold, maxdim));
+    if (renormalize && iscanonical) {
+      QR_TRY(dnormalize(s, h->lam[sl], h->lamlen[sl]));
+    } else if (renormalize) {
+      QR_TRY(normalize_impl(h, sl));  // at site 1 this raises after the QR sweeps, as the reference does
+    }
+  }
+  return QR_OK;
+}
+
+// ---- environment sweeps: <b|W|a> with per-site operators W (or none) ----------------------------
+__global__ void scale_env_k(double2* E, int ca, int w, int cb, const double* lk, const double* lb) {
+  long total = (long)ca * w * cb;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+    long a = t % ca, b = t / ((long)ca * w);
+    double f = (lk ? lk[a] : 1.0) * (lb ? lb[b] : 1.0);
+    E[t] = cscale(E[t], f);
+  }
+}
+
+// Y[b,o,w',a'] = sum_{w,i} W[w,o,i,w'] X[w,b,i,a']
+__global__ void mix_k(const double2* __restrict__ X, double2* __restrict__ Y, const double2* __restrict__ W,
+                      int wl, int wr, int d, int cb, int ca2) {
+  extern __shared__ double2 Ws[];
+  const int nw = wl * d * d * wr;
+  for (int t = threadIdx.x; t < nw; t += blockDim.x) Ws[t] = W[t];
+  __syncthreads();
+  long pairs = (long)cb * ca2;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < pairs; t += (long)gridDim.x * blockDim.x) {
+    long b = t % cb, a2 = t / cb;
+    for (int o = 0; o < d; o++)
+      for (int w2 = 0; w2 < wr; w2++) {
+        double2 acc = make_double2(0, 0);
+        for (int i = 0; i < d; i++)
+          for (int w = 0; w < wl; w++) {
+            double2 x = X[w + wl * (b + (long)cb * (i + (long)d * a2))];
+            acc = cadd(acc, cmul(Ws[w + wl * (o + d * (i + d * w2))], x));
+          }
+        Y[b + (long)cb * (o + (long)d * (w2 + (long)wr * a2))] = acc;
+      }
+  }
+}
+
+struct EnvOps {
+  std::vector<const double2*> W;  // per site, device (wl,o,i,wr) or nullptr for identity
+  std::vector<int> wl, wr;
+};
+
+int env_sweep(const qr_chain* a, const qr_chain* b, const EnvOps* ops, cudaStream_t s, double out[2]) {
+  const int n = a->n, d = a->d;
+  // largest buffers
+  size_t maxE = 1, maxX = 1;
+  for (int i = 0; i < n; i++) {
+    int wl = ops ? ops->wl[i] : 1, wr = ops ? ops->wr[i] : 1;
+    size_t e = (size_t)a->cr(i) * wr * b->cr(i);
+    size_t x = (size_t)wl * b->cl(i) * d * a->cr(i);
+    size_t y = (size_t)b->cl(i) * d * wr * a->cr(i);
+    if (e > maxE) maxE = e;
+    if (x > maxX) maxX = x;
+    if (y > maxX) maxX = y;
+  }
+  double2 *E0 = nullptr, *E1 = nullptr, *X = nullptr, *Y = nullptr;
+  QR_TRY(dalloc((void**)&E0, sizeof(double2) * maxE, s));
+  QR_TRY(dalloc((void**)&E1, sizeof(double2) * maxE, s));
+  QR_TRY(dalloc((void**)&X, sizeof(double2) * maxX, s));
+  QR_TRY(dalloc((void**)&Y, sizeof(double2) * maxX, s));
+  const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
+  double2 init = one;
+  QR_CUDA(cudaMemcpyAsync(E0, &init, sizeof(double2), cudaMemcpyHostToDevice, s));
+  int rc = QR_OK;
+  for (int i = 0; i < n && rc == QR_OK; i++) {
+    const int ca = a->cl(i), ca2 = a->cr(i), cb = b->cl(i), cb2 = b->cr(i);
+    const int wl = ops ? ops->wl[i] : 1, wr = ops ? ops->wr[i] : 1;
+    const double2* W = ops ? ops->W[i] : nullptr;
+    if (i > 0 && (a->lam[i - 1] || b->lam[i - 1])) {
+      long tot = (long)ca * wl * cb;
+      unsigned g = (unsigned)((tot + 255) / 256);
+      scale_env_k<<<g > 4864 ? 4864 : g, 256, 0, s>>>(E0, ca, wl, cb, a->lam[i - 1], b->lam[i - 1]);
+      count_launch();
+    }
+    // X[(w,b) x (i,a')] = E^T A
+    rc = zgemm(s, OP_T, OP_N, wl * cb, d * ca2, ca, one, E0, ca, 0, a->site[i], ca, 0, zero, X, wl * cb, 0, 1, nullptr);
+    if (rc) break;
+    const double2* Yp = X;
+    if (W) {
+      long pairs = (long)cb * ca2;
+      unsigned g = (unsigned)((pairs + 255) / 256);
+      mix_k<<<g > 4864 ? 4864 : g, 256, sizeof(double2) * wl * d * d * wr, s>>>(X, Y, W, wl, wr, d, cb, ca2);
+      count_launch();
+      Yp = Y;
+    }
+    // E'_w' = Y_w'^T conj(B)
+    rc = zgemm(s, OP_T, OP_R, ca2, cb2, cb * d, one, Yp, (long)cb * d * wr, (long)cb * d, b->site[i], (long)cb * d, 0,
+               zero, E1, (long)ca2 * wr, ca2, wr, nullptr);
+    std::swap(E0, E1);
+  }
+  if (rc == QR_OK) {
+    QR_CUDA(cudaGetLastError());
+    double2 r;
+    QR_CUDA(cudaMemcpyAsync(&r, E0, sizeof(double2), cudaMemcpyDeviceToHost, s));
+    QR_CUDA(cudaStreamSynchronize(s));
+    out[0] = r.x;
+    out[1] = r.y;
+  }
+  cudaFreeAsync(E0, s);
+  cudaFreeAsync(E1, s);
+  cudaFreeAsync(X, s);
+  cudaFreeAsync(Y, s);
+  return rc;
+}
+
+}  // namespace
+
+// =================================================================================================
+extern "C" {
+
+const char* qr_last_error_string(void) { return t_err.c_str(); }
+
+int qr_version(int* major, int* minor) {
+  if (major) *major = 0;
+  if (minor) *minor = 1;
+  return QR_OK;
+}
+
+int qr_device_count(int* count) {
+  int c = 0;
+  cudaError_t e = cudaGetDeviceCount(&c);
+  if (count) *count = (e == cudaSuccess) ? c : 0;
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDeviceCount");
+  return QR_OK;
+}
+
+int qr_set_device(int device) {
+  QR_CUDA(cudaSetDevice(device));
+  return QR_OK;
+}
+
+int qr_launch_count(uint64_t* count) {
+  if (count) *count = g_launches.load();
+  return QR_OK;
+}
+
+int qr_chain_create(int n, int d, const int* bond_dims, qr_chain** out) {
+  if (!out) return fail(QR_EINVAL, "null output");
+  *out = nullptr;
+  if (n < 2) return fail(QR_EINVAL, "a Chain needs at least 2 sites");
+  if (d < 2 || d > 4) return fail(QR_EINVAL, "physical dimension must be 2..4");
+  for (int b = 0; b < n - 1; b++)
+    if (!bond_dims || bond_dims[b] < 1) return fail(QR_EINVAL, "bond dimensions must be >= 1");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(QR_ENODEV, "no CUDA device");
+  std::call_once(g_pool_once, init_pool);
+  qr_chain* h = new qr_chain();
+  h->n = n;
+  h->d = d;
+  h->bd.assign(bond_dims, bond_dims + n - 1);
+  h->site.assign(n, nullptr);
+  h->lam.assign(n - 1, nullptr);
+  h->lamlen.assign(n - 1, 0);
+  cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) { delete h; return cuda_fail(e, "cudaStreamCreate"); }
+  h->svd = svd_work_create();
+  int rc = dalloc((void**)&h->gate, sizeof(double2) * 256, h->stream);
+  if (!rc) rc = dalloc((void**)&h->scal, sizeof(double) * 16, h->stream);
+  for (int i = 0; i < n && !rc; i++) {
+    rc = dalloc((void**)&h->site[i], sizeof(double2) * h->elems(i), h->stream);
+    if (!rc) rc = cuda_ok(cudaMemsetAsync(h->site[i], 0, sizeof(double2) * h->elems(i), h->stream), "memset");
+  }
+  if (rc) { qr_chain_free(h); return rc; }
+  *out = h;
+  return QR_OK;
+}
+
+int qr_chain_free(qr_chain* h) {
+  if (!h) return QR_OK;
+  cudaStreamSynchronize(h->stream);
+  for (auto p : h->site) if (p) cudaFree(p);
+  for (auto p : h->lam) if (p) cudaFree(p);
+  if (h->gate) cudaFree(h->gate);
+  if (h->scal) cudaFree(h->scal);
+  if (h->ws) cudaFree(h->ws);
+  svd_work_free(h->svd);
+  cudaStreamDestroy(h->stream);
+  delete h;
+  return QR_OK;
+}
+
+int qr_chain_copy(const qr_chain* src, qr_chain** out) {
+  if (!src || !out) return fail(QR_EINVAL, "null chain");
+  QR_CUDA(cudaStreamSynchronize(src->stream));
+  QR_TRY(qr_chain_create(src->n, src->d, src->bd.data(), out));
+  qr_chain* h = *out;
+  h->precision = src->precision;
+  for (int i = 0; i < src->n; i++)
+    QR_CUDA(cudaMemcpyAsync(h->site[i], src->site[i], sizeof(double2) * src->elems(i), cudaMemcpyDeviceToDevice, h->stream));
+  for (int b = 0; b < src->n - 1; b++)
+    if (src->lam[b]) QR_TRY(put_lambda(h, b, src->lam[b], src->lamlen[b]));
+  return QR_OK;
+}
+
+int qr_chain_upload_site(qr_chain* h, int site, const double* host, const char* order) {
+  QR_TRY(check_site(h, site));
+  if (!host) return fail(QR_EINVAL, "null host array");
+  if (!is_perm(order ? order : "", "olr")) return fail(QR_EINVAL, "order must be a permutation of (o, l, r)");
+  std::string ho = filtered(order, site == 0, site == h->n - 1);
+  long idims[3] = {h->cl(site), h->d, h->cr(site)};
+  Perm p = make_perm(ho, "lor", idims);
+  size_t ne = h->elems(site);
+  QR_TRY(ensure_ws(h, ne));
+  QR_CUDA(cudaMemcpyAsync(h->ws, host, sizeof(double2) * ne, cudaMemcpyHostToDevice, h->stream));
+  QR_TRY(zpermute(h->stream, h->ws, h->site[site], p));
+  QR_CUDA(cudaStreamSynchronize(h->stream));
+  return QR_OK;
+}
+
+int qr_chain_download_site(const qr_chain* hc, int site, double* host, const char* order) {
+  qr_chain* h = const_cast<qr_chain*>(hc);
+  QR_TRY(check_site(h, site));
+  if (!host) return fail(QR_EINVAL, "null host array");
+  if (!is_perm(order ? order : "", "olr")) return fail(QR_EINVAL, "order must be a permutation of (o, l, r)");
+  std::string ho = filtered(order, site == 0, site == h->n - 1);
+  // dst (host order) gathers from the internal (l,o,r) layout: build the inverse map
+  long dims_by_letter[3] = {h->cl(site), h->d, h->cr(site)};  // l, o, r
+  const std::string iord = "lor";
+  long istride[3] = {1, dims_by_letter[0], dims_by_letter[0] * dims_by_letter[1]};
+  Perm p;
+  p.nd = (int)ho.size();
+  for (int k = 0; k < p.nd; k++) {
+    size_t q = iord.find(ho[k]);
+    p.dims[k] = dims_by_letter[q];
+    p.src_stride[k] = istride[q];
+  }
+  size_t ne = h->elems(site);
+  QR_TRY(ensure_ws(h, ne));
+  QR_TRY(zpermute(h->stream, h->site[site], h->ws, p));
+  QR_CUDA(cudaMemcpyAsync(host, h->ws, sizeof(double2) * ne, cudaMemcpyDeviceToHost, h->stream));
+  QR_CUDA(cudaStreamSynchronize(h->stream));
+  return QR_OK;
+}
+
+int qr_chain_site_dims(const qr_chain* h, int site, int* chi_l, int* d, int* chi_r) {
+  QR_TRY(check_site(h, site));
+  if (chi_l) *chi_l = h->cl(site);
+  if (d) *d = h->d;
+  if (chi_r) *chi_r = h->cr(site);
+  return QR_OK;
+}
+
+int qr_chain_bond_dims(const qr_chain* h, int* out) {
+  if (!h || !out) return fail(QR_EINVAL, "null argument");
+  for (int b = 0; b < h->n - 1; b++) out[b] = h->bd[b];
+  return QR_OK;
+}
+
+int qr_chain_has_lambda(const qr_chain* h, int bond, int* flag) {
+  if (!h || !flag || bond < 0 || bond >= h->n - 1) return fail(QR_EINVAL, "Invalid bond");
+  *flag = h->lam[bond] != nullptr;
+  return QR_OK;
+}
+
+int qr_chain_get_lambda(const qr_chain* h, int bond, double* out, int* len) {
+  if (!h || bond < 0 || bond >= h->n - 1) return fail(QR_EINVAL, "Invalid bond");
+  if (!h->lam[bond]) {
+    if (len) *len = 0;
+    return fail(QR_ENO_SCHMIDT, "Can't access the spectrum on bond");
+  }
+  if (len) *len = h->lamlen[bond];
+  if (out) {
+    QR_CUDA(cudaMemcpyAsync(out, h->lam[bond], sizeof(double) * h->lamlen[bond], cudaMemcpyDeviceToHost, h->stream));
+    QR_CUDA(cudaStreamSynchronize(h->stream));
+  }
+  return QR_OK;
+}
+
+int qr_chain_set_lambda(qr_chain* h, int bond, const double* lam, int len) {
+  if (!h || bond < 0 || bond >= h->n - 1) return fail(QR_EINVAL, "Invalid bond");
+  if (!lam) { drop_lambda(h, bond); return QR_OK; }
+  if (len != h->bd[bond]) return fail(QR_EDIM, "Lambda length must equal the bond dimension");
+  double* p = nullptr;
+  QR_TRY(dalloc((void**)&p, sizeof(double) * len, h->stream));
+  QR_CUDA(cudaMemcpyAsync(p, lam, sizeof(double) * len, cudaMemcpyHostToDevice, h->stream));
+  QR_CUDA(cudaStreamSynchronize(h->stream));
+  drop_lambda(h, bond);
+  h->lam[bond] = p;
+  h->lamlen[bond] = len;
+  return QR_OK;
+}
+
+int qr_chain_ntensors(const qr_chain* h, int* out) {
+  if (!h || !out) return fail(QR_EINVAL, "null argument");
+  int c = h->n;
+  for (auto p : h->lam) c += (p != nullptr);
+  *out = c;
+  return QR_OK;
+}
+
+int qr_chain_nsites(const qr_chain* h, int* out) {
+  if (!h || !out) return fail(QR_EINVAL, "null argument");
+  *out = h->n;
+  return QR_OK;
+}
+
+int qr_chain_set_precision(qr_chain* h, int mode) {
+  if (!h) return fail(QR_EINVAL, "null chain");
+  if (mode != QR_FP64 && mode != QR_MIXED) return fail(QR_EINVAL, "precision must be QR_FP64 or QR_MIXED");
+  h->precision = mode;
+  return QR_OK;
+}
+
+int qr_chain_get_precision(const qr_chain* h, int* mode) {
+  if (!h || !mode) return fail(QR_EINVAL, "null argument");
+  *mode = h->precision;
+  return QR_OK;
+}
+
+int qr_chain_stream(const qr_chain* h, void** stream) {
+  if (!h || !stream) return fail(QR_EINVAL, "null argument");
+  *stream = (void*)h->stream;
+  return QR_OK;
+}
+
+int qr_chain_sync(const qr_chain* h) {
+  if (!h) return fail(QR_EINVAL, "null chain");
+  QR_CUDA(cudaStreamSynchronize(h->stream));
+  return QR_OK;
+}
+
+int qr_canonize_site(qr_chain* h, int site, int direction, int method) {
+  QR_TRY(canonize_site_impl(h, site, direction, method));
+  QR_CUDA(cudaStreamSynchronize(h->stream));
+  return QR_OK;
+}
+
+// canonize! (Chain.jl:469-497)
+int qr_canonize(qr_chain* h) {
+  if (!h) return fail(QR_EINVAL, "null chain");
+  const int n = h->n;
+  for (int i = n - 1; i >= 1; i--) QR_TRY(canonize_site_impl(h, i, QR_DIR_LEFT, QR_METHOD_QR));
+  std::vector<double*> lams(n - 1, nullptr);
+  std::vector<int> lens(n - 1, 0);
+  for (int i = 0; i < n - 1; i++) {
+    QR_TRY(canonize_site_impl(h, i, QR_DIR_RIGHT, QR_METHOD_SVD));
+    // pop Lambda_i and absorb it into A_{i+1}
+    lams[i] = h->lam[i];
+    lens[i] = h->lamlen[i];
+    h->lam[i] = nullptr;
+    h->lamlen[i] = 0;
+    QR_TRY(scale_site_by_lambda(h, i + 1, 0, lams[i], 0, 0.0));
+  }
+  for (int i = 1; i < n; i++) {
+    QR_TRY(scale_site_by_lambda(h, i, 0, lams[i - 1], 1, 1e-64));
+    h->lam[i - 1] = lams[i - 1];
+    h->lamlen[i - 1] = lens[i - 1];
+  }
+  QR_CUDA(cudaStreamSynchronize(h->stream));
+  return QR_OK;
+}
+
+int qr_mixed_canonize(qr_chain* h, int center) {
+  QR_TRY(mixed_canonize_impl(h, center));
+  QR_CUDA(cudaStreamSynchronize(h->stream));
+  return QR_OK;
+}
+
+int qr_normalize(qr_chain* h, int root) {
+  QR_TRY(normalize_impl(h, root));
+  QR_CUDA(cudaStreamSynchronize(h->stream));
+  return QR_OK;
+}
+
+// contract!(::Chain, Val(:between)) (Chain.jl:309-333)
+int qr_contract_between(qr_chain* h, int site1, int site2, int direction, int delete_lambda) {
+  QR_TRY(check_site(h, site1));
+  QR_TRY(check_site(h, site2));
+  if (site2 != site1 + 1) return fail(QR_EINVAL, "sites must be adjacent");
+  const int b = site1;
+  if (!h->lam[b]) return QR_OK;
+  if (direction == QR_DIR_RIGHT) {
+    QR_TRY(scale_site_by_lambda(h, site2, 0, h->lam[b], 0, 0.0));
+  } else if (direction == QR_DIR_LEFT) {
+    QR_TRY(scale_site_by_lambda(h, site1, 2, h->lam[b], 0, 0.0));
+  } else {
+    return fail(QR_EINVAL, "Unknown direction");
+  }
+  if (delete_lambda) drop_lambda(h, b);
+  QR_CUDA(cudaStreamSynchronize(h->stream));
+  return QR_OK;
+}
+
+int qr_canonicality_error(const qr_chain* hc, int site, int direction, double* err) {
+  qr_chain* h = const_cast<qr_chain*>(hc);
+  QR_TRY(check_site(h, site));
+  if (!err) return fail(QR_EINVAL, "null output");
+  cudaStream_t s = h->stream;
+  const int cl = h->cl(site), d = h->d, cr = h->cr(site);
+  const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
+  int nn = (direction == QR_DIR_LEFT) ? cr : cl;
+  QR_TRY(ensure_ws(h, (size_t)nn * nn));
+  if (direction == QR_DIR_LEFT) {  // A^H A over [(l,o) x r]
+    QR_TRY(zgemm(s, OP_C, OP_N, cr, cr, cl * d, one, h->site[site], cl * d, 0, h->site[site], cl * d, 0, zero, h->ws, cr, 0, 1, nullptr));
+  } else {  // A A^H over [l x (o,r)]
+    QR_TRY(zgemm(s, OP_N, OP_C, cl, cl, d * cr, one, h->site[site], cl, 0, h->site[site], cl, 0, zero, h->ws, cl, 0, 1, nullptr));
+  }
+  QR_TRY(zdist_identity(s, h->ws, nn, h->scal));
+  QR_CUDA(cudaMemcpyAsync(err, h->scal, sizeof(double), cudaMemcpyDeviceToHost, s));
+  QR_CUDA(cudaStreamSynchronize(s));
+  return QR_OK;
+}
+
+int qr_truncate(qr_chain* h, int site1, int site2, double threshold, int maxdim) {
+  QR_TRY(truncate_impl(h, site1, site2, threshold, maxdim));
+  QR_CUDA(cudaStreamSynchronize(h->stream));
+  return QR_OK;
+}
+
+// evolve_1site! (Chain.jl:586-603)
+int qr_evolve_1site(qr_chain* h, int site, const double* gate) {
+  QR_TRY(check_site(h, site));
+  if (!gate) return fail(QR_EINVAL, "null gate");
+  QR_TRY(upload_gate(h, gate, h->d));
+  QR_TRY(zgate1(h->stream, h->site[site], h->cl(site), h->d, h->cr(site), h->gate));
+  QR_CUDA(cudaStreamSynchronize(h->stream));
+  return QR_OK;
+}
+
+int qr_evolve_2site(qr_chain* h, int site_l, const double* gate, double threshold, int maxdim, int iscanonical,
+                    int renormalize) {
+  if (!gate) return fail(QR_EINVAL, "null gate");
+  QR_TRY(evolve2_impl(h, site_l, gate, threshold, maxdim, iscanonical, renormalize));
+  QR_CUDA(cudaStreamSynchronize(h->stream));
+  return QR_OK;
+}
+
+int qr_overlap(const qr_chain* a, const qr_chain* b, double* out) {
+  if (!a || !b || !out) return fail(QR_EINVAL, "null argument");
+  if (a->n != b->n || a->d != b->d) return fail(QR_EASSERT, "Ansatzes must have the same sites");
+  QR_CUDA(cudaStreamSynchronize(b->stream));
+  return env_sweep(a, b, nullptr, a->stream, out);
+}
+
+int qr_norm(const qr_chain* h, double* out) {
+  if (!h || !out) return fail(QR_EINVAL, "null argument");
+  double z[2];
+  QR_TRY(env_sweep(h, h, nullptr, h->stream, z));
+  *out = std::abs(std::sqrt(std::complex<double>(z[0], z[1])));
+  return QR_OK;
+}
+
+// expect (Chain.jl:724-735): the product operator O_{k-1}...O_0 is built as a small MPO on the
+// host (bond dimension d^2 per two-site observable) and contracted in one environment sweep.
+int qr_expect(const qr_chain* h, int nobs, const int* first, const int* nlanes, const double* mats, double* out) {
+  if (!h || !out) return fail(QR_EINVAL, "null argument");
+  if (nobs < 0 || (nobs > 0 && (!first || !nlanes || !mats))) return fail(QR_EINVAL, "bad observable list");
+  const int n = h->n, d = h->d;
+  typedef std::complex<double> cd;
+  // per-site operator tensors (wl, o, i, wr), wl fastest
+  std::vector<std::vector<cd>> W(n);
+  std::vector<int> wl(n, 1), wr(n, 1);
+  for (int i = 0; i < n; i++) {
+    W[i].assign(d * d, cd(0));
+    for (int o = 0; o < d; o++) W[i][o + d * o] = cd(1);
+  }
+  std::vector<bool> touched(n, false);
+  size_t off = 0;
+  for (int j = 0; j < nobs; j++) {
+    const int s0 = first[j], nl = nlanes[j];
+    if (nl != 1 && nl != 2) return fail(QR_EINVAL, "Invalid number of lanes, maximum is 2");
+    if (s0 < 0 || s0 + nl > n) return fail(QR_EINVAL, "Gate inputs must be a subset of the TN sites");
+    const int dim = nl == 1 ? d : d * d;
+    const cd* G = reinterpret_cast<const cd*>(mats) + off;
+    off += (size_t)dim * dim;
+    if (nl == 1) {
+      const int s = s0, a = wl[s], b = wr[s];
+      std::vector<cd> nw(W[s].size(), cd(0));
+      for (int w2 = 0; w2 < b; w2++)
+        for (int i = 0; i < d; i++)
+          for (int o = 0; o < d; o++)
+            for (int w = 0; w < a; w++) {
+              cd acc(0);
+              for (int mm = 0; mm < d; mm++) acc += G[o * d + mm] * W[s][w + a * (mm + d * (i + d * w2))];
+              nw[w + a * (o + d * (i + d * w2))] = acc;
+            }
+      W[s] = nw;
+      touched[s] = true;
+    } else {
+      // G[(o1,o2),(m1,m2)] = sum_{t=(p,c)} |p><c| (x) R_t,  R_t[o2,m2] = G[(p,o2),(c,m2)]
+      const int s = s0, s2 = s0 + 1;
+      const int a1 = wl[s], b1 = wr[s], a2 = wl[s2], b2 = wr[s2];
+      const int T = d * d;
+      std::vector<cd> n1((size_t)a1 * d * d * b1 * T, cd(0));
+      for (int t = 0; t < T; t++) {
+        const int p = t % d, c = t / d;
+        for (int w2 = 0; w2 < b1; w2++)
+          for (int i = 0; i < d; i++)
+            for (int w = 0; w < a1; w++)
+              n1[w + a1 * (p + d * (i + d * (w2 + b1 * t)))] = W[s][w + a1 * (c + d * (i + d * w2))];
+      }
+      std::vector<cd> n2((size_t)a2 * T * d * d * b2, cd(0));
+      for (int t = 0; t < T; t++) {
+        const int p = t % d, c = t / d;
+        for (int w2 = 0; w2 < b2; w2++)
+          for (int i = 0; i < d; i++)
+            for (int o2 = 0; o2 < d; o2++)
+              for (int w = 0; w < a2; w++) {
+                cd acc(0);
+                for (int m2 = 0; m2 < d; m2++)
+                  acc += G[(p * d + o2) * T + (c * d + m2)] * W[s2][w + a2 * (m2 + d * (i + d * w2))];
+                n2[(w + a2 * t) + (a2 * T) * (o2 + d * (i + d * w2))] = acc;
+              }
+      }
+      W[s] = n1;
+      W[s2] = n2;
+      wr[s] = b1 * T;
+      wl[s2] = a2 * T;
+      touched[s] = touched[s2] = true;
+    }
+  }
+  EnvOps ops;
+  ops.W.assign(n, nullptr);
+  ops.wl = wl;
+  ops.wr = wr;
+  std::vector<double2*> dev(n, nullptr);
+  int rc = QR_OK;
+  for (int i = 0; i < n && !rc; i++) {
+    if (!touched[i]) continue;
+    rc = dalloc((void**)&dev[i], sizeof(double2) * W[i].size(), h->stream);
+    if (!rc) rc = cuda_ok(cudaMemcpyAsync(dev[i], W[i].data(), sizeof(double2) * W[i].size(), cudaMemcpyHostToDevice, h->stream), "memcpy");
+    ops.W[i] = dev[i];
+  }
+  if (!rc) rc = env_sweep(h, h, &ops, h->stream, out);
+  cudaStreamSynchronize(h->stream);
+  for (auto p : dev) if (p) cudaFreeAsync(p, h->stream);
+  return rc;
+}
+
+int qr_mpo_create(int n, int d, const int* bond_dims, qr_mpo** out) {
+  if (!out) return fail(QR_EINVAL, "null output");
+  *out = nullptr;
+  if (n < 2 || d < 2 || d > 4 || !bond_dims) return fail(QR_EINVAL, "bad MPO shape");
+  qr_mpo* w = new qr_mpo();
+  w->n = n;
+  w->d = d;
+  w->bd.assign(bond_dims, bond_dims + n - 1);
+  w->site.assign(n, nullptr);
+  for (int i = 0; i < n; i++) {
+    size_t ne = (size_t)w->wl(i) * d * d * w->wr(i);
+    if (cudaMalloc(&w->site[i], sizeof(double2) * ne) != cudaSuccess) { qr_mpo_free(w); return fail(QR_ENOMEM, "MPO allocation"); }
+    cudaMemset(w->site[i], 0, sizeof(double2) * ne);
+  }
+  *out = w;
+  return QR_OK;
+}
+
+int qr_mpo_free(qr_mpo* w) {
+  if (!w) return QR_OK;
+  for (auto p : w->site) if (p) cudaFree(p);
+  delete w;
+  return QR_OK;
+}
+
+int qr_mpo_upload_site(qr_mpo* w, int site, const double* host, const char* order) {
+  if (!w || site < 0 || site >= w->n || !host) return fail(QR_EINVAL, "bad MPO site");
+  if (!is_perm(order ? order : "", "oilr")) return fail(QR_EINVAL, "order must be a permutation of (o, i, l, r)");
+  std::string ho = filtered(order, site == 0, site == w->n - 1);
+  long idims[4] = {w->wl(site), w->d, w->d, w->wr(site)};
+  Perm p = make_perm(ho, "loir", idims);
+  size_t ne = (size_t)idims[0] * idims[1] * idims[2] * idims[3];
+  double2* tmp = nullptr;
+  QR_CUDA(cudaMalloc(&tmp, sizeof(double2) * ne));
+  cudaError_t e = cudaMemcpy(tmp, host, sizeof(double2) * ne, cudaMemcpyHostToDevice);
+  int rc = (e == cudaSuccess) ? zpermute(0, tmp, w->site[site], p) : cuda_fail(e, "cudaMemcpy");
+  cudaDeviceSynchronize();
+  cudaFree(tmp);
+  return rc;
+}
+
+int qr_mpo_expect(const qr_chain* h, const qr_mpo* w, double* out) {
+  if (!h || !w || !out) return fail(QR_EINVAL, "null argument");
+  if (w->n != h->n || w->d != h->d) return fail(QR_EASSERT, "Outputs of the state must match inputs of the operator");
+  EnvOps ops;
+  ops.W.assign(w->site.begin(), w->site.end());
+  ops.wl.resize(h->n);
+  ops.wr.resize(h->n);
+  for (int i = 0; i < h->n; i++) { ops.wl[i] = w->wl(i); ops.wr[i] = w->wr(i); }
+  return env_sweep(h, h, &ops, h->stream, out);
+}
+
+}  // extern "C"

@@ -1,0 +1,62 @@
+// Shared device/host helpers for the qrochet GB300 library.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <cmath>
+#include <string>
+#include <atomic>
+
+#include "../../include/qrochet_gpu.h"
+
+namespace qr {
+
+// ---- complex arithmetic on CUDA vector types (re = .x, im = .y) ------------------------------
+template <typename T> struct cplx;
+template <> struct cplx<double> { using type = double2; };
+template <> struct cplx<float> { using type = float2; };
+template <typename T> using cplx_t = typename cplx<T>::type;
+
+__host__ __device__ inline double2 mk(double r, double i) { return make_double2(r, i); }
+__host__ __device__ inline float2 mk(float r, float i) { return make_float2(r, i); }
+template <typename C> __host__ __device__ inline C cadd(C a, C b) { C r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
+template <typename C> __host__ __device__ inline C csub(C a, C b) { C r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+template <typename C> __host__ __device__ inline C cmul(C a, C b) {
+  C r; r.x = a.x * b.x - a.y * b.y; r.y = a.x * b.y + a.y * b.x; return r;
+}
+// conj(a) * b
+template <typename C> __host__ __device__ inline C cmulc(C a, C b) {
+  C r; r.x = a.x * b.x + a.y * b.y; r.y = a.x * b.y - a.y * b.x; return r;
+}
+template <typename C> __host__ __device__ inline C cconj(C a) { C r; r.x = a.x; r.y = -a.y; return r; }
+template <typename C, typename T> __host__ __device__ inline C cscale(C a, T s) { C r; r.x = a.x * s; r.y = a.y * s; return r; }
+
+// ---- error plumbing ----------------------------------------------------------------------------
+void set_error(const std::string& msg);
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+
+extern std::atomic<uint64_t> g_launches;
+inline void count_launch(uint64_t n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+#define QR_CUDA(call)                                        \
+  do {                                                       \
+    cudaError_t _e = (call);                                 \
+    if (_e != cudaSuccess) return ::qr::cuda_fail(_e, #call); \
+  } while (0)
+
+#define QR_CHECK_LAUNCH(what)                                   \
+  do {                                                          \
+    ::qr::count_launch();                                       \
+    cudaError_t _e = cudaGetLastError();                        \
+    if (_e != cudaSuccess) return ::qr::cuda_fail(_e, what);    \
+  } while (0)
+
+#define QR_TRY(expr)              \
+  do {                            \
+    int _s = (expr);              \
+    if (_s != QR_OK) return _s;   \
+  } while (0)
+
+inline unsigned ceil_div(long a, long b) { return (unsigned)((a + b - 1) / b); }
+
+}  // namespace qr

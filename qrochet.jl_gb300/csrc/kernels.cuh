@@ -1,0 +1,58 @@
+// Internal launch wrappers of the qrochet GB300 library (all enqueue on the given stream).
+#pragma once
+#include "common.cuh"
+
+namespace qr {
+
+enum { OP_N = 0, OP_T = 1, OP_C = 2, OP_R = 3 };
+
+// ---- gemm.cu -----------------------------------------------------------------------------------
+int zgemm(cudaStream_t s, int opA, int opB, int M, int N, int K, double2 alpha,
+          const double2* A, long lda, long sA, const double2* B, long ldb, long sB,
+          double2 beta, double2* C, long ldc, long sC, int batch, const double* dk);
+
+// ---- misc.cu -----------------------------------------------------------------------------------
+int zscale_matrix(cudaStream_t s, int M, int N, double2 alpha, double2* C, long ldc, long sC,
+                  int batch);
+// dst (column-major, dims dst_dims[0..nd)) gathers src through per-dst-dim source strides
+struct Perm {
+  int nd;
+  long dims[4];
+  long src_stride[4];
+};
+int zpermute(cudaStream_t s, const double2* src, double2* dst, const Perm& p);
+// A[l,o,r] *= f(lam[l]) (side 0) or f(lam[r]) (side 2); f = x, or pinv with atol when inv
+int zscale_bond(cudaStream_t s, double2* A, int cl, int d, int cr, const double* lam, int side,
+                int inv, double atol);
+// A[l,o',r] = sum_o G[o',o] A[l,o,r], G row-major d x d in device memory
+int zgate1(cudaStream_t s, double2* A, int cl, int d, int cr, const double2* G);
+// theta[(l,o1),(o2,r)] (ld cl*d) <- G[(o1',o2'),(o1,o2)] theta, G row-major d^2 x d^2 (device)
+int zgate2(cudaStream_t s, double2* theta, int cl, int d, int cr, const double2* G);
+// dst[j + i*ldd] = op(src[i + j*lds]) for i<rows, j<cols (transpose, optional conjugate)
+int ztranspose(cudaStream_t s, const double2* src, long lds, int rows, int cols, double2* dst,
+               long ldd, int conj);
+int zset_identity(cudaStream_t s, double2* A, int rows, int cols, long lda);
+int cset_identity(cudaStream_t s, float2* A, int rows, int cols, long lda);
+int z2c(cudaStream_t s, const double2* src, long lds, float2* dst, long ldd, int rows, int cols);
+int c2z(cudaStream_t s, const float2* src, long lds, double2* dst, long ldd, int rows, int cols);
+// out[0] = || G - I ||_F for the n x n matrix G (ld n); out is device memory
+int zdist_identity(cudaStream_t s, const double2* G, int n, double* out);
+// lam[i] /= norm2(lam) in place (device)
+int dnormalize(cudaStream_t s, double* lam, int len);
+
+// ---- qr.cu -------------------------------------------------------------------------------------
+// Thin Householder QR of the m x n matrix A (ld lda, overwritten).  Q: m x k (ld ldq) and
+// R: k x n (ld ldr), k = min(m, n).  tau: device workspace of k entries.
+int zqr_thin(cudaStream_t s, double2* A, int m, int n, long lda, double2* Q, long ldq,
+             double2* R, long ldr, double2* tau);
+
+// ---- svd.cu ------------------------------------------------------------------------------------
+struct SvdWork;  // opaque, grows on demand
+SvdWork* svd_work_create();
+void svd_work_free(SvdWork* w);
+// Thin SVD of the m x n matrix A (ld lda; A is preserved).  U: m x k (ld ldu), S: k (device),
+// Vh: k x n (ld ldvh), k = min(m,n), S descending.  mode: QR_FP64 or QR_MIXED.
+int zsvd_thin(cudaStream_t s, SvdWork* w, int mode, const double2* A, int m, int n, long lda,
+              double2* U, long ldu, double* S, double2* Vh, long ldvh);
+
+}  // namespace qr

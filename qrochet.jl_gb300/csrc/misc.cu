@@ -1,0 +1,263 @@
+// Memory-bound kernels of the Chain path: layout permutes at the host boundary, bond scaling by
+// Lambda (and its pseudo-inverse), physical-index gates, transposes, precision conversions.
+// All are grid-stride loops over the output with coalesced writes.
+#include "kernels.cuh"
+
+namespace qr {
+
+namespace {
+
+constexpr int TPB = 256;
+
+inline unsigned grid_for(long n) {
+  long g = (n + TPB - 1) / TPB;
+  if (g > 152L * 32) g = 152L * 32;  // grid-stride beyond 32 CTAs per SM
+  return (unsigned)(g < 1 ? 1 : g);
+}
+
+__global__ void scale_matrix_k(int M, int N, double2 alpha, double2* C, long ldc, long sC) {
+  C += blockIdx.y * sC;
+  long total = (long)M * N;
+  const bool zero = (alpha.x == 0.0 && alpha.y == 0.0);
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+    long i = t % M, j = t / M;
+    double2* p = C + i + j * ldc;
+    *p = zero ? make_double2(0.0, 0.0) : cmul(alpha, *p);
+  }
+}
+
+__global__ void permute_k(const double2* __restrict__ src, double2* __restrict__ dst, Perm p, long total) {
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+    long rem = t, off = 0;
+    for (int k = 0; k < p.nd; k++) {
+      long c = rem % p.dims[k];
+      rem /= p.dims[k];
+      off += c * p.src_stride[k];
+    }
+    dst[t] = src[off];
+  }
+}
+
+__global__ void scale_bond_k(double2* A, int cl, int d, int cr, const double* __restrict__ lam,
+                             int side, int inv, double atol) {
+  long total = (long)cl * d * cr;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+    long idx = (side == 0) ? (t % cl) : (t / ((long)cl * d));
+    double x = lam[idx];
+    double f = inv ? ((fabs(x) > atol) ? 1.0 / x : 0.0) : x;
+    A[t] = cscale(A[t], f);
+  }
+}
+
+__global__ void gate1_k(double2* A, int cl, int d, int cr, const double2* __restrict__ G) {
+  long pairs = (long)cl * cr;
+  double2 in[8];
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < pairs; t += (long)gridDim.x * blockDim.x) {
+    long l = t % cl, r = t / cl;
+    double2* base = A + l + (long)cl * d * r;
+    for (int o = 0; o < d; o++) in[o] = base[(long)cl * o];
+    for (int o2 = 0; o2 < d; o2++) {
+      double2 acc = make_double2(0.0, 0.0);
+      for (int o = 0; o < d; o++) acc = cadd(acc, cmul(G[o2 * d + o], in[o]));
+      base[(long)cl * o2] = acc;
+    }
+  }
+}
+
+// theta rows (l + cl*o1), cols (o2 + d*r), ld = cl*d
+__global__ void gate2_k(double2* th, int cl, int d, int cr, const double2* __restrict__ G) {
+  long pairs = (long)cl * cr;
+  const long ld = (long)cl * d;
+  double2 in[16];
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < pairs; t += (long)gridDim.x * blockDim.x) {
+    long l = t % cl, r = t / cl;
+    for (int a = 0; a < d; a++)
+      for (int b = 0; b < d; b++) in[a * d + b] = th[(l + (long)cl * a) + (b + (long)d * r) * ld];
+    for (int a2 = 0; a2 < d; a2++)
+      for (int b2 = 0; b2 < d; b2++) {
+        double2 acc = make_double2(0.0, 0.0);
+        const double2* g = G + (a2 * d + b2) * d * d;
+        for (int q = 0; q < d * d; q++) acc = cadd(acc, cmul(g[q], in[q]));
+        th[(l + (long)cl * a2) + (b2 + (long)d * r) * ld] = acc;
+      }
+  }
+}
+
+__global__ void transpose_k(const double2* __restrict__ src, long lds, int rows, int cols,
+                            double2* __restrict__ dst, long ldd, int conj) {
+  __shared__ double2 tile[32][33];
+  int i0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    int i = i0 + threadIdx.x, j = j0 + k;
+    if (i < rows && j < cols) tile[k][threadIdx.x] = src[i + (long)j * lds];
+  }
+  __syncthreads();
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    int j = j0 + threadIdx.x, i = i0 + k;  // dst[j + i*ldd] = src[i + j*lds]
+    if (i < rows && j < cols) {
+      double2 v = tile[threadIdx.x][k];
+      if (conj) v.y = -v.y;
+      dst[j + (long)i * ldd] = v;
+    }
+  }
+}
+
+template <typename C>
+__global__ void identity_k(C* A, int rows, int cols, long lda) {
+  long total = (long)rows * cols;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+    long i = t % rows, j = t / rows;
+    C v; v.x = (i == j) ? 1 : 0; v.y = 0;
+    A[i + j * lda] = v;
+  }
+}
+
+__global__ void z2c_k(const double2* __restrict__ s, long lds, float2* __restrict__ d, long ldd, int rows, int cols) {
+  long total = (long)rows * cols;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+    long i = t % rows, j = t / rows;
+    double2 v = s[i + j * lds];
+    d[i + j * ldd] = make_float2((float)v.x, (float)v.y);
+  }
+}
+
+__global__ void c2z_k(const float2* __restrict__ s, long lds, double2* __restrict__ d, long ldd, int rows, int cols) {
+  long total = (long)rows * cols;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+    long i = t % rows, j = t / rows;
+    float2 v = s[i + j * lds];
+    d[i + j * ldd] = make_double2((double)v.x, (double)v.y);
+  }
+}
+
+__device__ double block_sum(double v) {
+  __shared__ double red[32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  v = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
+  if (w == 0)
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;  // valid in thread 0
+}
+
+__global__ void dist_identity_k(const double2* G, int n, double* out) {
+  double acc = 0.0;
+  long total = (long)n * n;
+  for (long t = threadIdx.x; t < total; t += blockDim.x) {
+    long i = t % n, j = t / n;
+    double2 v = G[t];
+    double re = v.x - (i == j ? 1.0 : 0.0);
+    acc += re * re + v.y * v.y;
+  }
+  acc = block_sum(acc);
+  if (threadIdx.x == 0) out[0] = sqrt(acc);
+}
+
+__global__ void dnormalize_k(double* lam, int len) {
+  double acc = 0.0;
+  for (int t = threadIdx.x; t < len; t += blockDim.x) acc += lam[t] * lam[t];
+  acc = block_sum(acc);
+  __shared__ double nrm;
+  if (threadIdx.x == 0) nrm = sqrt(acc);
+  __syncthreads();
+  for (int t = threadIdx.x; t < len; t += blockDim.x) lam[t] = lam[t] / nrm;
+}
+
+}  // namespace
+
+int zscale_matrix(cudaStream_t s, int M, int N, double2 alpha, double2* C, long ldc, long sC, int batch) {
+  if (M <= 0 || N <= 0 || batch <= 0) return QR_OK;
+  dim3 g(grid_for((long)M * N), batch);
+  scale_matrix_k<<<g, TPB, 0, s>>>(M, N, alpha, C, ldc, sC);
+  QR_CHECK_LAUNCH("scale_matrix_k");
+  return QR_OK;
+}
+
+int zpermute(cudaStream_t s, const double2* src, double2* dst, const Perm& p) {
+  long total = 1;
+  for (int k = 0; k < p.nd; k++) total *= p.dims[k];
+  if (total == 0) return QR_OK;
+  permute_k<<<grid_for(total), TPB, 0, s>>>(src, dst, p, total);
+  QR_CHECK_LAUNCH("permute_k");
+  return QR_OK;
+}
+
+int zscale_bond(cudaStream_t s, double2* A, int cl, int d, int cr, const double* lam, int side, int inv, double atol) {
+  long total = (long)cl * d * cr;
+  if (total == 0) return QR_OK;
+  scale_bond_k<<<grid_for(total), TPB, 0, s>>>(A, cl, d, cr, lam, side, inv, atol);
+  QR_CHECK_LAUNCH("scale_bond_k");
+  return QR_OK;
+}
+
+int zgate1(cudaStream_t s, double2* A, int cl, int d, int cr, const double2* G) {
+  if (d > 8) return fail(QR_EINVAL, "physical dimension above 8 is not supported");
+  long pairs = (long)cl * cr;
+  if (pairs == 0) return QR_OK;
+  gate1_k<<<grid_for(pairs), TPB, 0, s>>>(A, cl, d, cr, G);
+  QR_CHECK_LAUNCH("gate1_k");
+  return QR_OK;
+}
+
+int zgate2(cudaStream_t s, double2* th, int cl, int d, int cr, const double2* G) {
+  if (d > 4) return fail(QR_EINVAL, "two-site gates need physical dimension <= 4");
+  long pairs = (long)cl * cr;
+  if (pairs == 0) return QR_OK;
+  gate2_k<<<grid_for(pairs), TPB, 0, s>>>(th, cl, d, cr, G);
+  QR_CHECK_LAUNCH("gate2_k");
+  return QR_OK;
+}
+
+int ztranspose(cudaStream_t s, const double2* src, long lds, int rows, int cols, double2* dst, long ldd, int conj) {
+  if (rows <= 0 || cols <= 0) return QR_OK;
+  dim3 g(ceil_div(rows, 32), ceil_div(cols, 32)), b(32, 8);
+  transpose_k<<<g, b, 0, s>>>(src, lds, rows, cols, dst, ldd, conj);
+  QR_CHECK_LAUNCH("transpose_k");
+  return QR_OK;
+}
+
+int zset_identity(cudaStream_t s, double2* A, int rows, int cols, long lda) {
+  if (rows <= 0 || cols <= 0) return QR_OK;
+  identity_k<double2><<<grid_for((long)rows * cols), TPB, 0, s>>>(A, rows, cols, lda);
+  QR_CHECK_LAUNCH("identity_k");
+  return QR_OK;
+}
+
+int cset_identity(cudaStream_t s, float2* A, int rows, int cols, long lda) {
+  if (rows <= 0 || cols <= 0) return QR_OK;
+  identity_k<float2><<<grid_for((long)rows * cols), TPB, 0, s>>>(A, rows, cols, lda);
+  QR_CHECK_LAUNCH("identity_k");
+  return QR_OK;
+}
+
+int z2c(cudaStream_t s, const double2* src, long lds, float2* dst, long ldd, int rows, int cols) {
+  if (rows <= 0 || cols <= 0) return QR_OK;
+  z2c_k<<<grid_for((long)rows * cols), TPB, 0, s>>>(src, lds, dst, ldd, rows, cols);
+  QR_CHECK_LAUNCH("z2c_k");
+  return QR_OK;
+}
+
+int c2z(cudaStream_t s, const float2* src, long lds, double2* dst, long ldd, int rows, int cols) {
+  if (rows <= 0 || cols <= 0) return QR_OK;
+  c2z_k<<<grid_for((long)rows * cols), TPB, 0, s>>>(src, lds, dst, ldd, rows, cols);
+  QR_CHECK_LAUNCH("c2z_k");
+  return QR_OK;
+}
+
+int zdist_identity(cudaStream_t s, const double2* G, int n, double* out) {
+  dist_identity_k<<<1, 1024, 0, s>>>(G, n, out);
+  QR_CHECK_LAUNCH("dist_identity_k");
+  return QR_OK;
+}
+
+int dnormalize(cudaStream_t s, double* lam, int len) {
+  if (len <= 0) return QR_OK;
+  dnormalize_k<<<1, 1024, 0, s>>>(lam, len);
+  QR_CHECK_LAUNCH("dnormalize_k");
+  return QR_OK;
+}
+
+}  // namespace qr

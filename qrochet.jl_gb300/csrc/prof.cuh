@@ -1,0 +1,13 @@
+// Opt-in per-kernel-class event timing (see prof.cu).
+#pragma once
+#include "common.cuh"
+
+namespace qr {
+enum ProfKind { PK_ZGEMM = 0, PK_JACOBI64 = 1, PK_JACOBI32 = 2, PK_QR = 3, PK_ENV = 4, PK_COUNT = 5 };
+bool prof_on();
+// returns a record index (or -1 when profiling is off); pair with prof_end on the same stream
+int prof_begin(cudaStream_t s, int kind, double flops, double bytes);
+void prof_end(cudaStream_t s, int idx);
+// set the work of a record after the fact (flops/bytes known only once the launches ran)
+void prof_account(int idx, double flops, double bytes);
+}  // namespace qr

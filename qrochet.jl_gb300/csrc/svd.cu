@@ -1,0 +1,404 @@
+// Thin complex SVD for canonize_site!(...; method=:svd) and evolve_2site!'s bond compression.
+//
+// QR_FP64 (plain): one-sided (Hestenes) Jacobi in FP64.  Columns of B = A (or A^H when A is
+// wide) are rotated pairwise until mutually orthogonal: B V = U Sigma.  Pairs follow the
+// round-robin (circle) ordering, so each round is n/2 independent pair rotations, one warp per
+// pair.  Converged when no pair has |b_p^H b_q| > tol sqrt(|b_p|^2 |b_q|^2), tol = sqrt(m) eps.
+//
+// QR_MIXED: the same Jacobi in FP32 (FFMA runs ~70x faster than DFMA on GB300) gives
+// approximate right singular vectors X; then FP64 refinement on the DMMA GEMM (Ogita & Aishima,
+// "Iterative refinement for symmetric eigenvalue decomposition", 2018, applied to A^H A):
+//     R = I - X^H X,  B = A X,  S = B^H B,  lt_i = S_ii / (1 - R_ii),
+//     E_ij = (S_ij + lt_j R_ij) / (lt_j - lt_i)   (i != j, separated pairs),  E_ij = R_ij / 2
+//     otherwise,  X <- X (I + E).
+// Each step squares the error of separated pairs, so two steps take FP32 accuracy to FP64.
+// Sigma = column norms of A X in FP64, so singular values and the truncation cutoff are FP64.
+//
+// Left singular vectors are the normalised columns B/sigma.  When the spectrum spans many
+// decades (or has exact zeros) those columns lose orthogonality in proportion to
+// sigma_max/sigma_j; they are then re-orthonormalised with a Householder QR, keeping each
+// column's phase, which moves the represented matrix by O(eps sigma_max) only.
+#include <vector>
+#include <algorithm>
+#include "kernels.cuh"
+#include "prof.cuh"
+
+namespace qr {
+
+struct DBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  int ensure(size_t bytes, cudaStream_t s) {
+    if (bytes <= cap) return QR_OK;
+    if (p) cudaFreeAsync(p, s);
+    p = nullptr;
+    cap = 0;
+    size_t want = bytes + bytes / 4 + 256;
+    cudaError_t e = cudaMallocAsync(&p, want, s);
+    if (e != cudaSuccess) return fail(QR_ENOMEM, std::string("SVD workspace: ") + cudaGetErrorString(e));
+    cap = want;
+    return QR_OK;
+  }
+  template <typename T> T* as() { return reinterpret_cast<T*>(p); }
+};
+
+struct SvdWork {
+  DBuf B, V, B32, V32, X, Rm, Sm, E, T1, nrm, perm, cnt, tau, qtmp, host_sig;
+  std::vector<double> hs;
+  std::vector<unsigned> hc;
+  cudaStream_t last = nullptr;
+};
+
+SvdWork* svd_work_create() { return new SvdWork(); }
+void svd_work_free(SvdWork* w) {
+  if (!w) return;
+  DBuf* all[] = {&w->B, &w->V, &w->B32, &w->V32, &w->X, &w->Rm, &w->Sm, &w->E, &w->T1,
+                 &w->nrm, &w->perm, &w->cnt, &w->tau, &w->qtmp, &w->host_sig};
+  for (DBuf* b : all)
+    if (b->p) cudaFree(b->p);
+  delete w;
+}
+
+namespace {
+
+constexpr int TPB = 256;
+
+template <typename T> struct Eps;
+template <> struct Eps<double> { static constexpr double v = 2.220446049250313e-16; };
+template <> struct Eps<float> { static constexpr float v = 1.1920929e-07f; };
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// One round of the round-robin ordering: warp w handles pair w.
+template <typename T>
+__global__ void __launch_bounds__(TPB) jacobi_round_k(cplx_t<T>* __restrict__ B, long ldb, int m,
+                                                      int n, cplx_t<T>* __restrict__ V, long ldv,
+                                                      int nv, int np, int round, T tol,
+                                                      unsigned* __restrict__ count) {
+  using C = cplx_t<T>;
+  const int lane = threadIdx.x & 31;
+  const int pair = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (pair >= np / 2) return;
+  const int np1 = np - 1;
+  int p, q;
+  if (pair == 0) { p = round; q = np1; }
+  else { p = (round + pair) % np1; q = (round - pair + np1) % np1; }
+  if (p >= n || q >= n) return;
+  if (p > q) { int t = p; p = q; q = t; }
+  C* bp = B + (long)p * ldb;
+  C* bq = B + (long)q * ldb;
+  T a = 0, b = 0, gr = 0, gi = 0;
+  for (int r = lane; r < m; r += 32) {
+    C x = bp[r], y = bq[r];
+    a += x.x * x.x + x.y * x.y;
+    b += y.x * y.x + y.y * y.y;
+    gr += x.x * y.x + x.y * y.y;  // conj(x) * y
+    gi += x.x * y.y - x.y * y.x;
+  }
+  a = warp_sum(a); b = warp_sum(b); gr = warp_sum(gr); gi = warp_sum(gi);
+  T g = sqrt(gr * gr + gi * gi);
+  if (!(a > 0) || !(b > 0) || !(g > tol * sqrt(a) * sqrt(b))) return;
+  T zeta = (b - a) / (2 * g);
+  T t = (zeta >= 0 ? T(1) : T(-1)) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
+  T c = T(1) / sqrt(T(1) + t * t);
+  T sr = t * c * gr / g, si = t * c * gi / g;  // s = t c e^{i phi}, gamma = |gamma| e^{i phi}
+  // p' = c p - conj(s) q ;  q' = s p + c q
+  for (int r = lane; r < m; r += 32) {
+    C x = bp[r], y = bq[r];
+    C xn, yn;
+    xn.x = c * x.x - (sr * y.x + si * y.y);
+    xn.y = c * x.y - (sr * y.y - si * y.x);
+    yn.x = (sr * x.x - si * x.y) + c * y.x;
+    yn.y = (sr * x.y + si * x.x) + c * y.y;
+    bp[r] = xn; bq[r] = yn;
+  }
+  C* vp = V + (long)p * ldv;
+  C* vq = V + (long)q * ldv;
+  for (int r = lane; r < nv; r += 32) {
+    C x = vp[r], y = vq[r];
+    C xn, yn;
+    xn.x = c * x.x - (sr * y.x + si * y.y);
+    xn.y = c * x.y - (sr * y.y - si * y.x);
+    yn.x = (sr * x.x - si * x.y) + c * y.x;
+    yn.y = (sr * x.y + si * x.x) + c * y.y;
+    vp[r] = xn; vq[r] = yn;
+  }
+  if (lane == 0) atomicAdd(count, 1u);
+}
+
+// nrm[j] = |col_j| in FP64 (one warp per column)
+template <typename C>
+__global__ void col_norms_k(const C* __restrict__ B, long ldb, int m, int n, double* __restrict__ nrm) {
+  const int lane = threadIdx.x & 31;
+  const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (j >= n) return;
+  const C* col = B + (long)j * ldb;
+  double acc = 0.0;
+  for (int r = lane; r < m; r += 32) {
+    double x = col[r].x, y = col[r].y;
+    acc += x * x + y * y;
+  }
+  acc = warp_sum(acc);
+  if (lane == 0) nrm[j] = sqrt(acc);
+}
+
+// perm[rank] = j, descending by key (ties by index), one thread per element
+__global__ void rank_sort_k(const double* __restrict__ key, int n, int* __restrict__ perm, double* __restrict__ sorted) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double ki = key[i];
+  int rank = 0;
+  for (int j = 0; j < n; j++) {
+    double kj = key[j];
+    rank += (kj > ki) || (kj == ki && j < i);
+  }
+  perm[rank] = i;
+  if (sorted) sorted[rank] = ki;
+}
+
+// dst[:, j] = src[:, perm[j]] * (scale ? 1/scale[j] : 1), with 1/0 -> 0
+template <typename CS>
+__global__ void gather_cols_k(const CS* __restrict__ src, long lds, int rows, int cols,
+                              const int* __restrict__ perm, const double* __restrict__ sorted_scale,
+                              double2* __restrict__ dst, long ldd) {
+  long total = (long)rows * cols;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+    long i = t % rows, j = t / rows;
+    CS v = src[i + (long)perm[j] * lds];
+    double f = 1.0;
+    if (sorted_scale) { double sv = sorted_scale[j]; f = sv > 0.0 ? 1.0 / sv : 0.0; }
+    dst[i + j * ldd] = make_double2((double)v.x * f, (double)v.y * f);
+  }
+}
+
+// Ogita-Aishima correction matrix (n x n): see file header.  Returns E; also writes
+// off[0] = max over separated pairs of |S_ij| / sqrt(S_ii S_jj) (as uint bits, atomicMax).
+__global__ void oa_correction_k(const double2* __restrict__ S, const double2* __restrict__ Rm, int n,
+                                double2* __restrict__ E, unsigned long long* __restrict__ off) {
+  long total = (long)n * n;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+    int i = (int)(t % n), j = (int)(t / n);
+    double2 r = Rm[t];
+    double2 e;
+    if (i == j) {
+      e = make_double2(0.5 * r.x, 0.5 * r.y);
+    } else {
+      double lti = S[i + (long)i * n].x / (1.0 - Rm[i + (long)i * n].x);
+      double ltj = S[j + (long)j * n].x / (1.0 - Rm[j + (long)j * n].x);
+      double2 s = S[t];
+      double2 num = make_double2(s.x + ltj * r.x, s.y + ltj * r.y);
+      double gap = ltj - lti;
+      double an = sqrt(num.x * num.x + num.y * num.y);
+      if (an <= 0.1 * fabs(gap)) {
+        e = make_double2(num.x / gap, num.y / gap);
+      } else {
+        e = make_double2(0.5 * r.x, 0.5 * r.y);
+      }
+      double den = sqrt(fabs(S[i + (long)i * n].x) * fabs(S[j + (long)j * n].x));
+      if (den > 0.0) {
+        double rel = sqrt(s.x * s.x + s.y * s.y) / den;
+        atomicMax(off, (unsigned long long)__double_as_longlong(rel));
+      }
+    }
+    E[t] = e;
+  }
+}
+
+__global__ void add_identity_k(double2* A, int n, long lda, double alpha) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) A[i + (long)i * lda].x += alpha;
+}
+
+// Q[:, j] *= phase(R_jj) (R_jj == 0 -> 1): keeps Q as close to the input columns as possible
+__global__ void phase_fix_k(double2* Q, long ldq, int m, int k, const double2* R, long ldr) {
+  long total = (long)m * k;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+    long i = t % m, j = t / m;
+    double2 d = R[j + j * ldr];
+    double a = sqrt(d.x * d.x + d.y * d.y);
+    double2 ph = a > 0.0 ? make_double2(d.x / a, d.y / a) : make_double2(1.0, 0.0);
+    Q[i + j * ldq] = cmul(Q[i + j * ldq], ph);
+  }
+}
+
+inline unsigned gs(long n) {
+  long g = (n + TPB - 1) / TPB;
+  if (g > 152L * 32) g = 152L * 32;
+  return (unsigned)(g < 1 ? 1 : g);
+}
+
+// Hestenes sweeps on B (rows x k) accumulating V (k x k), until no rotation happens.
+template <typename T>
+int jacobi(cudaStream_t s, SvdWork* w, cplx_t<T>* B, long ldb, int rows, int k, cplx_t<T>* V,
+           long ldv, int max_sweeps, T tol) {
+  const int np = k + (k & 1);
+  unsigned* cnt = w->cnt.as<unsigned>();
+  const unsigned grid = ceil_div((long)(np / 2) * 32, TPB);
+  const int kind = sizeof(T) == 8 ? PK_JACOBI64 : PK_JACOBI32;
+  const double pairs = 0.5 * (double)k * (k - 1);
+  for (int sweep = 0; sweep < max_sweeps; sweep++) {
+    QR_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned), s));
+    int pr = prof_begin(s, kind, 0.0, 0.0);
+    for (int r = 0; r < np - 1; r++) {
+      jacobi_round_k<T><<<grid, TPB, 0, s>>>(B, ldb, rows, k, V, ldv, k, np, r, tol, cnt);
+      QR_CHECK_LAUNCH("jacobi_round_k");
+    }
+    prof_end(s, pr);
+    unsigned h = 0;
+    QR_CUDA(cudaMemcpyAsync(&h, cnt, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    QR_CUDA(cudaStreamSynchronize(s));
+    // algorithmic work of the sweep: three inner products per pair (16 real flops per row) and
+    // two column rotations of B and V for every rotated pair (20 flops per row and column)
+    prof_account(pr, 16.0 * rows * pairs + 20.0 * (double)h * (rows + k) * 2.0,
+                 sizeof(cplx_t<T>) * ((double)rows + k) * 2.0 * (pairs + h));
+    if (h == 0) return QR_OK;
+  }
+  return fail(QR_ENOCONV, "Jacobi SVD did not converge");
+}
+
+}  // namespace
+
+// Re-orthonormalise the m x k column block L in place (Householder QR, phase-preserving).
+static int reorthonormalize(cudaStream_t s, SvdWork* w, double2* L, long ldl, int m, int k) {
+  QR_TRY(w->qtmp.ensure(sizeof(double2) * ((size_t)m * k + (size_t)k * k), s));
+  QR_TRY(w->tau.ensure(sizeof(double2) * (size_t)k, s));
+  double2* Rr = w->qtmp.as<double2>() + (size_t)m * k;
+  // factor a copy; Q overwrites L
+  double2* Acopy = w->qtmp.as<double2>();
+  QR_CUDA(cudaMemcpy2DAsync(Acopy, sizeof(double2) * m, L, sizeof(double2) * ldl, sizeof(double2) * m, k,
+                            cudaMemcpyDeviceToDevice, s));
+  QR_TRY(zqr_thin(s, Acopy, m, k, m, L, ldl, Rr, k, w->tau.as<double2>()));
+  phase_fix_k<<<gs((long)m * k), TPB, 0, s>>>(L, ldl, m, k, Rr, k);
+  QR_CHECK_LAUNCH("phase_fix_k");
+  return QR_OK;
+}
+
+int zsvd_thin(cudaStream_t s, SvdWork* w, int mode, const double2* A, int m, int n, long lda,
+              double2* U, long ldu, double* S, double2* Vh, long ldvh) {
+  if (m <= 0 || n <= 0) return QR_OK;
+  const bool tall = m >= n;
+  const int rows = tall ? m : n;  // B = A (tall) or A^H (wide): rows x k
+  const int k = tall ? n : m;
+  QR_TRY(w->B.ensure(sizeof(double2) * (size_t)rows * k, s));
+  QR_TRY(w->V.ensure(sizeof(double2) * (size_t)k * k, s));
+  QR_TRY(w->nrm.ensure(sizeof(double) * (size_t)k * 2, s));
+  QR_TRY(w->perm.ensure(sizeof(int) * (size_t)k, s));
+  QR_TRY(w->cnt.ensure(sizeof(unsigned long long) * 2, s));
+  double2* B = w->B.as<double2>();
+  double2* V = w->V.as<double2>();
+  double* nrm = w->nrm.as<double>();
+  double* sorted = nrm + k;
+  int* perm = w->perm.as<int>();
+
+  // B = A or A^H (FP64 copy; A is preserved)
+  if (tall) {
+    QR_CUDA(cudaMemcpy2DAsync(B, sizeof(double2) * rows, A, sizeof(double2) * lda, sizeof(double2) * m, n,
+                              cudaMemcpyDeviceToDevice, s));
+  } else {
+    QR_TRY(ztranspose(s, A, lda, m, n, B, rows, 1));
+  }
+
+  if (mode == QR_FP64) {
+    QR_TRY(zset_identity(s, V, k, k, k));
+    double tol = sqrt((double)rows) * Eps<double>::v;
+    QR_TRY(jacobi<double>(s, w, B, rows, rows, k, V, k, 60, tol));
+  } else {
+    // ---- FP32 Jacobi preconditioner
+    QR_TRY(w->B32.ensure(sizeof(float2) * (size_t)rows * k, s));
+    QR_TRY(w->V32.ensure(sizeof(float2) * (size_t)k * k, s));
+    float2* B32 = w->B32.as<float2>();
+    float2* V32 = w->V32.as<float2>();
+    QR_TRY(z2c(s, B, rows, B32, rows, rows, k));
+    QR_TRY(cset_identity(s, V32, k, k, k));
+    float tol32 = sqrtf((float)rows) * Eps<float>::v;
+    QR_TRY(jacobi<float>(s, w, B32, rows, rows, k, V32, k, 40, tol32));
+    // X = V32 sorted by the FP32 column norms (descending), promoted to FP64
+    col_norms_k<float2><<<ceil_div((long)k * 32, TPB), TPB, 0, s>>>(B32, rows, rows, k, nrm);
+    QR_CHECK_LAUNCH("col_norms_k");
+    rank_sort_k<<<ceil_div(k, TPB), TPB, 0, s>>>(nrm, k, perm, nullptr);
+    QR_CHECK_LAUNCH("rank_sort_k");
+    QR_TRY(w->X.ensure(sizeof(double2) * (size_t)k * k, s));
+    QR_TRY(w->Rm.ensure(sizeof(double2) * (size_t)k * k, s));
+    QR_TRY(w->Sm.ensure(sizeof(double2) * (size_t)k * k, s));
+    QR_TRY(w->E.ensure(sizeof(double2) * (size_t)k * k, s));
+    double2* X = w->X.as<double2>();
+    double2* Rm = w->Rm.as<double2>();
+    double2* Sm = w->Sm.as<double2>();
+    double2* E = w->E.as<double2>();
+    gather_cols_k<float2><<<gs((long)k * k), TPB, 0, s>>>(V32, k, k, k, perm, nullptr, X, k);
+    QR_CHECK_LAUNCH("gather_cols_k");
+    unsigned long long* off = w->cnt.as<unsigned long long>();
+    const double2 one = make_double2(1.0, 0.0), zero = make_double2(0.0, 0.0), mone = make_double2(-1.0, 0.0);
+    const double2* Bsrc = B;  // A (tall) or A^H (wide) in FP64, rows x k
+    // B is reused below as the product A X, so keep the FP64 source in T1
+    QR_TRY(w->T1.ensure(sizeof(double2) * (size_t)rows * k, s));
+    double2* Asrc = w->T1.as<double2>();
+    QR_CUDA(cudaMemcpyAsync(Asrc, Bsrc, sizeof(double2) * (size_t)rows * k, cudaMemcpyDeviceToDevice, s));
+    for (int it = 0; it < 3; it++) {
+      // R = I - X^H X
+      QR_TRY(zgemm(s, OP_C, OP_N, k, k, k, mone, X, k, 0, X, k, 0, zero, Rm, k, 0, 1, nullptr));
+      add_identity_k<<<ceil_div(k, TPB), TPB, 0, s>>>(Rm, k, k, 1.0);
+      QR_CHECK_LAUNCH("add_identity_k");
+      // B = A X ; S = B^H B
+      QR_TRY(zgemm(s, OP_N, OP_N, rows, k, k, one, Asrc, rows, 0, X, k, 0, zero, B, rows, 0, 1, nullptr));
+      QR_TRY(zgemm(s, OP_C, OP_N, k, k, rows, one, B, rows, 0, B, rows, 0, zero, Sm, k, 0, 1, nullptr));
+      QR_CUDA(cudaMemsetAsync(off, 0, sizeof(unsigned long long), s));
+      oa_correction_k<<<gs((long)k * k), TPB, 0, s>>>(Sm, Rm, k, E, off);
+      QR_CHECK_LAUNCH("oa_correction_k");
+      unsigned long long hoff = 0;
+      QR_CUDA(cudaMemcpyAsync(&hoff, off, sizeof(hoff), cudaMemcpyDeviceToHost, s));
+      QR_CUDA(cudaStreamSynchronize(s));
+      double offv;
+      memcpy(&offv, &hoff, sizeof(double));
+      if (offv < 4.0 * Eps<double>::v * sqrt((double)rows) && it > 0) break;
+      // X <- X + X E  (V as scratch)
+      QR_CUDA(cudaMemcpyAsync(V, X, sizeof(double2) * (size_t)k * k, cudaMemcpyDeviceToDevice, s));
+      QR_TRY(zgemm(s, OP_N, OP_N, k, k, k, one, V, k, 0, E, k, 0, one, X, k, 0, 1, nullptr));
+    }
+    // final B = A X, V = X
+    QR_TRY(zgemm(s, OP_N, OP_N, rows, k, k, one, Asrc, rows, 0, X, k, 0, zero, B, rows, 0, 1, nullptr));
+    QR_CUDA(cudaMemcpyAsync(V, X, sizeof(double2) * (size_t)k * k, cudaMemcpyDeviceToDevice, s));
+  }
+
+  // ---- sigma, ordering, factors
+  col_norms_k<double2><<<ceil_div((long)k * 32, TPB), TPB, 0, s>>>(B, rows, rows, k, nrm);
+  QR_CHECK_LAUNCH("col_norms_k");
+  rank_sort_k<<<ceil_div(k, TPB), TPB, 0, s>>>(nrm, k, perm, sorted);
+  QR_CHECK_LAUNCH("rank_sort_k");
+  QR_CUDA(cudaMemcpyAsync(S, sorted, sizeof(double) * k, cudaMemcpyDeviceToDevice, s));
+  // decide on re-orthonormalisation from the spectrum
+  w->hs.resize(k);
+  QR_CUDA(cudaMemcpyAsync(w->hs.data(), sorted, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+  QR_CUDA(cudaStreamSynchronize(s));
+  const double smax = w->hs[0], smin = w->hs[k - 1];
+  const bool reorth = !(smin > 1e-6 * smax);
+
+  // left factor L (rows x k) = B[:, perm] / sigma ; right factor Rf (k x k) = V[:, perm]
+  QR_TRY(w->E.ensure(sizeof(double2) * (size_t)k * k, s));
+  double2* Rf = w->E.as<double2>();
+  if (tall) {
+    gather_cols_k<double2><<<gs((long)rows * k), TPB, 0, s>>>(B, rows, rows, k, perm, sorted, U, ldu);
+    QR_CHECK_LAUNCH("gather_cols_k");
+    if (reorth) QR_TRY(reorthonormalize(s, w, U, ldu, m, k));
+    gather_cols_k<double2><<<gs((long)k * k), TPB, 0, s>>>(V, k, k, k, perm, nullptr, Rf, k);
+    QR_CHECK_LAUNCH("gather_cols_k");
+    QR_TRY(ztranspose(s, Rf, k, k, k, Vh, ldvh, 1));  // Vh = Rf^H (k x n)
+  } else {
+    // A^H = L Sigma Rf^H  =>  A = Rf Sigma L^H : U = Rf (m x m), Vh = L^H (m x n)
+    QR_TRY(w->Rm.ensure(sizeof(double2) * (size_t)rows * k, s));
+    double2* L = w->Rm.as<double2>();
+    gather_cols_k<double2><<<gs((long)rows * k), TPB, 0, s>>>(B, rows, rows, k, perm, sorted, L, rows);
+    QR_CHECK_LAUNCH("gather_cols_k");
+    if (reorth) QR_TRY(reorthonormalize(s, w, L, rows, rows, k));
+    gather_cols_k<double2><<<gs((long)k * k), TPB, 0, s>>>(V, k, k, k, perm, nullptr, U, ldu);
+    QR_CHECK_LAUNCH("gather_cols_k");
+    QR_TRY(ztranspose(s, L, rows, rows, k, Vh, ldvh, 1));
+  }
+  return QR_OK;
+}
+
+}  // namespace qr

@@ -1,0 +1,25 @@
+"""qrochet -- GB300 (sm_103a) implementation of Qrochet.jl's Chain (MPS/MPO) hot path.
+
+Python mirror of the reference's Julia API; every operation runs in libqrochet_gpu.so through
+its C ABI (include/qrochet_gpu.h).  ``f!`` in Julia is ``f_`` here.
+"""
+from ._lib import (ArgumentError, DimensionMismatch, GPUError, MissingSchmidtCoefficientsException,
+                   launch_count)
+from .chain import (MPO, MPS, Chain, Open, Periodic, canonicality_error, canonize, canonize_,
+                    canonize_site, canonize_site_, contract_between, contract_between_, device_count,
+                    evolve_, expect, isleftcanonical, isrightcanonical, mixed_canonize, mixed_canonize_,
+                    mpo_expect, norm, normalize_, overlap, truncate, truncate_, zeros_chain,
+                    PinnedArray, probe_peak, prof_enable, prof_read, set_device, PROF_KINDS)
+from .dense import Dense, Operator, State, gate_from_matrix, validate_gate
+from .site import Site, nextindex, site
+
+__all__ = [
+    "ArgumentError", "DimensionMismatch", "GPUError", "MissingSchmidtCoefficientsException",
+    "launch_count", "MPO", "MPS", "Chain", "Open", "Periodic", "canonicality_error", "canonize",
+    "canonize_", "canonize_site", "canonize_site_", "contract_between", "contract_between_",
+    "device_count", "evolve_", "expect", "isleftcanonical", "isrightcanonical", "mixed_canonize",
+    "mixed_canonize_", "mpo_expect", "norm", "normalize_", "overlap", "truncate", "truncate_",
+    "zeros_chain", "Dense", "Operator", "State", "gate_from_matrix", "validate_gate", "Site",
+    "nextindex", "site", "PinnedArray", "probe_peak", "prof_enable", "prof_read", "set_device",
+    "PROF_KINDS",
+]

@@ -1,0 +1,93 @@
+"""CPU checks of the boundary: the C-ABI library loads and exports every symbol its header
+declares, and the host-side logic (sites, gates, validation) behaves like the reference."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import __graft_entry__ as g
+
+    g.build()
+    from qrochet import _lib
+
+    return _lib.lib()
+
+
+def _declared():
+    text = open(os.path.join(ROOT, "include", "qrochet_gpu.h")).read()
+    return sorted(set(re.findall(r"\b(qr_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_symbols_exported(lib):
+    names = _declared()
+    assert len(names) >= 30
+    for name in names:
+        assert hasattr(lib, name), name
+
+
+def test_python_binding_covers_header():
+    from qrochet import _lib
+
+    names = set(_declared())
+    bound = set(_lib.SIGNATURES) | {"qr_last_error_string"}
+    assert names <= bound, names - bound
+
+
+def test_no_device_is_reported_not_faked(lib):
+    import qrochet as Q
+
+    if Q.device_count() > 0:
+        pytest.skip("a GPU is present")
+    with pytest.raises(Q.GPUError):
+        Q.MPS([np.ones((2, 1)), np.ones((2, 1))])
+
+
+def test_site_parsing_and_adjoint():
+    from qrochet import Site, site
+
+    assert site("3") == Site(3)
+    assert site("3'") == Site(3, True)
+    assert Site(2).adjoint() == Site(2, True)
+    assert Site(1) < Site(2)
+    with pytest.raises(ValueError):
+        site("x1")
+
+
+def test_dense_matrix_and_validation():
+    import qrochet as Q
+    from qrochet import random as R
+
+    u = R.haar_unitary(R.rng(1), 4)
+    g = Q.gate_from_matrix(u, [2, 3])
+    assert np.allclose(g.matrix([2, 3]), u)
+    t = u.reshape(2, 2, 2, 2).transpose(1, 0, 3, 2)
+    g2 = Q.Dense(Q.Operator(), t, [Q.Site(3), Q.Site(2), Q.Site(3, True), Q.Site(2, True)])
+    assert np.allclose(g2.matrix([2, 3]), u)
+    assert Q.validate_gate(5, g) == [2, 3]
+    with pytest.raises(Q.ArgumentError):
+        Q.validate_gate(5, Q.gate_from_matrix(np.eye(4), [2, 4]))
+    with pytest.raises(Q.ArgumentError):
+        Q.validate_gate(3, Q.gate_from_matrix(np.eye(2), [4]))
+    with pytest.raises(Q.ArgumentError):
+        Q.validate_gate(5, Q.Dense(Q.Operator(), np.ones((2, 2)), [Q.Site(1), Q.Site(2)]))
+    with pytest.raises(AssertionError):
+        Q.Dense(Q.Operator(), np.ones((2, 1)), [Q.Site(1), Q.Site(1, True)])
+
+
+def test_index_counter_and_random_generators():
+    from qrochet import nextindex
+    from qrochet import random as R
+
+    a, b = nextindex(), nextindex()
+    assert a != b
+    u = R.haar_unitary(R.rng(3), 4)
+    assert np.allclose(u.conj().T @ u, np.eye(4))
+    arrs = R.gaussian_mps_arrays(5, 3, seed=4)
+    assert arrs[0].shape == (2, 3) and arrs[2].shape == (2, 3, 3) and arrs[4].shape == (2, 3)
+    assert all(a.flags.f_contiguous for a in arrs)

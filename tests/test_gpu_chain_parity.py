@@ -1,0 +1,308 @@
+"""GPU parity of every Chain operation against the CPU oracle, through the C ABI.
+
+Tolerances: FP64 path -- gauge-invariant quantities (state vectors, norms, Lambda spectra,
+expectation values) within 1e-10 relative; bond dimensions and Lambda placement bit-exact.
+"""
+import numpy as np
+import pytest
+
+import qrochet as Q
+from oracle import chain_oracle as O
+from qrochet import random as R
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-10
+
+
+def _close(a, b, rtol=RTOL):
+    a, b = np.asarray(a), np.asarray(b)
+    scale = max(1e-300, float(np.max(np.abs(b))) if b.size else 1.0)
+    return float(np.max(np.abs(a - b))) <= rtol * scale if a.size else True
+
+
+def _sv(psi: Q.Chain):
+    """State vector of a GPU chain (download + oracle contraction)."""
+    ch = O.from_reference_arrays(psi.arrays())
+    for b, f in enumerate(psi.lambda_flags()):
+        if f:
+            ch.lam[b] = psi.lambda_between(b + 1, b + 2)
+    return O.to_statevector(ch)
+
+
+def _pair(n, chi, seed, uniform=True, real=False):
+    if real:
+        g = R.rng(seed)
+        shapes = [(2, chi)] + [(2, chi, chi)] * (n - 2) + [(2, chi)]
+        arrays = [np.asfortranarray(g.random(s)) for s in shapes]
+    else:
+        arrays = R.gaussian_mps_arrays(n, chi, seed=seed, uniform=uniform)
+    return Q.MPS(arrays), O.from_reference_arrays(arrays)
+
+
+def _check_same(psi, ref, rtol=RTOL, statevector=True):
+    assert psi.bond_dims() == ref.bond_dims()
+    assert psi.lambda_flags() == ref.lambda_flags()
+    assert psi.ntensors() == ref.ntensors()
+    for b, lm in enumerate(ref.lam):
+        if lm is not None:
+            assert _close(psi.lambda_between(b + 1, b + 2), lm, rtol), b
+    if statevector:
+        assert _close(_sv(psi), O.to_statevector(ref), rtol)
+
+
+@pytest.mark.parametrize("order", [("o", "l", "r"), ("r", "o", "l"), ("l", "r", "o")])
+def test_upload_download_roundtrip(order):
+    arrays = R.gaussian_mps_arrays(5, 3, seed=3, uniform=False)
+    psi = Q.MPS(arrays)
+    perm = []
+    for i, a in enumerate(arrays):
+        src = [x for x in ("o", "l", "r") if not ((i == 0 and x == "l") or (i == 4 and x == "r"))]
+        dst = [x for x in order if not ((i == 0 and x == "l") or (i == 4 and x == "r"))]
+        perm.append(np.transpose(a, [src.index(x) for x in dst]))
+    psi2 = Q.MPS(perm, order=order)
+    for i in range(5):
+        assert np.array_equal(psi.site_array(i + 1), arrays[i])
+        assert np.array_equal(psi2.site_array(i + 1), arrays[i])
+        assert np.array_equal(psi2.site_array(i + 1, order), perm[i])
+
+
+@pytest.mark.parametrize("method", ["qr", "svd"])
+@pytest.mark.parametrize("site,direction", [(1, "right"), (2, "right"), (2, "left"), (3, "left")])
+def test_canonize_site(method, site, direction):
+    psi, ref = _pair(3, 4, seed=7, real=True)
+    Q.canonize_site_(psi, site, direction, method)
+    O.canonize_site_(ref, site - 1, direction, method)
+    _check_same(psi, ref)
+    pred = Q.isleftcanonical if direction == "right" else Q.isrightcanonical
+    assert pred(psi, site)
+
+
+def test_canonize_site_errors():
+    psi, _ = _pair(3, 4, seed=7, real=True)
+    with pytest.raises(Q.ArgumentError):
+        Q.canonize_site_(psi, 1, "left")
+    with pytest.raises(Q.ArgumentError):
+        Q.canonize_site_(psi, 3, "right")
+    with pytest.raises(Q.ArgumentError):
+        Q.canonize_site_(psi, 2, "up")
+    assert Q.canonize_site(psi, 2, "left", "svd").ntensors() == 4
+
+
+def test_canonize_reference_properties():
+    # the checks of test/Ansatz/Chain_test.jl:308-356 on the GPU chain
+    psi, ref = _pair(5, 4, seed=9, real=True)
+    can = Q.canonize(psi)
+    O.canonize_(ref)
+    assert can.ntensors() == 9
+    _check_same(can, ref)
+    assert np.isclose(Q.norm(psi), Q.norm(can), rtol=RTOL)
+    nrm2 = Q.norm(can) ** 2
+    for b in range(4):
+        assert np.isclose(np.sum(can.lambda_between(b + 1, b + 2) ** 2), nrm2, rtol=1e-10)
+    for i in range(1, 6):
+        c = Q.canonize(psi)
+        if i == 1:
+            assert Q.isleftcanonical(c, i)
+        else:
+            Q.contract_between_(c, i - 1, i, direction="right")
+            if i == 5:  # the end tensor carries the norm: its 1x1 Gram is ||psi||^2
+                assert abs(Q.canonicality_error(c, i, "left") - abs(nrm2 - 1)) <= 1e-10 * nrm2
+            else:
+                assert Q.isleftcanonical(c, i)
+    for i in range(1, 6):
+        c = Q.canonize(psi)
+        if i == 5:
+            assert Q.isrightcanonical(c, i)
+        else:
+            Q.contract_between_(c, i, i + 1, direction="left")
+            if i == 1:
+                assert abs(Q.canonicality_error(c, i, "right") - abs(nrm2 - 1)) <= 1e-10 * nrm2
+            else:
+                assert Q.isrightcanonical(c, i)
+
+
+@pytest.mark.parametrize("n,chi,seed", [(16, 32, 1), (9, 7, 2), (6, 40, 3)])
+def test_canonize_gaussian(n, chi, seed):
+    psi, ref = _pair(n, chi, seed)
+    Q.canonize_(psi)
+    O.canonize_(ref)
+    _check_same(psi, ref, statevector=n <= 12)
+
+
+def test_mixed_canonize_and_normalize():
+    psi, ref = _pair(5, 4, seed=13, real=True)
+    can = Q.mixed_canonize(psi, 3)
+    O.mixed_canonize_(ref, 2)
+    _check_same(can, ref)
+    assert Q.isleftcanonical(can, 1) and Q.isleftcanonical(can, 2)
+    for s in (3, 4, 5):
+        assert Q.isrightcanonical(can, s)
+    with pytest.raises(Q.ArgumentError):
+        Q.mixed_canonize(psi, 1)
+    Q.normalize_(psi, 3)
+    assert np.isclose(Q.norm(psi), 1.0, rtol=1e-12)
+
+
+def test_truncate():
+    psi, ref = _pair(3, 2, seed=11, real=True)
+    Q.canonize_site_(psi, 2, "right", "svd")
+    O.canonize_site_(ref, 1, "right", "svd")
+    with pytest.raises(Q.MissingSchmidtCoefficientsException):
+        Q.truncate_(psi.copy(), (1, 2), maxdim=1)
+    with pytest.raises(Q.ArgumentError):
+        Q.truncate_(psi.copy(), (1, 3), maxdim=1)
+    t = Q.truncate(psi, (2, 3), maxdim=1)
+    assert t.bond_dims()[1] == 1
+    lam = psi.lambda_between(2, 3)
+    t = Q.truncate(psi, (2, 3), threshold=lam[1] + 0.1)
+    assert t.bond_dims()[1] == 1
+    O.truncate_(ref, (1, 2), maxdim=1)
+    Q.truncate_(psi, (2, 3), maxdim=1)
+    _check_same(psi, ref)
+
+
+def test_contract_between():
+    # Chain_test.jl:241-266 runs on rand(Chain, Open, State; n=5, p=2, chi=20): a normalised state
+    arrays = R.rand_chain_state_arrays(R.rng(21), 5, 20, p=2)
+    psi, ref = Q.MPS(arrays), O.from_reference_arrays(arrays)
+    Q.canonize_(psi)
+    O.canonize_(ref)
+    for i in range(1, 5):
+        a = Q.contract_between(psi, i, i + 1)
+        r = O.contract_between_(ref.copy(), i - 1, i)
+        _check_same(a, r)
+        assert Q.isrightcanonical(a, i)
+        b = Q.contract_between(psi, i, i + 1, direction="right")
+        assert Q.isleftcanonical(b, i + 1)
+    with pytest.raises(Q.ArgumentError):
+        Q.contract_between(psi, 1, 2, direction="dummy")
+
+
+def test_evolve_1site_and_2site_exact():
+    n = 7
+    psi, ref = _pair(n, 4, seed=31, uniform=False)
+    for layer in R.brickwall_layers(n, 4, seed=32):
+        for s, u in layer:
+            Q.evolve_(psi, Q.gate_from_matrix(u, [s, s + 1]))
+            O.evolve_2site_(ref, s - 1, u)
+    x = R.haar_unitary(R.rng(33), 2)
+    Q.evolve_(psi, Q.gate_from_matrix(x, [4]))
+    O.evolve_1site_(ref, 3, x)
+    _check_same(psi, ref)
+
+
+def test_evolve_gate_site_order():
+    psi, _ = _pair(4, 3, seed=41)
+    u = R.haar_unitary(R.rng(42), 4)
+    a = Q.evolve_(psi.copy(), Q.gate_from_matrix(u, [2, 3]))
+    t = u.reshape(2, 2, 2, 2).transpose(1, 0, 3, 2)
+    g = Q.Dense(Q.Operator(), t, [Q.Site(3), Q.Site(2), Q.Site(3, True), Q.Site(2, True)])
+    b = Q.evolve_(psi.copy(), g)
+    assert _close(_sv(a), _sv(b))
+
+
+def test_evolve_errors():
+    psi, _ = _pair(4, 2, seed=43)
+    with pytest.raises(Q.ArgumentError):
+        Q.evolve_(psi, Q.gate_from_matrix(np.eye(4), [1, 3]))
+    with pytest.raises(Q.ArgumentError):
+        Q.evolve_(psi, Q.gate_from_matrix(np.eye(2), [7]))
+    with pytest.raises(Q.ArgumentError):
+        Q.evolve_(psi, Q.gate_from_matrix(np.eye(8), [1, 2, 3]))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_tebd_with_truncation(precision):
+    # TEBD of the n=64 / chi_max=256 workload shrunk to oracle size: |0..0>, Haar brick wall,
+    # threshold 1e-10 and maxdim; bond dims must match after every gate.
+    n, depth, maxdim = 12, 8, 12
+    arrays = R.zero_product_arrays(n)
+    psi, ref = Q.MPS(arrays), O.from_reference_arrays(arrays)
+    psi.set_precision(precision)
+    for layer in R.brickwall_layers(n, depth, seed=51):
+        for s, u in layer:
+            Q.evolve_(psi, Q.gate_from_matrix(u, [s, s + 1]), threshold=1e-10, maxdim=maxdim)
+            O.evolve_2site_(ref, s - 1, u, threshold=1e-10, maxdim=maxdim)
+            assert psi.bond_dims() == ref.bond_dims()
+    tol = RTOL if precision == "fp64" else 1e-8
+    _check_same(psi, ref, rtol=tol)
+    for i in range(1, n + 1):
+        xi = Q.gate_from_matrix(R.PAULI["X"], [i])
+        e = Q.expect(psi, [xi])
+        e_ref = O.expect(ref, [O.ODense(R.PAULI["X"], (O.OSite(i), O.OSite(i, True)))])
+        assert abs(e - e_ref) <= tol * max(1.0, abs(e_ref))
+
+
+def test_config1_pipeline():
+    # plain workload: n=16, d=2, chi=32 Gaussian MPS; canonize!, norm, <Z_i Z_{i+1}> for all i
+    psi, ref = _pair(16, 32, seed=1)
+    Q.canonize_(psi)
+    O.canonize_(ref)
+    _check_same(psi, ref, statevector=False)
+    assert np.isclose(Q.norm(psi), O.norm(ref), rtol=RTOL)
+    zz = np.kron(R.PAULI["Z"], R.PAULI["Z"])
+    for i in range(1, 16):
+        e = Q.expect(psi, [Q.gate_from_matrix(zz, [i, i + 1])])
+        e_ref = O.expect(ref, [O.ODense(zz.reshape(2, 2, 2, 2), (O.OSite(i), O.OSite(i + 1),
+                                                              O.OSite(i, True), O.OSite(i + 1, True)))])
+        assert abs(e - e_ref) <= RTOL * abs(O.norm(ref)) ** 2
+
+
+def test_expect_products_and_overlap():
+    n = 7
+    psi, ref = _pair(n, 6, seed=61)
+    phi, refp = _pair(n, 5, seed=62)
+    assert np.isclose(Q.overlap(psi, phi), O.overlap(ref, refp), rtol=RTOL)
+    zz = np.kron(R.PAULI["Z"], R.PAULI["Z"])
+    obs_q = [Q.gate_from_matrix(R.PAULI["X"], [2]), Q.gate_from_matrix(R.PAULI["Y"], [5]),
+             Q.gate_from_matrix(zz, [3, 4]), Q.gate_from_matrix(R.haar_unitary(R.rng(63), 4), [2, 3])]
+    obs_o = [O.ODense(g.array, tuple(O.OSite(s.id, s.dual) for s in g.sites)) for g in obs_q]
+    assert np.isclose(Q.expect(psi, obs_q), O.expect(ref, obs_o), rtol=RTOL)
+
+
+def test_mpo_expect_xxz():
+    n = 8
+    psi, ref = _pair(n, 6, seed=71)
+    arrs = R.xxz_mpo_arrays(n, 1.0, 0.7)
+    H = Q.MPO(arrs)
+    ws = []
+    for i, a in enumerate(arrs):
+        a = np.asarray(a)
+        if i == 0:
+            a = a[:, :, None, :]
+        elif i == n - 1:
+            a = a[:, :, :, None]
+        ws.append(np.transpose(a, (2, 0, 1, 3)))
+    assert np.isclose(Q.mpo_expect(psi, H), O.mpo_expect(ref, ws), rtol=RTOL)
+
+
+def test_vidal_path_and_renormalize():
+    n = 6
+    psi, ref = _pair(n, 4, seed=81, uniform=False)
+    Q.canonize_(psi)
+    O.canonize_(ref)
+    u = R.haar_unitary(R.rng(82), 4)
+    a = Q.evolve_(psi.copy(), Q.gate_from_matrix(u, [3, 4]), iscanonical=True)
+    ra = O.evolve_2site_(ref.copy(), 2, u, iscanonical=True)
+    _check_same(a, ra)
+    b = Q.evolve_(psi.copy(), Q.gate_from_matrix(u, [3, 4]), maxdim=2, iscanonical=True, renormalize=True)
+    rb = O.evolve_2site_(ref.copy(), 2, u, maxdim=2, iscanonical=True, renormalize=True)
+    _check_same(b, rb)
+    c = Q.evolve_(psi.copy(), Q.gate_from_matrix(u, [3, 4]), maxdim=2, renormalize=True)
+    rc = O.evolve_2site_(ref.copy(), 2, u, maxdim=2, renormalize=True)
+    _check_same(c, rc)
+    assert np.isclose(Q.norm(c), 1.0, rtol=1e-12)
+    with pytest.raises(Q.ArgumentError):
+        Q.evolve_(psi.copy(), Q.gate_from_matrix(u, [1, 2]), maxdim=2, renormalize=True)
+
+
+def test_rank_deficient_and_zero_singular_values():
+    # identity gate on |0..0> leaves theta rank 1: thin SVD keeps a zero singular value and
+    # an orthonormal completion of U, like LAPACK
+    n = 4
+    psi, ref = Q.zeros_chain(n), O.from_reference_arrays(R.zero_product_arrays(n))
+    Q.evolve_(psi, Q.gate_from_matrix(np.eye(4), [2, 3]))
+    O.evolve_2site_(ref, 1, np.eye(4))
+    _check_same(psi, ref)
+    assert Q.isleftcanonical(psi, 2)
