@@ -131,6 +131,14 @@ int qr_mpo_free(qr_mpo* w);
 int qr_mpo_upload_site(qr_mpo* w, int site, const double* host, const char* order);
 int qr_mpo_expect(const qr_chain* h, const qr_mpo* w, double* out);
 
+/* ---- kernel-level test hooks (no reference counterpart): host matrices in and out, complex
+   interleaved, column-major; op codes 0 N, 1 T, 2 C (conjugate transpose), 3 R (conjugate) ----- */
+int qr_test_zgemm(int opA, int opB, int M, int N, int K, const double* alpha, const double* A, long lda,
+                  const double* B, long ldb, const double* beta, double* C, long ldc, const double* dk,
+                  int iters, double* ms_per_iter);
+int qr_test_svd(int mode, int m, int n, const double* A, double* U, double* S, double* Vh, double* ms);
+int qr_test_qr(int m, int n, const double* A, double* Q, double* R, double* ms);
+
 #ifdef __cplusplus
 }
 #endif

@@ -345,7 +345,7 @@ int evolve2_impl(qr_chain* h, int sl, const double* g, double threshold, int max
   double2 *U = nullptr, *Vh = nullptr;
   QR_TRY(dalloc((void**)&U, sizeof(double2) * (size_t)m * k, s));
   QR_TRY(dalloc((void**)&Vh, sizeof(double2) * (size_t)k * nn, s));
-  QR_TRY(zsvd_thin(s, h->svd, h->precision, th, m, nn, m, U, m, S, Vh, k));
+  QR_TRY(zsvd_thin(s, h->svd, h->precision, th, m, nn, m, U, m, S, Vh, k, maxdim >= 0 ? maxdim : 0));
   set_site(h, sl, U);
   set_site(h, sr, Vh);
   h->bd[sl] = k;

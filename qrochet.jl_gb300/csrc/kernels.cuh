@@ -51,8 +51,10 @@ struct SvdWork;  // opaque, grows on demand
 SvdWork* svd_work_create();
 void svd_work_free(SvdWork* w);
 // Thin SVD of the m x n matrix A (ld lda; A is preserved).  U: m x k (ld ldu), S: k (device),
-// Vh: k x n (ld ldvh), k = min(m,n), S descending.  mode: QR_FP64 or QR_MIXED.
+// Vh: k x n (ld ldvh), k = min(m,n), S descending.  mode: QR_FP64 or QR_MIXED.  The leading
+// `keep` singular vectors (keep <= 0: all k) are orthonormal to ~1e-11; the rest may be less so
+// when their singular values are many decades below sigma_max (callers then discard them).
 int zsvd_thin(cudaStream_t s, SvdWork* w, int mode, const double2* A, int m, int n, long lda,
-              double2* U, long ldu, double* S, double2* Vh, long ldvh);
+              double2* U, long ldu, double* S, double2* Vh, long ldvh, int keep = 0);
 
 }  // namespace qr

@@ -6,13 +6,13 @@
 // pair.  Converged when no pair has |b_p^H b_q| > tol sqrt(|b_p|^2 |b_q|^2), tol = sqrt(m) eps.
 //
 // QR_MIXED: the same Jacobi in FP32 (FFMA runs ~70x faster than DFMA on GB300) gives
-// approximate right singular vectors X; then FP64 refinement on the DMMA GEMM (Ogita & Aishima,
-// "Iterative refinement for symmetric eigenvalue decomposition", 2018, applied to A^H A):
-//     R = I - X^H X,  B = A X,  S = B^H B,  lt_i = S_ii / (1 - R_ii),
-//     E_ij = (S_ij + lt_j R_ij) / (lt_j - lt_i)   (i != j, separated pairs),  E_ij = R_ij / 2
-//     otherwise,  X <- X (I + E).
-// Each step squares the error of separated pairs, so two steps take FP32 accuracy to FP64.
-// Sigma = column norms of A X in FP64, so singular values and the truncation cutoff are FP64.
+// approximate right singular vectors X.  FP64 then takes over: two Newton-Schulz steps make X
+// unitary to FP64 (DMMA GEMMs), B = A X is formed in FP64, and FP64 Hestenes sweeps polish
+// (B, X); they start from couplings ~1e-5 and converge quadratically, so a few sweeps replace
+// the ~15 of the plain path.  Sigma = column norms of B in FP64, so singular values and the
+// truncation cutoff are FP64.  (A first-order Ogita-Aishima update was tried as the polish and
+// rejected: FP32 couplings (~1e-5 lambda_max) are not small against the lambda gaps of dense
+// random spectra (~5e-4 lambda_max at n = 2048), and the update lost orthogonality.)
 //
 // Left singular vectors are the normalised columns B/sigma.  When the spectrum spans many
 // decades (or has exact zeros) those columns lose orthogonality in proportion to
@@ -20,6 +20,9 @@
 // column's phase, which moves the represented matrix by O(eps sigma_max) only.
 #include <vector>
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cmath>
 #include "kernels.cuh"
 #include "prof.cuh"
 
@@ -63,6 +66,13 @@ namespace {
 
 constexpr int TPB = 256;
 
+// QR_DEBUG=1 in the environment prints sweep counts and refinement residuals to stderr
+bool debug_on() {
+  static int v = -1;
+  if (v < 0) v = getenv("QR_DEBUG") ? 1 : 0;
+  return v == 1;
+}
+
 template <typename T> struct Eps;
 template <> struct Eps<double> { static constexpr double v = 2.220446049250313e-16; };
 template <> struct Eps<float> { static constexpr float v = 1.1920929e-07f; };
@@ -73,16 +83,45 @@ __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
-// One round of the round-robin ordering: warp w handles pair w.
-template <typename T>
-__global__ void __launch_bounds__(TPB) jacobi_round_k(cplx_t<T>* __restrict__ B, long ldb, int m,
-                                                      int n, cplx_t<T>* __restrict__ V, long ldv,
-                                                      int nv, int np, int round, T tol,
-                                                      unsigned* __restrict__ count) {
+// One round of the round-robin (circle) ordering: CTA b handles pair b.  When the column length
+// fits (m <= NT * RPT) both columns stay in registers between the inner products and the
+// rotation, so each round reads and writes every column of B once; V's columns are rotated in a
+// second loop once the rotation is known.
+template <typename T, int NT>
+__device__ __forceinline__ void block_sum4(T& a, T& b, T& c, T& d) {
+  __shared__ T red[4][NT / 32];
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+    c += __shfl_xor_sync(0xffffffffu, c, o);
+    d += __shfl_xor_sync(0xffffffffu, d, o);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) { red[0][w] = a; red[1][w] = b; red[2][w] = c; red[3][w] = d; }
+  __syncthreads();
+  a = b = c = d = T(0);
+#pragma unroll
+  for (int k = 0; k < NT / 32; k++) { a += red[0][k]; b += red[1][k]; c += red[2][k]; d += red[3][k]; }
+}
+
+template <typename C, typename T>
+__device__ __forceinline__ void rot(C& x, C& y, T c, T sr, T si) {
+  C xn, yn;
+  xn.x = c * x.x - (sr * y.x + si * y.y);
+  xn.y = c * x.y - (sr * y.y - si * y.x);
+  yn.x = (sr * x.x - si * x.y) + c * y.x;
+  yn.y = (sr * x.y + si * x.x) + c * y.y;
+  x = xn;
+  y = yn;
+}
+
+template <typename T, int NT, int RPT>
+__global__ void __launch_bounds__(NT) jacobi_round_k(cplx_t<T>* __restrict__ B, long ldb, int m,
+                                                     int n, cplx_t<T>* __restrict__ V, long ldv,
+                                                     int nv, int np, int round, T tol, T smax,
+                                                     unsigned* __restrict__ count) {
   using C = cplx_t<T>;
-  const int lane = threadIdx.x & 31;
-  const int pair = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (pair >= np / 2) return;
+  const int pair = blockIdx.x;
   const int np1 = np - 1;
   int p, q;
   if (pair == 0) { p = round; q = np1; }
@@ -91,43 +130,65 @@ __global__ void __launch_bounds__(TPB) jacobi_round_k(cplx_t<T>* __restrict__ B,
   if (p > q) { int t = p; p = q; q = t; }
   C* bp = B + (long)p * ldb;
   C* bq = B + (long)q * ldb;
+  const bool fits = m <= NT * RPT;
+  C x[RPT], y[RPT];
   T a = 0, b = 0, gr = 0, gi = 0;
-  for (int r = lane; r < m; r += 32) {
-    C x = bp[r], y = bq[r];
-    a += x.x * x.x + x.y * x.y;
-    b += y.x * y.x + y.y * y.y;
-    gr += x.x * y.x + x.y * y.y;  // conj(x) * y
-    gi += x.x * y.y - x.y * y.x;
+  if (fits) {
+#pragma unroll
+    for (int j = 0; j < RPT; j++) {
+      int r = threadIdx.x + j * NT;
+      if (r < m) { x[j] = bp[r]; y[j] = bq[r]; }
+      else { x[j].x = x[j].y = y[j].x = y[j].y = T(0); }
+    }
+#pragma unroll
+    for (int j = 0; j < RPT; j++) {
+      a += x[j].x * x[j].x + x[j].y * x[j].y;
+      b += y[j].x * y[j].x + y[j].y * y[j].y;
+      gr += x[j].x * y[j].x + x[j].y * y[j].y;
+      gi += x[j].x * y[j].y - x[j].y * y[j].x;
+    }
+  } else {
+    for (int r = threadIdx.x; r < m; r += NT) {
+      C u = bp[r], w = bq[r];
+      a += u.x * u.x + u.y * u.y;
+      b += w.x * w.x + w.y * w.y;
+      gr += u.x * w.x + u.y * w.y;
+      gi += u.x * w.y - u.y * w.x;
+    }
   }
-  a = warp_sum(a); b = warp_sum(b); gr = warp_sum(gr); gi = warp_sum(gi);
+  block_sum4<T, NT>(a, b, gr, gi);
   T g = sqrt(gr * gr + gi * gi);
-  if (!(a > 0) || !(b > 0) || !(g > tol * sqrt(a) * sqrt(b))) return;
+  // rotate when the coupling exceeds tol * sigma_max * sigma_min(pair): columns end orthogonal to
+  // the backward-stable (LAPACK-level) accuracy eps * ||A||, without chasing relative accuracy
+  // among columns far below sigma_max
+  if (!(a > 0) || !(b > 0) || !(g > tol * smax * sqrt(a < b ? a : b))) return;
   T zeta = (b - a) / (2 * g);
   T t = (zeta >= 0 ? T(1) : T(-1)) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
   T c = T(1) / sqrt(T(1) + t * t);
   T sr = t * c * gr / g, si = t * c * gi / g;  // s = t c e^{i phi}, gamma = |gamma| e^{i phi}
   // p' = c p - conj(s) q ;  q' = s p + c q
-  for (int r = lane; r < m; r += 32) {
-    C x = bp[r], y = bq[r];
-    C xn, yn;
-    xn.x = c * x.x - (sr * y.x + si * y.y);
-    xn.y = c * x.y - (sr * y.y - si * y.x);
-    yn.x = (sr * x.x - si * x.y) + c * y.x;
-    yn.y = (sr * x.y + si * x.x) + c * y.y;
-    bp[r] = xn; bq[r] = yn;
+  if (fits) {
+#pragma unroll
+    for (int j = 0; j < RPT; j++) {
+      int r = threadIdx.x + j * NT;
+      rot(x[j], y[j], c, sr, si);
+      if (r < m) { bp[r] = x[j]; bq[r] = y[j]; }
+    }
+  } else {
+    for (int r = threadIdx.x; r < m; r += NT) {
+      C u = bp[r], w = bq[r];
+      rot(u, w, c, sr, si);
+      bp[r] = u; bq[r] = w;
+    }
   }
   C* vp = V + (long)p * ldv;
   C* vq = V + (long)q * ldv;
-  for (int r = lane; r < nv; r += 32) {
-    C x = vp[r], y = vq[r];
-    C xn, yn;
-    xn.x = c * x.x - (sr * y.x + si * y.y);
-    xn.y = c * x.y - (sr * y.y - si * y.x);
-    yn.x = (sr * x.x - si * x.y) + c * y.x;
-    yn.y = (sr * x.y + si * x.x) + c * y.y;
-    vp[r] = xn; vq[r] = yn;
+  for (int r = threadIdx.x; r < nv; r += NT) {
+    C u = vp[r], w = vq[r];
+    rot(u, w, c, sr, si);
+    vp[r] = u; vq[r] = w;
   }
-  if (lane == 0) atomicAdd(count, 1u);
+  if (threadIdx.x == 0) atomicAdd(count, 1u);
 }
 
 // nrm[j] = |col_j| in FP64 (one warp per column)
@@ -175,39 +236,6 @@ __global__ void gather_cols_k(const CS* __restrict__ src, long lds, int rows, in
   }
 }
 
-// Ogita-Aishima correction matrix (n x n): see file header.  Returns E; also writes
-// off[0] = max over separated pairs of |S_ij| / sqrt(S_ii S_jj) (as uint bits, atomicMax).
-__global__ void oa_correction_k(const double2* __restrict__ S, const double2* __restrict__ Rm, int n,
-                                double2* __restrict__ E, unsigned long long* __restrict__ off) {
-  long total = (long)n * n;
-  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
-    int i = (int)(t % n), j = (int)(t / n);
-    double2 r = Rm[t];
-    double2 e;
-    if (i == j) {
-      e = make_double2(0.5 * r.x, 0.5 * r.y);
-    } else {
-      double lti = S[i + (long)i * n].x / (1.0 - Rm[i + (long)i * n].x);
-      double ltj = S[j + (long)j * n].x / (1.0 - Rm[j + (long)j * n].x);
-      double2 s = S[t];
-      double2 num = make_double2(s.x + ltj * r.x, s.y + ltj * r.y);
-      double gap = ltj - lti;
-      double an = sqrt(num.x * num.x + num.y * num.y);
-      if (an <= 0.1 * fabs(gap)) {
-        e = make_double2(num.x / gap, num.y / gap);
-      } else {
-        e = make_double2(0.5 * r.x, 0.5 * r.y);
-      }
-      double den = sqrt(fabs(S[i + (long)i * n].x) * fabs(S[j + (long)j * n].x));
-      if (den > 0.0) {
-        double rel = sqrt(s.x * s.x + s.y * s.y) / den;
-        atomicMax(off, (unsigned long long)__double_as_longlong(rel));
-      }
-    }
-    E[t] = e;
-  }
-}
-
 __global__ void add_identity_k(double2* A, int n, long lda, double alpha) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) A[i + (long)i * lda].x += alpha;
@@ -234,17 +262,30 @@ inline unsigned gs(long n) {
 // Hestenes sweeps on B (rows x k) accumulating V (k x k), until no rotation happens.
 template <typename T>
 int jacobi(cudaStream_t s, SvdWork* w, cplx_t<T>* B, long ldb, int rows, int k, cplx_t<T>* V,
-           long ldv, int max_sweeps, T tol) {
+           long ldv, int max_sweeps, T tol, bool must_converge = true) {
   const int np = k + (k & 1);
   unsigned* cnt = w->cnt.as<unsigned>();
-  const unsigned grid = ceil_div((long)(np / 2) * 32, TPB);
+  const unsigned grid = (unsigned)(np / 2);
+  constexpr int NT = sizeof(T) == 8 ? 256 : 128;
+  constexpr int RPT = sizeof(T) == 8 ? 8 : 16;
   const int kind = sizeof(T) == 8 ? PK_JACOBI64 : PK_JACOBI32;
   const double pairs = 0.5 * (double)k * (k - 1);
+  // sigma_max from the largest column norm (the column norms' maximum never exceeds it and is
+  // within a factor sqrt(k) of it; the criterion only needs its scale)
+  double* nrm = w->nrm.as<double>();
+  col_norms_k<cplx_t<T>><<<ceil_div((long)k * 32, TPB), TPB, 0, s>>>(B, ldb, rows, k, nrm);
+  QR_CHECK_LAUNCH("col_norms_k");
+  w->hs.resize(k);
+  QR_CUDA(cudaMemcpyAsync(w->hs.data(), nrm, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+  QR_CUDA(cudaStreamSynchronize(s));
+  double smax_h = 0.0;
+  for (int j = 0; j < k; j++) smax_h = w->hs[j] > smax_h ? w->hs[j] : smax_h;
+  const T smax = (T)smax_h;
   for (int sweep = 0; sweep < max_sweeps; sweep++) {
     QR_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned), s));
     int pr = prof_begin(s, kind, 0.0, 0.0);
     for (int r = 0; r < np - 1; r++) {
-      jacobi_round_k<T><<<grid, TPB, 0, s>>>(B, ldb, rows, k, V, ldv, k, np, r, tol, cnt);
+      jacobi_round_k<T, NT, RPT><<<grid, NT, 0, s>>>(B, ldb, rows, k, V, ldv, k, np, r, tol, smax, cnt);
       QR_CHECK_LAUNCH("jacobi_round_k");
     }
     prof_end(s, pr);
@@ -255,8 +296,10 @@ int jacobi(cudaStream_t s, SvdWork* w, cplx_t<T>* B, long ldb, int rows, int k, 
     // two column rotations of B and V for every rotated pair (20 flops per row and column)
     prof_account(pr, 16.0 * rows * pairs + 20.0 * (double)h * (rows + k) * 2.0,
                  sizeof(cplx_t<T>) * ((double)rows + k) * 2.0 * (pairs + h));
+    if (debug_on()) fprintf(stderr, "[qr] jacobi<%s> %dx%d sweep %d rotations %u\n", sizeof(T) == 8 ? "f64" : "f32", rows, k, sweep, h);
     if (h == 0) return QR_OK;
   }
+  if (!must_converge) return QR_OK;
   return fail(QR_ENOCONV, "Jacobi SVD did not converge");
 }
 
@@ -278,7 +321,7 @@ static int reorthonormalize(cudaStream_t s, SvdWork* w, double2* L, long ldl, in
 }
 
 int zsvd_thin(cudaStream_t s, SvdWork* w, int mode, const double2* A, int m, int n, long lda,
-              double2* U, long ldu, double* S, double2* Vh, long ldvh) {
+              double2* U, long ldu, double* S, double2* Vh, long ldvh, int keep) {
   if (m <= 0 || n <= 0) return QR_OK;
   const bool tall = m >= n;
   const int rows = tall ? m : n;  // B = A (tall) or A^H (wide): rows x k
@@ -287,7 +330,7 @@ int zsvd_thin(cudaStream_t s, SvdWork* w, int mode, const double2* A, int m, int
   QR_TRY(w->V.ensure(sizeof(double2) * (size_t)k * k, s));
   QR_TRY(w->nrm.ensure(sizeof(double) * (size_t)k * 2, s));
   QR_TRY(w->perm.ensure(sizeof(int) * (size_t)k, s));
-  QR_TRY(w->cnt.ensure(sizeof(unsigned long long) * 2, s));
+  QR_TRY(w->cnt.ensure(sizeof(unsigned long long) * 4, s));
   double2* B = w->B.as<double2>();
   double2* V = w->V.as<double2>();
   double* nrm = w->nrm.as<double>();
@@ -314,8 +357,10 @@ int zsvd_thin(cudaStream_t s, SvdWork* w, int mode, const double2* A, int m, int
     float2* V32 = w->V32.as<float2>();
     QR_TRY(z2c(s, B, rows, B32, rows, rows, k));
     QR_TRY(cset_identity(s, V32, k, k, k));
-    float tol32 = sqrtf((float)rows) * Eps<float>::v;
-    QR_TRY(jacobi<float>(s, w, B32, rows, rows, k, V32, k, 40, tol32));
+    // a preconditioner: 1e-5 relative orthogonality is plenty for the FP64 refinement, and sits
+    // above the FP32 rounding floor (~sqrt(m) eps32) so sweeps stop once rotations are noise
+    float tol32 = fmaxf(4e-6f, 2.0f * sqrtf((float)rows) * Eps<float>::v);
+    QR_TRY(jacobi<float>(s, w, B32, rows, rows, k, V32, k, 20, tol32, false));
     // X = V32 sorted by the FP32 column norms (descending), promoted to FP64
     col_norms_k<float2><<<ceil_div((long)k * 32, TPB), TPB, 0, s>>>(B32, rows, rows, k, nrm);
     QR_CHECK_LAUNCH("col_norms_k");
@@ -338,30 +383,23 @@ int zsvd_thin(cudaStream_t s, SvdWork* w, int mode, const double2* A, int m, int
     QR_TRY(w->T1.ensure(sizeof(double2) * (size_t)rows * k, s));
     double2* Asrc = w->T1.as<double2>();
     QR_CUDA(cudaMemcpyAsync(Asrc, Bsrc, sizeof(double2) * (size_t)rows * k, cudaMemcpyDeviceToDevice, s));
-    for (int it = 0; it < 3; it++) {
-      // R = I - X^H X
+    // X must be unitary to FP64 before it can carry the polish rotations: two Newton-Schulz
+    // steps X <- X + X (I - X^H X) / 2 square the FP32-level error twice (1e-5 -> 1e-10 -> 1e-20)
+    const double2 half = make_double2(0.5, 0.0);
+    for (int it = 0; it < 2; it++) {
       QR_TRY(zgemm(s, OP_C, OP_N, k, k, k, mone, X, k, 0, X, k, 0, zero, Rm, k, 0, 1, nullptr));
       add_identity_k<<<ceil_div(k, TPB), TPB, 0, s>>>(Rm, k, k, 1.0);
       QR_CHECK_LAUNCH("add_identity_k");
-      // B = A X ; S = B^H B
-      QR_TRY(zgemm(s, OP_N, OP_N, rows, k, k, one, Asrc, rows, 0, X, k, 0, zero, B, rows, 0, 1, nullptr));
-      QR_TRY(zgemm(s, OP_C, OP_N, k, k, rows, one, B, rows, 0, B, rows, 0, zero, Sm, k, 0, 1, nullptr));
-      QR_CUDA(cudaMemsetAsync(off, 0, sizeof(unsigned long long), s));
-      oa_correction_k<<<gs((long)k * k), TPB, 0, s>>>(Sm, Rm, k, E, off);
-      QR_CHECK_LAUNCH("oa_correction_k");
-      unsigned long long hoff = 0;
-      QR_CUDA(cudaMemcpyAsync(&hoff, off, sizeof(hoff), cudaMemcpyDeviceToHost, s));
-      QR_CUDA(cudaStreamSynchronize(s));
-      double offv;
-      memcpy(&offv, &hoff, sizeof(double));
-      if (offv < 4.0 * Eps<double>::v * sqrt((double)rows) && it > 0) break;
-      // X <- X + X E  (V as scratch)
       QR_CUDA(cudaMemcpyAsync(V, X, sizeof(double2) * (size_t)k * k, cudaMemcpyDeviceToDevice, s));
-      QR_TRY(zgemm(s, OP_N, OP_N, k, k, k, one, V, k, 0, E, k, 0, one, X, k, 0, 1, nullptr));
+      QR_TRY(zgemm(s, OP_N, OP_N, k, k, k, half, V, k, 0, Rm, k, 0, one, X, k, 0, 1, nullptr));
     }
-    // final B = A X, V = X
+    (void)E;
+    (void)Sm;
+    // B = A X, then FP64 Hestenes sweeps on (B, X): they finish the near-degenerate pairs the
+    // first-order step leaves alone and certify orthogonality with the FP64 tolerance
     QR_TRY(zgemm(s, OP_N, OP_N, rows, k, k, one, Asrc, rows, 0, X, k, 0, zero, B, rows, 0, 1, nullptr));
     QR_CUDA(cudaMemcpyAsync(V, X, sizeof(double2) * (size_t)k * k, cudaMemcpyDeviceToDevice, s));
+    QR_TRY(jacobi<double>(s, w, B, rows, rows, k, V, k, 60, sqrt((double)rows) * Eps<double>::v));
   }
 
   // ---- sigma, ordering, factors
@@ -374,8 +412,12 @@ int zsvd_thin(cudaStream_t s, SvdWork* w, int mode, const double2* A, int m, int
   w->hs.resize(k);
   QR_CUDA(cudaMemcpyAsync(w->hs.data(), sorted, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
   QR_CUDA(cudaStreamSynchronize(s));
-  const double smax = w->hs[0], smin = w->hs[k - 1];
-  const bool reorth = !(smin > 1e-6 * smax);
+  // columns that truncation may retain must be orthonormal to ~1e-11: B/sigma columns are
+  // orthogonal to tol * sigma_max / sigma_j, so re-orthonormalise when sigma_keep < 1e-3 sigma_max
+  const int kk = (keep > 0 && keep < k) ? keep : k;
+  const double smax = w->hs[0], smin = w->hs[kk - 1];
+  if (!(smax >= 0.0) || !std::isfinite(smax)) return fail(QR_ENOCONV, "non-finite singular values");
+  const bool reorth = !(smin > 1e-3 * smax);
 
   // left factor L (rows x k) = B[:, perm] / sigma ; right factor Rf (k x k) = V[:, perm]
   QR_TRY(w->E.ensure(sizeof(double2) * (size_t)k * k, s));
@@ -383,7 +425,7 @@ int zsvd_thin(cudaStream_t s, SvdWork* w, int mode, const double2* A, int m, int
   if (tall) {
     gather_cols_k<double2><<<gs((long)rows * k), TPB, 0, s>>>(B, rows, rows, k, perm, sorted, U, ldu);
     QR_CHECK_LAUNCH("gather_cols_k");
-    if (reorth) QR_TRY(reorthonormalize(s, w, U, ldu, m, k));
+    if (reorth) QR_TRY(reorthonormalize(s, w, U, ldu, m, kk));
     gather_cols_k<double2><<<gs((long)k * k), TPB, 0, s>>>(V, k, k, k, perm, nullptr, Rf, k);
     QR_CHECK_LAUNCH("gather_cols_k");
     QR_TRY(ztranspose(s, Rf, k, k, k, Vh, ldvh, 1));  // Vh = Rf^H (k x n)
@@ -393,7 +435,7 @@ int zsvd_thin(cudaStream_t s, SvdWork* w, int mode, const double2* A, int m, int
     double2* L = w->Rm.as<double2>();
     gather_cols_k<double2><<<gs((long)rows * k), TPB, 0, s>>>(B, rows, rows, k, perm, sorted, L, rows);
     QR_CHECK_LAUNCH("gather_cols_k");
-    if (reorth) QR_TRY(reorthonormalize(s, w, L, rows, rows, k));
+    if (reorth) QR_TRY(reorthonormalize(s, w, L, rows, rows, kk));
     gather_cols_k<double2><<<gs((long)k * k), TPB, 0, s>>>(V, k, k, k, perm, nullptr, U, ldu);
     QR_CHECK_LAUNCH("gather_cols_k");
     QR_TRY(ztranspose(s, L, rows, rows, k, Vh, ldvh, 1));

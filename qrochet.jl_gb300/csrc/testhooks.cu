@@ -1,0 +1,127 @@
+// Kernel-level entry points for unit tests and kernel benchmarks: host matrices in, host results
+// and CUDA-event timings out.  They have no counterpart in the reference.
+#include <vector>
+#include "kernels.cuh"
+
+using namespace qr;
+
+namespace {
+struct Dev {
+  void* p = nullptr;
+  ~Dev() {
+    if (p) cudaFree(p);
+  }
+};
+int up(Dev& d, const double* h, size_t n_complex) {
+  QR_CUDA(cudaMalloc(&d.p, sizeof(double2) * (n_complex ? n_complex : 1)));
+  if (h) QR_CUDA(cudaMemcpy(d.p, h, sizeof(double2) * n_complex, cudaMemcpyHostToDevice));
+  return QR_OK;
+}
+}  // namespace
+
+extern "C" {
+
+// C = alpha op(A) diag(dk) op(B) + beta C, column-major; `iters` timed repetitions (C is
+// recomputed from the original each time).  ms_per_iter receives the average event time.
+int qr_test_zgemm(int opA, int opB, int M, int N, int K, const double* alpha, const double* A, long lda,
+                  const double* B, long ldb, const double* beta, double* C, long ldc, const double* dk,
+                  int iters, double* ms_per_iter) {
+  if (M <= 0 || N <= 0 || K < 0 || iters < 1) return fail(QR_EINVAL, "bad gemm shape");
+  long ra = (opA == OP_N || opA == OP_R) ? M : K, ca = (opA == OP_N || opA == OP_R) ? K : M;
+  long rb = (opB == OP_N || opB == OP_R) ? K : N, cb = (opB == OP_N || opB == OP_R) ? N : K;
+  if (lda < ra || ldb < rb || ldc < M) return fail(QR_EINVAL, "bad leading dimension");
+  Dev dA, dB, dC, dC0, dD;
+  QR_TRY(up(dA, A, (size_t)lda * ca));
+  QR_TRY(up(dB, B, (size_t)ldb * cb));
+  QR_TRY(up(dC0, C, (size_t)ldc * N));
+  QR_TRY(up(dC, C, (size_t)ldc * N));
+  if (dk) {
+    QR_CUDA(cudaMalloc(&dD.p, sizeof(double) * (K ? K : 1)));
+    QR_CUDA(cudaMemcpy(dD.p, dk, sizeof(double) * K, cudaMemcpyHostToDevice));
+  }
+  double2 al = make_double2(alpha[0], alpha[1]), be = make_double2(beta[0], beta[1]);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float total = 0;
+  int rc = QR_OK;
+  for (int it = 0; it < iters && rc == QR_OK; it++) {
+    QR_CUDA(cudaMemcpy(dC.p, dC0.p, sizeof(double2) * ldc * N, cudaMemcpyDeviceToDevice));
+    cudaEventRecord(e0);
+    rc = zgemm(0, opA, opB, M, N, K, al, (double2*)dA.p, lda, 0, (double2*)dB.p, ldb, 0, be, (double2*)dC.p, ldc, 0,
+               1, (double*)dD.p);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    total += ms;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  QR_TRY(rc);
+  QR_CUDA(cudaMemcpy(C, dC.p, sizeof(double2) * ldc * N, cudaMemcpyDeviceToHost));
+  if (ms_per_iter) *ms_per_iter = total / iters;
+  return QR_OK;
+}
+
+// Thin SVD of the m x n column-major A: U (m x k), S (k), Vh (k x n), k = min(m, n).
+int qr_test_svd(int mode, int m, int n, const double* A, double* U, double* S, double* Vh, double* ms) {
+  if (m <= 0 || n <= 0) return fail(QR_EINVAL, "bad svd shape");
+  const int k = m < n ? m : n;
+  Dev dA, dU, dV, dS;
+  QR_TRY(up(dA, A, (size_t)m * n));
+  QR_TRY(up(dU, nullptr, (size_t)m * k));
+  QR_TRY(up(dV, nullptr, (size_t)k * n));
+  QR_CUDA(cudaMalloc(&dS.p, sizeof(double) * k));
+  cudaStream_t s;
+  QR_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  SvdWork* w = svd_work_create();
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, s);
+  int rc = zsvd_thin(s, w, mode, (double2*)dA.p, m, n, m, (double2*)dU.p, m, (double*)dS.p, (double2*)dV.p, k);
+  cudaEventRecord(e1, s);
+  cudaStreamSynchronize(s);
+  float t = 0;
+  cudaEventElapsedTime(&t, e0, e1);
+  if (ms) *ms = t;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  svd_work_free(w);
+  cudaStreamDestroy(s);
+  QR_TRY(rc);
+  if (U) QR_CUDA(cudaMemcpy(U, dU.p, sizeof(double2) * m * k, cudaMemcpyDeviceToHost));
+  if (Vh) QR_CUDA(cudaMemcpy(Vh, dV.p, sizeof(double2) * k * n, cudaMemcpyDeviceToHost));
+  if (S) QR_CUDA(cudaMemcpy(S, dS.p, sizeof(double) * k, cudaMemcpyDeviceToHost));
+  return QR_OK;
+}
+
+// Thin Householder QR of the m x n column-major A: Q (m x k), R (k x n).
+int qr_test_qr(int m, int n, const double* A, double* Q, double* R, double* ms) {
+  if (m <= 0 || n <= 0) return fail(QR_EINVAL, "bad qr shape");
+  const int k = m < n ? m : n;
+  Dev dA, dQ, dR, dT;
+  QR_TRY(up(dA, A, (size_t)m * n));
+  QR_TRY(up(dQ, nullptr, (size_t)m * k));
+  QR_TRY(up(dR, nullptr, (size_t)k * n));
+  QR_TRY(up(dT, nullptr, (size_t)k));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0);
+  int rc = zqr_thin(0, (double2*)dA.p, m, n, m, (double2*)dQ.p, m, (double2*)dR.p, k, (double2*)dT.p);
+  cudaEventRecord(e1);
+  cudaEventSynchronize(e1);
+  float t = 0;
+  cudaEventElapsedTime(&t, e0, e1);
+  if (ms) *ms = t;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  QR_TRY(rc);
+  QR_CUDA(cudaMemcpy(Q, dQ.p, sizeof(double2) * m * k, cudaMemcpyDeviceToHost));
+  QR_CUDA(cudaMemcpy(R, dR.p, sizeof(double2) * k * n, cudaMemcpyDeviceToHost));
+  return QR_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,123 @@
+"""Kernel-level GPU checks through the C ABI test hooks: the FP64 DMMA ZGEMM against NumPy, and
+the thin SVD / Householder QR against LAPACK (through NumPy) on tall, wide, rank-deficient and
+graded matrices.  FP64 tolerance 1e-12 relative (GEMM) and 1e-10 relative on gauge-invariant SVD
+quantities (singular values, U S Vh); the mixed SVD is held to the same bar because its singular
+values and vectors come out of the FP64 refinement."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from qrochet import _lib
+from qrochet import random as R
+
+pytestmark = pytest.mark.gpu
+
+OPS = {0: lambda x: x, 1: lambda x: x.T, 2: lambda x: x.conj().T, 3: lambda x: x.conj()}
+
+
+def _p(a):
+    return _lib.dptr(a)
+
+
+def zgemm(opA, opB, A, B, Cm, alpha=1.0, beta=0.0, dk=None):
+    M, N = Cm.shape
+    K = OPS[opA](A).shape[1]
+    A = np.asfortranarray(A, dtype=np.complex128)
+    B = np.asfortranarray(B, dtype=np.complex128)
+    out = np.asfortranarray(Cm, dtype=np.complex128).copy(order="F")
+    al = np.array([complex(alpha).real, complex(alpha).imag])
+    be = np.array([complex(beta).real, complex(beta).imag])
+    ms = C.c_double()
+    dkp = None if dk is None else _p(np.ascontiguousarray(dk, dtype=np.float64))
+    _lib.check(_lib.lib().qr_test_zgemm(opA, opB, M, N, K, _p(al), _p(A), A.shape[0], _p(B), B.shape[0],
+                                        _p(be), _p(out), M, dkp, 1, C.byref(ms)))
+    return out
+
+
+@pytest.mark.parametrize("opA", [0, 1, 2, 3])
+@pytest.mark.parametrize("opB", [0, 1, 2, 3])
+def test_zgemm_ops(opA, opB):
+    g = R.rng(100 + 4 * opA + opB)
+    M, N, K = 77, 45, 130
+    A0 = R.complex_gaussian(g, (M, K))
+    B0 = R.complex_gaussian(g, (K, N))
+    A = OPS[opA](A0) if opA in (0, 3) else A0.T.copy() if opA == 1 else A0.conj().T.copy()
+    B = OPS[opB](B0) if opB in (0, 3) else B0.T.copy() if opB == 1 else B0.conj().T.copy()
+    A = A if opA != 3 else A0.conj()
+    B = B if opB != 3 else B0.conj()
+    Cm = R.complex_gaussian(g, (M, N))
+    alpha, beta = 0.7 - 0.2j, -0.3 + 0.4j
+    dk = g.random(K)
+    got = zgemm(opA, opB, A, B, Cm, alpha, beta, dk)
+    ref = alpha * (OPS[opA](A) * dk[None, :]) @ OPS[opB](B) + beta * Cm
+    assert np.max(np.abs(got - ref)) <= 1e-12 * np.max(np.abs(ref))
+
+
+def test_zgemm_large_exact_tiles():
+    g = R.rng(7)
+    A = R.complex_gaussian(g, (256, 512))
+    B = R.complex_gaussian(g, (512, 192))
+    got = zgemm(0, 0, A, B, np.zeros((256, 192)))
+    assert np.max(np.abs(got - A @ B)) <= 1e-12 * np.max(np.abs(A @ B))
+
+
+def svd(mode, A):
+    A = np.asfortranarray(A, dtype=np.complex128)
+    m, n = A.shape
+    k = min(m, n)
+    U = np.empty((m, k), dtype=np.complex128, order="F")
+    Vh = np.empty((k, n), dtype=np.complex128, order="F")
+    S = np.empty(k)
+    ms = C.c_double()
+    _lib.check(_lib.lib().qr_test_svd(mode, m, n, _p(A), _p(U), _p(S), _p(Vh), C.byref(ms)))
+    return U, S, Vh
+
+
+def _graded(g, m, n, decades):
+    u, _ = np.linalg.qr(R.complex_gaussian(g, (m, min(m, n))))
+    v, _ = np.linalg.qr(R.complex_gaussian(g, (n, min(m, n))))
+    s = np.logspace(0, -decades, min(m, n))
+    return (u * s) @ v.conj().T
+
+
+CASES = {
+    "square": lambda g: R.complex_gaussian(g, (96, 96)),
+    "tall": lambda g: R.complex_gaussian(g, (200, 64)),
+    "wide": lambda g: R.complex_gaussian(g, (48, 130)),
+    "rank2": lambda g: R.complex_gaussian(g, (60, 2)) @ R.complex_gaussian(g, (2, 50)),
+    "graded12": lambda g: _graded(g, 80, 80, 12),
+    "zero_cols": lambda g: np.hstack([R.complex_gaussian(g, (40, 10)), np.zeros((40, 6))]),
+    "tiny": lambda g: R.complex_gaussian(g, (2, 1)),
+}
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_svd_against_lapack(mode, case):
+    g = R.rng(hash(case) % 1000)
+    A = CASES[case](g)
+    U, S, Vh = svd(mode, A)
+    s_ref = np.linalg.svd(A, compute_uv=False)
+    smax = s_ref[0]
+    assert np.all(np.diff(S) <= 1e-14 * smax)  # descending
+    assert np.max(np.abs(S - s_ref)) <= 1e-10 * smax
+    assert np.max(np.abs((U * S) @ Vh - A)) <= 1e-10 * smax * np.sqrt(max(A.shape))
+    k = S.size
+    assert np.max(np.abs(U.conj().T @ U - np.eye(k))) <= 1e-10
+    assert np.max(np.abs(Vh @ Vh.conj().T - np.eye(k))) <= 1e-10
+
+
+def test_qr_against_lapack():
+    g = R.rng(5)
+    for m, n in [(64, 32), (32, 64), (50, 50), (2, 1)]:
+        A = np.asfortranarray(R.complex_gaussian(g, (m, n)))
+        k = min(m, n)
+        Q = np.empty((m, k), dtype=np.complex128, order="F")
+        Rm = np.empty((k, n), dtype=np.complex128, order="F")
+        ms = C.c_double()
+        _lib.check(_lib.lib().qr_test_qr(m, n, _p(A), _p(Q), _p(Rm), C.byref(ms)))
+        assert np.allclose(Q @ Rm, A, atol=1e-12 * np.abs(A).max())
+        assert np.allclose(Q.conj().T @ Q, np.eye(k), atol=1e-12)
+        assert np.allclose(np.tril(Rm, -1), 0)
+        assert np.allclose(np.abs(np.diag(Rm)), np.abs(np.diag(np.linalg.qr(A)[1])), rtol=1e-10)
