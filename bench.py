@@ -48,6 +48,8 @@ def parse():
     p.add_argument("--cpu-steps", type=int, default=2)
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--quick", action="store_true", help="small chi for a fast functional run")
+    p.add_argument("--launch-list", action="store_true",
+                   help="only the warm-up and timed steps of the mixed path (for ncu launch lists)")
     return p.parse_args()
 
 
@@ -232,6 +234,11 @@ def run_ours(args, chi):
     clk = clocks.stop()
     dt_max = dist.max(dt)
     value = world * args.steps / dt_max
+    if args.launch_list:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": "gate-steps/s", "steps": args.steps,
+                              "warmup": args.warmup, "gpu_launches": launches, "mode": "launch-list"}), flush=True)
+        return
 
     # ---- plain FP64 path ---------------------------------------------------------------------------
     fp64 = None

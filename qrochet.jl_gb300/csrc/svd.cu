@@ -21,6 +21,7 @@
 #include <vector>
 #include <algorithm>
 #include <cstdio>
+#include <cstring>
 #include <cstdlib>
 #include <cmath>
 #include "kernels.cuh"
@@ -97,6 +98,7 @@ __device__ __forceinline__ void block_sum4(T& a, T& b, T& c, T& d) {
     d += __shfl_xor_sync(0xffffffffu, d, o);
   }
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();  // previous readers of red are done
   if (l == 0) { red[0][w] = a; red[1][w] = b; red[2][w] = c; red[3][w] = d; }
   __syncthreads();
   a = b = c = d = T(0);
@@ -116,12 +118,11 @@ __device__ __forceinline__ void rot(C& x, C& y, T c, T sr, T si) {
 }
 
 template <typename T, int NT, int RPT>
-__global__ void __launch_bounds__(NT) jacobi_round_k(cplx_t<T>* __restrict__ B, long ldb, int m,
-                                                     int n, cplx_t<T>* __restrict__ V, long ldv,
-                                                     int nv, int np, int round, T tol, T smax,
-                                                     unsigned* __restrict__ count) {
+__device__ __forceinline__ void jacobi_pair(cplx_t<T>* __restrict__ B, long ldb, int m, int n,
+                                            cplx_t<T>* __restrict__ V, long ldv, int nv, int np,
+                                            int round, int pair, T tol, T smax,
+                                            unsigned* __restrict__ count) {
   using C = cplx_t<T>;
-  const int pair = blockIdx.x;
   const int np1 = np - 1;
   int p, q;
   if (pair == 0) { p = round; q = np1; }
@@ -188,8 +189,57 @@ __global__ void __launch_bounds__(NT) jacobi_round_k(cplx_t<T>* __restrict__ B, 
     rot(u, w, c, sr, si);
     vp[r] = u; vq[r] = w;
   }
-  if (threadIdx.x == 0) atomicAdd(count, 1u);
+  if (threadIdx.x == 0) {
+    atomicAdd(count, 1u);
+    atomicMax(count + 1, __float_as_uint((float)fabs(t)));  // largest rotation tangent of the sweep
+  }
 }
+
+// Grid-wide barrier for a cooperative launch (all CTAs resident).  The wait is bounded: after
+// ~2^22 polls (about a second) the CTA records a timeout in bar[2] and proceeds; every CTA checks
+// bar[2] after the barrier and leaves the sweep, so the kernel always returns.
+__device__ __forceinline__ bool grid_barrier(unsigned* bar) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned* vb = bar;
+    const unsigned gen = vb[1];
+    __threadfence();
+    const unsigned arrived = atomicAdd(&bar[0], 1u) + 1u;
+    if (arrived == gridDim.x) {
+      atomicExch(&bar[0], 0u);
+      __threadfence();
+      atomicAdd(&bar[1], 1u);
+    } else {
+      unsigned polls = 0;
+      while (vb[1] == gen) {
+        if (++polls > (1u << 22)) {
+          atomicExch(&bar[2], 1u);
+          break;
+        }
+        __nanosleep(200);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return ((volatile unsigned*)bar)[2] == 0u;
+}
+
+// One full sweep (np-1 rounds) in one cooperative launch: CTAs stride over the round's pairs.
+template <typename T, int NT, int RPT>
+__global__ void __launch_bounds__(NT) jacobi_sweep_k(cplx_t<T>* __restrict__ B, long ldb, int m, int n,
+                                                     cplx_t<T>* __restrict__ V, long ldv, int np, T tol,
+                                                     T smax, unsigned* __restrict__ count,
+                                                     unsigned* __restrict__ bar) {
+  const int npairs = np / 2;
+  for (int round = 0; round < np - 1; round++) {
+    for (int pair = blockIdx.x; pair < npairs; pair += gridDim.x)
+      jacobi_pair<T, NT, RPT>(B, ldb, m, n, V, ldv, n, np, round, pair, tol, smax, count);
+    if (!grid_barrier(bar)) return;
+  }
+}
+
+
 
 // nrm[j] = |col_j| in FP64 (one warp per column)
 template <typename C>
@@ -265,9 +315,18 @@ int jacobi(cudaStream_t s, SvdWork* w, cplx_t<T>* B, long ldb, int rows, int k, 
            long ldv, int max_sweeps, T tol, bool must_converge = true) {
   const int np = k + (k & 1);
   unsigned* cnt = w->cnt.as<unsigned>();
-  const unsigned grid = (unsigned)(np / 2);
+  unsigned* bar = cnt + 4;
   constexpr int NT = sizeof(T) == 8 ? 256 : 128;
   constexpr int RPT = sizeof(T) == 8 ? 8 : 16;
+  // persistent cooperative grid: as many CTAs as can be resident, at most one per pair
+  int dev = 0, sms = 0, per_sm = 0;
+  QR_CUDA(cudaGetDevice(&dev));
+  QR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  QR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, jacobi_sweep_k<T, NT, RPT>, NT, 0));
+  if (per_sm < 1) return fail(QR_ECUDA, "Jacobi sweep kernel cannot be resident");
+  int grid = per_sm * sms;
+  if (grid > np / 2) grid = np / 2;
+  if (grid < 1) grid = 1;
   const int kind = sizeof(T) == 8 ? PK_JACOBI64 : PK_JACOBI32;
   const double pairs = 0.5 * (double)k * (k - 1);
   // sigma_max from the largest column norm (the column norms' maximum never exceeds it and is
@@ -282,22 +341,38 @@ int jacobi(cudaStream_t s, SvdWork* w, cplx_t<T>* B, long ldb, int rows, int k, 
   for (int j = 0; j < k; j++) smax_h = w->hs[j] > smax_h ? w->hs[j] : smax_h;
   const T smax = (T)smax_h;
   for (int sweep = 0; sweep < max_sweeps; sweep++) {
-    QR_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned), s));
+    QR_CUDA(cudaMemsetAsync(cnt, 0, 8 * sizeof(unsigned), s));
     int pr = prof_begin(s, kind, 0.0, 0.0);
-    for (int r = 0; r < np - 1; r++) {
-      jacobi_round_k<T, NT, RPT><<<grid, NT, 0, s>>>(B, ldb, rows, k, V, ldv, k, np, r, tol, smax, cnt);
-      QR_CHECK_LAUNCH("jacobi_round_k");
+    {
+      cplx_t<T>* Bp = B;
+      cplx_t<T>* Vp = V;
+      int mm = rows, kk2 = k, npp = np;
+      long ldbb = ldb, ldvv = ldv;
+      T tl = tol, sm = smax;
+      void* args[] = {&Bp, &ldbb, &mm, &kk2, &Vp, &ldvv, &npp, &tl, &sm, &cnt, &bar};
+      QR_CUDA(cudaLaunchCooperativeKernel((const void*)jacobi_sweep_k<T, NT, RPT>, dim3(grid), dim3(NT), args, 0, s));
+      count_launch();
     }
     prof_end(s, pr);
-    unsigned h = 0;
-    QR_CUDA(cudaMemcpyAsync(&h, cnt, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    unsigned hh[3] = {0, 0, 0};
+    QR_CUDA(cudaMemcpyAsync(hh, cnt, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    QR_CUDA(cudaMemcpyAsync(hh + 2, bar + 2, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
     QR_CUDA(cudaStreamSynchronize(s));
+    if (hh[2]) return fail(QR_ECUDA, "Jacobi sweep: grid barrier timed out");
+    const unsigned h = hh[0];
+    float tmax;
+    memcpy(&tmax, &hh[1], sizeof(float));
     // algorithmic work of the sweep: three inner products per pair (16 real flops per row) and
     // two column rotations of B and V for every rotated pair (20 flops per row and column)
     prof_account(pr, 16.0 * rows * pairs + 20.0 * (double)h * (rows + k) * 2.0,
                  sizeof(cplx_t<T>) * ((double)rows + k) * 2.0 * (pairs + h));
-    if (debug_on()) fprintf(stderr, "[qr] jacobi<%s> %dx%d sweep %d rotations %u\n", sizeof(T) == 8 ? "f64" : "f32", rows, k, sweep, h);
+    if (debug_on())
+      fprintf(stderr, "[qr] jacobi<%s> %dx%d sweep %d rotations %u max tan %.2e\n", sizeof(T) == 8 ? "f64" : "f32",
+              rows, k, sweep, h, tmax);
     if (h == 0) return QR_OK;
+    // a sweep whose rotations were all below tau leaves couplings O(tau^2): with tau < 1e-8 in
+    // FP64 the next sweep would find nothing above the tolerance, so it is skipped
+    if (sizeof(T) == 8 && tmax < 1e-8f) return QR_OK;
   }
   if (!must_converge) return QR_OK;
   return fail(QR_ENOCONV, "Jacobi SVD did not converge");
@@ -330,7 +405,7 @@ int zsvd_thin(cudaStream_t s, SvdWork* w, int mode, const double2* A, int m, int
   QR_TRY(w->V.ensure(sizeof(double2) * (size_t)k * k, s));
   QR_TRY(w->nrm.ensure(sizeof(double) * (size_t)k * 2, s));
   QR_TRY(w->perm.ensure(sizeof(int) * (size_t)k, s));
-  QR_TRY(w->cnt.ensure(sizeof(unsigned long long) * 4, s));
+  QR_TRY(w->cnt.ensure(sizeof(unsigned) * 8, s));
   double2* B = w->B.as<double2>();
   double2* V = w->V.as<double2>();
   double* nrm = w->nrm.as<double>();

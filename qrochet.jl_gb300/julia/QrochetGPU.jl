@@ -1,0 +1,203 @@
+# QrochetGPU.jl -- Julia binding of libqrochet_gpu.so (include/qrochet_gpu.h).
+#
+# Adds methods of Qrochet's Chain API on a device-resident `GPUChain`, so existing Julia code
+# that calls canonize!/evolve!/expect/overlap/norm on a Chain can run them on a GB300.  Every
+# method is a thin `ccall`; status codes become the exceptions Qrochet throws.
+#
+# Not executed in this repository's CI: the build image has no Julia.  The Python package in
+# ../qrochet calls the same symbols with the same arguments and is tested on the GPU.
+module QrochetGPU
+
+using LinearAlgebra
+import Qrochet
+using Qrochet: Chain, Site, Dense, Open, State, MissingSchmidtCoefficientsException
+
+const libqrochet = get(ENV, "QROCHET_GPU_LIB", joinpath(@__DIR__, "..", "lib", "libqrochet_gpu.so"))
+
+const QR_OK, QR_EINVAL, QR_EASSERT, QR_ENO_SCHMIDT, QR_EDIM = 0, 1, 2, 3, 4
+const QR_FP64, QR_MIXED = 0, 1
+const QR_DIR_LEFT, QR_DIR_RIGHT = 0, 1
+const QR_METHOD_QR, QR_METHOD_SVD = 0, 1
+
+lasterror() = unsafe_string(ccall((:qr_last_error_string, libqrochet), Cstring, ()))
+
+function check(rc::Cint, bond = nothing)
+    rc == QR_OK && return nothing
+    msg = lasterror()
+    rc == QR_EINVAL && throw(ArgumentError(msg))
+    rc == QR_EASSERT && throw(AssertionError(msg))
+    rc == QR_ENO_SCHMIDT && throw(MissingSchmidtCoefficientsException(bond))
+    rc == QR_EDIM && throw(DimensionMismatch(msg))
+    error("libqrochet_gpu: status $rc: $msg")
+end
+
+"""
+    GPUChain(arrays; order = (:o, :l, :r), precision = :fp64)
+
+Open-boundary MPS resident on the GPU, built from the same arrays as `MPS(arrays)`
+(`Chain(State(), Open(), arrays; order)`).
+"""
+mutable struct GPUChain
+    handle::Ptr{Cvoid}
+    n::Int
+    d::Int
+end
+
+function GPUChain(arrays::Vector{<:AbstractArray}; order = (:o, :l, :r), precision = :fp64)
+    n = length(arrays)
+    ord = collect(order)
+    dims = map(enumerate(arrays)) do (i, a)
+        sub = filter(x -> !((i == 1 && x == :l) || (i == n && x == :r)), ord)
+        Dict(zip(sub, size(a)))
+    end
+    d = dims[1][:o]
+    bonds = Cint[dims[i][:r] for i in 1:n-1]
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:qr_chain_create, libqrochet), Cint, (Cint, Cint, Ptr{Cint}, Ref{Ptr{Cvoid}}), n, d, bonds, h))
+    chain = GPUChain(h[], n, d)
+    finalizer(c -> ccall((:qr_chain_free, libqrochet), Cint, (Ptr{Cvoid},), c.handle), chain)
+    ordstr = join(String.(ord))
+    for (i, a) in enumerate(arrays)
+        buf = convert(Array{ComplexF64}, a)
+        check(ccall((:qr_chain_upload_site, libqrochet), Cint, (Ptr{Cvoid}, Cint, Ptr{ComplexF64}, Cstring),
+                    chain.handle, i - 1, buf, ordstr))
+    end
+    setprecision!(chain, precision)
+    return chain
+end
+
+setprecision!(c::GPUChain, p::Symbol) =
+    check(ccall((:qr_chain_set_precision, libqrochet), Cint, (Ptr{Cvoid}, Cint), c.handle,
+                p === :mixed ? QR_MIXED : QR_FP64))
+
+function Base.copy(c::GPUChain)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:qr_chain_copy, libqrochet), Cint, (Ptr{Cvoid}, Ref{Ptr{Cvoid}}), c.handle, h))
+    out = GPUChain(h[], c.n, c.d)
+    finalizer(x -> ccall((:qr_chain_free, libqrochet), Cint, (Ptr{Cvoid},), x.handle), out)
+    return out
+end
+
+Qrochet.nsites(c::GPUChain) = c.n
+
+function bond_dims(c::GPUChain)
+    out = Vector{Cint}(undef, c.n - 1)
+    check(ccall((:qr_chain_bond_dims, libqrochet), Cint, (Ptr{Cvoid}, Ptr{Cint}), c.handle, out))
+    return Int.(out)
+end
+
+"""Site tensor `i` back on the host, dims in `order` (`arrays(::Chain)` layout)."""
+function sitearray(c::GPUChain, i::Integer; order = (:o, :l, :r))
+    cl, d, cr = Ref{Cint}(0), Ref{Cint}(0), Ref{Cint}(0)
+    check(ccall((:qr_chain_site_dims, libqrochet), Cint, (Ptr{Cvoid}, Cint, Ref{Cint}, Ref{Cint}, Ref{Cint}),
+                c.handle, i - 1, cl, d, cr))
+    dims = Dict(:l => cl[], :o => d[], :r => cr[])
+    sub = filter(x -> !((i == 1 && x == :l) || (i == c.n && x == :r)), collect(order))
+    out = Array{ComplexF64}(undef, (dims[x] for x in sub)...)
+    check(ccall((:qr_chain_download_site, libqrochet), Cint, (Ptr{Cvoid}, Cint, Ptr{ComplexF64}, Cstring),
+                c.handle, i - 1, out, join(String.(collect(order)))))
+    return out
+end
+
+"""Λ on the bond between sites `i` and `i+1` (`tensors(tn; between)`), or `nothing`."""
+function spectrum(c::GPUChain, i::Integer)
+    flag = Ref{Cint}(0)
+    check(ccall((:qr_chain_has_lambda, libqrochet), Cint, (Ptr{Cvoid}, Cint, Ref{Cint}), c.handle, i - 1, flag))
+    flag[] == 0 && return nothing
+    len = Ref{Cint}(0)
+    check(ccall((:qr_chain_get_lambda, libqrochet), Cint, (Ptr{Cvoid}, Cint, Ptr{Float64}, Ref{Cint}),
+                c.handle, i - 1, C_NULL, len))
+    out = Vector{Float64}(undef, len[])
+    check(ccall((:qr_chain_get_lambda, libqrochet), Cint, (Ptr{Cvoid}, Cint, Ptr{Float64}, Ref{Cint}),
+                c.handle, i - 1, out, len))
+    return out
+end
+
+# ---- the reference's Chain methods ----------------------------------------------------------
+_dir(d::Symbol) = d === :left ? QR_DIR_LEFT : d === :right ? QR_DIR_RIGHT : throw(ArgumentError("Unknown direction=:$d"))
+_method(m::Symbol) = m === :qr ? QR_METHOD_QR : m === :svd ? QR_METHOD_SVD : throw(ArgumentError("Unknown factorization method=:$m"))
+
+function Qrochet.canonize_site!(c::GPUChain, site::Site; direction::Symbol, method = :qr)
+    check(ccall((:qr_canonize_site, libqrochet), Cint, (Ptr{Cvoid}, Cint, Cint, Cint), c.handle,
+                Qrochet.id(site) - 1, _dir(direction), _method(method)))
+    return c
+end
+
+Qrochet.canonize!(c::GPUChain) = (check(ccall((:qr_canonize, libqrochet), Cint, (Ptr{Cvoid},), c.handle)); c)
+Qrochet.canonize(c::GPUChain) = Qrochet.canonize!(copy(c))
+
+Qrochet.mixed_canonize!(c::GPUChain, center::Site) =
+    (check(ccall((:qr_mixed_canonize, libqrochet), Cint, (Ptr{Cvoid}, Cint), c.handle, Qrochet.id(center) - 1)); c)
+
+LinearAlgebra.normalize!(c::GPUChain, root::Site) =
+    (check(ccall((:qr_normalize, libqrochet), Cint, (Ptr{Cvoid}, Cint), c.handle, Qrochet.id(root) - 1)); c)
+
+function Qrochet.truncate!(c::GPUChain, bond; threshold = nothing, maxdim = nothing)
+    s1, s2 = Qrochet.id.(bond)
+    check(ccall((:qr_truncate, libqrochet), Cint, (Ptr{Cvoid}, Cint, Cint, Cdouble, Cint), c.handle, s1 - 1, s2 - 1,
+                isnothing(threshold) ? NaN : Float64(threshold), isnothing(maxdim) ? -1 : maxdim), Tuple(bond))
+    return c
+end
+
+"""Row-major M[(o_1..o_k),(i_1..i_k)] (left lane slowest) of a Dense gate for `lanes`."""
+function gatematrix(gate::Dense, lanes)
+    arr = only(Qrochet.arrays(gate))
+    ind = Qrochet.inds(gate; at = Site(first(lanes)))  # dims follow `sites` (Dense.jl:21-34)
+    sites = [s for s in Qrochet.sites(gate)]
+    perm = vcat([findfirst(==(Site(l)), sites) for l in lanes], [findfirst(==(Site(l; dual = true)), sites) for l in lanes])
+    t = permutedims(arr, perm)
+    d = size(t, 1)
+    k = length(lanes)
+    # column-major reshape groups the first lane fastest; reverse lanes to make it slowest
+    t = permutedims(t, vcat(reverse(1:k), reverse(k+1:2k)))
+    M = reshape(t, d^k, d^k)
+    return collect(transpose(M))  # row-major storage of M
+end
+
+function Qrochet.evolve!(c::GPUChain, gate::Dense; threshold = nothing, maxdim = nothing, iscanonical = false,
+                         renormalize = false)
+    lanes = sort!(map(Qrochet.id, Qrochet.outputs(gate)))
+    length(lanes) > 2 && throw(ArgumentError("Invalid number of lanes $(length(lanes)), maximum is 2"))
+    length(lanes) == 2 && lanes[2] != lanes[1] + 1 && throw(ArgumentError("Gate lanes must be contiguous"))
+    M = ComplexF64.(gatematrix(gate, lanes))
+    if length(lanes) == 1
+        check(ccall((:qr_evolve_1site, libqrochet), Cint, (Ptr{Cvoid}, Cint, Ptr{ComplexF64}), c.handle, lanes[1] - 1, M))
+    else
+        check(ccall((:qr_evolve_2site, libqrochet), Cint,
+                    (Ptr{Cvoid}, Cint, Ptr{ComplexF64}, Cdouble, Cint, Cint, Cint), c.handle, lanes[1] - 1, M,
+                    isnothing(threshold) ? NaN : Float64(threshold), isnothing(maxdim) ? -1 : maxdim,
+                    iscanonical, renormalize))
+    end
+    return c
+end
+
+function Qrochet.overlap(a::GPUChain, b::GPUChain)
+    out = Ref{ComplexF64}(0)
+    check(ccall((:qr_overlap, libqrochet), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ref{ComplexF64}), a.handle, b.handle, out))
+    return out[]
+end
+
+function LinearAlgebra.norm(c::GPUChain, p::Real = 2)
+    p == 2 || throw(ArgumentError("only L2-norm is implemented yet"))
+    out = Ref{Float64}(0)
+    check(ccall((:qr_norm, libqrochet), Cint, (Ptr{Cvoid}, Ref{Float64}), c.handle, out))
+    return out[]
+end
+
+function Qrochet.expect(c::GPUChain, observables)
+    firsts, nl, mats = Cint[], Cint[], ComplexF64[]
+    for o in observables
+        lanes = sort!(map(Qrochet.id, Qrochet.outputs(o)))
+        push!(firsts, lanes[1] - 1)
+        push!(nl, length(lanes))
+        append!(mats, vec(permutedims(gatematrix(o, lanes))))  # row-major flattening
+    end
+    out = Ref{ComplexF64}(0)
+    check(ccall((:qr_expect, libqrochet), Cint, (Ptr{Cvoid}, Cint, Ptr{Cint}, Ptr{Cint}, Ptr{ComplexF64}, Ref{ComplexF64}),
+                c.handle, length(firsts), firsts, nl, mats, out))
+    return out[]
+end
+
+export GPUChain, bond_dims, sitearray, spectrum, setprecision!
+
+end # module

@@ -1,0 +1,67 @@
+"""Kernel-level benchmark of the library's hot kernels through the C ABI test hooks.
+
+    python qrochet.jl_gb300/kernel_bench.py zgemm M N K [iters]
+    python qrochet.jl_gb300/kernel_bench.py svd fp64|mixed N [M]
+    python qrochet.jl_gb300/kernel_bench.py qr M N
+
+Inputs are seeded complex Gaussians; prints one JSON line with the event-timed duration, the
+algorithmic flop count and the achieved rate.  Used for ncu captures of single kernels.
+"""
+import ctypes as C
+import json
+import os
+import sys
+
+import numpy as np
+
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+from qrochet import _lib  # noqa: E402
+from qrochet import random as R  # noqa: E402
+
+p = _lib.dptr
+
+
+def main(argv):
+    L = _lib.lib()
+    g = R.rng(1)
+    what = argv[0]
+    if what == "zgemm":
+        M, N, K = (int(x) for x in argv[1:4])
+        iters = int(argv[4]) if len(argv) > 4 else 3
+        A = np.asfortranarray(R.complex_gaussian(g, (M, K)))
+        B = np.asfortranarray(R.complex_gaussian(g, (K, N)))
+        Cm = np.zeros((M, N), dtype=np.complex128, order="F")
+        ms = C.c_double()
+        _lib.check(L.qr_test_zgemm(0, 0, M, N, K, p(np.array([1.0, 0.0])), p(A), M, p(B), K, p(np.zeros(2)), p(Cm),
+                                   M, None, iters, C.byref(ms)))
+        fl = 8.0 * M * N * K
+        out = {"op": "zgemm", "M": M, "N": N, "K": K, "ms": ms.value, "tflops": fl / ms.value / 1e9}
+    elif what == "svd":
+        mode = {"fp64": 0, "mixed": 1}[argv[1]]
+        n = int(argv[2])
+        m = int(argv[3]) if len(argv) > 3 else n
+        A = np.asfortranarray(R.complex_gaussian(g, (m, n)))
+        k = min(m, n)
+        U = np.empty((m, k), dtype=np.complex128, order="F")
+        Vh = np.empty((k, n), dtype=np.complex128, order="F")
+        S = np.empty(k)
+        ms = C.c_double()
+        _lib.check(L.qr_test_svd(mode, m, n, p(A), p(U), p(S), p(Vh), C.byref(ms)))
+        out = {"op": "svd", "mode": argv[1], "m": m, "n": n, "ms": ms.value,
+               "recon": float(np.max(np.abs((U * S) @ Vh - A)) / S[0])}
+    elif what == "qr":
+        m, n = int(argv[1]), int(argv[2])
+        A = np.asfortranarray(R.complex_gaussian(g, (m, n)))
+        k = min(m, n)
+        Q = np.empty((m, k), dtype=np.complex128, order="F")
+        Rm = np.empty((k, n), dtype=np.complex128, order="F")
+        ms = C.c_double()
+        _lib.check(L.qr_test_qr(m, n, p(A), p(Q), p(Rm), C.byref(ms)))
+        out = {"op": "qr", "m": m, "n": n, "ms": ms.value}
+    else:
+        raise SystemExit(__doc__)
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])
