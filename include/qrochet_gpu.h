@@ -131,6 +131,19 @@ int qr_mpo_free(qr_mpo* w);
 int qr_mpo_upload_site(qr_mpo* w, int site, const double* host, const char* order);
 int qr_mpo_expect(const qr_chain* h, const qr_mpo* w, double* out);
 
+/* ---- allocation-free thin SVD (no counterpart in the reference) ----------------------------
+   For callers that must not have a library allocate device memory (a Julia process whose CUDA.jl
+   pool owns the device, a serving loop that allocates only at start-up).  Plain FP64 Jacobi SVD
+   A = U diag(S) Vh of the column-major m x n A, all in caller-owned device buffers (complex
+   interleaved; U m x k, S k doubles, Vh k x n, k = min(m,n)), ordered on `stream` (a
+   cudaStream_t, 0 = legacy default) and complete on return.  Limit: max(m,n) <= 512 and
+   min(m,n) <= 256, larger sizes return QR_EINVAL.  Scratch is one ~5.3 MB static device array per
+   device, reserved while the library is loaded and shared by all calls: calls that overlap on the
+   GPU (other threads or streams) race on it.  The first call on a device looks up the array's
+   device address; make that first call before any stream capture.  No cudaMalloc/cudaFree. */
+int qr_svd_noalloc(int m, int n, const double* A, long lda, double* U, long ldu, double* S, double* Vh,
+                   long ldvh, void* stream);
+
 /* ---- kernel-level test hooks (no reference counterpart): host matrices in and out, complex
    interleaved, column-major; op codes 0 N, 1 T, 2 C (conjugate transpose), 3 R (conjugate) ----- */
 int qr_test_zgemm(int opA, int opB, int M, int N, int K, const double* alpha, const double* A, long lda,

@@ -24,6 +24,7 @@
 #include <cstring>
 #include <cstdlib>
 #include <cmath>
+#include <mutex>
 #include "kernels.cuh"
 #include "prof.cuh"
 
@@ -518,4 +519,168 @@ int zsvd_thin(cudaStream_t s, SvdWork* w, int mode, const double2* A, int m, int
   return QR_OK;
 }
 
+
+// =================================================================================================
+// Allocation-free thin SVD.
+//
+// Some callers cannot let a library call cudaMalloc: a Julia process whose CUDA.jl pool owns the
+// device memory (an allocation behind its back breaks its accounting and can fail under its
+// memory pressure), or a serving loop that may only allocate at start-up.  For them,
+// qr_svd_noalloc runs the plain FP64 Jacobi SVD on caller-owned device buffers with all scratch
+// in the file-scope array below, sized for matrices up to QR_NOALLOC_MAX_ROWS x
+// QR_NOALLOC_MAX_K (rows = max(m, n), k = min(m, n)); the array stays reserved on every device
+// that loads the library until the process exits.
+// =================================================================================================
+namespace {
+constexpr int NOALLOC_MAX_ROWS = 512;
+constexpr int NOALLOC_MAX_K = 256;
+constexpr size_t NA_B = (size_t)NOALLOC_MAX_ROWS * NOALLOC_MAX_K;  // B, later the QR copy
+constexpr size_t NA_V = (size_t)NOALLOC_MAX_K * NOALLOC_MAX_K;     // V, later the R factor
+constexpr size_t NA_L = (size_t)NOALLOC_MAX_ROWS * NOALLOC_MAX_K;  // gathered left/right factor
+constexpr size_t NA_BYTES = sizeof(double2) * (NA_B + NA_V + NA_L + NOALLOC_MAX_K) +
+                            sizeof(double) * 2 * NOALLOC_MAX_K + sizeof(int) * NOALLOC_MAX_K +
+                            sizeof(unsigned) * 8;
+constexpr int NA_MAX_DEVICES = 64;
+
+__device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
+
+std::mutex g_na_mu;
+void* g_na_ptr[NA_MAX_DEVICES] = {nullptr};
+
+// The symbol's device address, looked up once per device with that device current.  In host
+// code `g_noalloc_scratch` names a host-side stand-in, not device memory, so kernels must be
+// given this address instead.
+int noalloc_scratch(void** out) {
+  int dev = 0;
+  QR_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= NA_MAX_DEVICES) return fail(QR_EINVAL, "qr_svd_noalloc: device index out of range");
+  std::lock_guard<std::mutex> lk(g_na_mu);
+  if (!g_na_ptr[dev]) {
+    void* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "qr_svd_noalloc: cudaGetSymbolAddress");
+    g_na_ptr[dev] = ptr;
+  }
+  *out = g_na_ptr[dev];
+  return QR_OK;
+}
+}  // namespace
+
+}  // namespace qr
+
+using namespace qr;
+
+extern "C" int qr_svd_noalloc(int m, int n, const double* A, long lda, double* U, long ldu, double* S, double* Vh,
+                              long ldvh, void* stream) {
+  if (m <= 0 || n <= 0) return fail(QR_EINVAL, "qr_svd_noalloc: empty matrix");
+  if (!A || !U || !S || !Vh) return fail(QR_EINVAL, "qr_svd_noalloc: null buffer");
+  const bool tall = m >= n;
+  const int rows = tall ? m : n, k = tall ? n : m;
+  if (rows > NOALLOC_MAX_ROWS || k > NOALLOC_MAX_K)
+    return fail(QR_EINVAL, "qr_svd_noalloc: matrix exceeds the 512 x 256 scratch limit (max(m,n) <= 512, "
+                           "min(m,n) <= 256); use the allocating SVD for larger blocks");
+  if (lda < m || ldu < m || ldvh < k) return fail(QR_EINVAL, "qr_svd_noalloc: bad leading dimension");
+  cudaStream_t s = (cudaStream_t)stream;
+  void* base = nullptr;
+  QR_TRY(noalloc_scratch(&base));
+  double2* B = (double2*)base;
+  double2* V = B + NA_B;
+  double2* L = V + NA_V;
+  double2* tau = L + NA_L;
+  double* nrm = (double*)(tau + NOALLOC_MAX_K);
+  double* sorted = nrm + NOALLOC_MAX_K;
+  int* perm = (int*)(sorted + NOALLOC_MAX_K);
+  unsigned* cnt = (unsigned*)(perm + NOALLOC_MAX_K);
+  unsigned* bar = cnt + 4;
+  const double2* Ad = (const double2*)A;
+
+  // B = A (tall) or A^H (wide); V = I: every buffer read below is written first
+  if (tall) {
+    QR_CUDA(cudaMemcpy2DAsync(B, sizeof(double2) * rows, Ad, sizeof(double2) * lda, sizeof(double2) * m, n,
+                              cudaMemcpyDeviceToDevice, s));
+  } else {
+    QR_TRY(ztranspose(s, Ad, lda, m, n, B, rows, 1));
+  }
+  QR_TRY(zset_identity(s, V, k, k, k));
+
+  // sigma_max scale for the rotation criterion (host copy into a stack array: no allocation)
+  double hn[NOALLOC_MAX_K];
+  col_norms_k<double2><<<ceil_div((long)k * 32, TPB), TPB, 0, s>>>(B, rows, rows, k, nrm);
+  QR_CHECK_LAUNCH("col_norms_k");
+  QR_CUDA(cudaMemcpyAsync(hn, nrm, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+  QR_CUDA(cudaStreamSynchronize(s));
+  double smax = 0.0;
+  for (int j = 0; j < k; j++) smax = hn[j] > smax ? hn[j] : smax;
+
+  constexpr int NT = 256, RPT = 8;
+  const int np = k + (k & 1);
+  int dev = 0, sms = 0, per_sm = 0;
+  QR_CUDA(cudaGetDevice(&dev));
+  QR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  QR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, jacobi_sweep_k<double, NT, RPT>, NT, 0));
+  int grid = per_sm * sms;
+  if (grid > np / 2) grid = np / 2;
+  if (grid < 1) grid = 1;
+  double tol = sqrt((double)rows) * Eps<double>::v;
+  bool converged = false;
+  for (int sweep = 0; sweep < 60 && !converged; sweep++) {
+    // counters and the grid barrier start every sweep at zero
+    QR_CUDA(cudaMemsetAsync(cnt, 0, 8 * sizeof(unsigned), s));
+    double2* Bp = B;
+    double2* Vp = V;
+    int mm = rows, kk = k, npp = np;
+    long ldbb = rows, ldvv = k;
+    double tl = tol, sm = smax;
+    void* args[] = {&Bp, &ldbb, &mm, &kk, &Vp, &ldvv, &npp, &tl, &sm, &cnt, &bar};
+    QR_CUDA(cudaLaunchCooperativeKernel((const void*)jacobi_sweep_k<double, NT, RPT>, dim3(grid), dim3(NT), args, 0, s));
+    count_launch();
+    unsigned hh[3] = {0, 0, 0};
+    QR_CUDA(cudaMemcpyAsync(hh, cnt, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    QR_CUDA(cudaMemcpyAsync(hh + 2, bar + 2, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    QR_CUDA(cudaStreamSynchronize(s));
+    if (hh[2]) return fail(QR_ECUDA, "qr_svd_noalloc: grid barrier timed out");
+    float tmax;
+    memcpy(&tmax, &hh[1], sizeof(float));
+    converged = hh[0] == 0 || tmax < 1e-8f;
+  }
+  if (!converged) return fail(QR_ENOCONV, "qr_svd_noalloc: Jacobi SVD did not converge");
+
+  col_norms_k<double2><<<ceil_div((long)k * 32, TPB), TPB, 0, s>>>(B, rows, rows, k, nrm);
+  QR_CHECK_LAUNCH("col_norms_k");
+  rank_sort_k<<<ceil_div(k, TPB), TPB, 0, s>>>(nrm, k, perm, sorted);
+  QR_CHECK_LAUNCH("rank_sort_k");
+  QR_CUDA(cudaMemcpyAsync(S, sorted, sizeof(double) * k, cudaMemcpyDeviceToDevice, s));
+  QR_CUDA(cudaMemcpyAsync(hn, sorted, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+  QR_CUDA(cudaStreamSynchronize(s));
+  if (!(hn[0] >= 0.0) || !std::isfinite(hn[0])) return fail(QR_ENOCONV, "qr_svd_noalloc: non-finite singular values");
+  const bool reorth = !(hn[k - 1] > 1e-3 * hn[0]);
+
+  // left factor Lf (rows x k) = B[:, perm] / sigma ; right factor (k x k) = V[:, perm]
+  double2* Ud = (double2*)U;
+  double2* Lf = tall ? Ud : L;
+  const long ldl = tall ? ldu : rows;
+  double2* Rf = tall ? L : Ud;
+  const long ldr = tall ? k : ldu;
+  gather_cols_k<double2><<<gs((long)rows * k), TPB, 0, s>>>(B, rows, rows, k, perm, sorted, Lf, ldl);
+  QR_CHECK_LAUNCH("gather_cols_k");
+  gather_cols_k<double2><<<gs((long)k * k), TPB, 0, s>>>(V, k, k, k, perm, nullptr, Rf, ldr);
+  QR_CHECK_LAUNCH("gather_cols_k");
+  if (reorth) {
+    // B and V are free now: QR copy in B, R in V
+    QR_CUDA(cudaMemcpy2DAsync(B, sizeof(double2) * rows, Lf, sizeof(double2) * ldl, sizeof(double2) * rows, k,
+                              cudaMemcpyDeviceToDevice, s));
+    QR_TRY(zqr_thin(s, B, rows, k, rows, Lf, ldl, V, k, tau));
+    phase_fix_k<<<gs((long)rows * k), TPB, 0, s>>>(Lf, ldl, rows, k, V, k);
+    QR_CHECK_LAUNCH("phase_fix_k");
+  }
+  if (tall) {
+    QR_TRY(ztranspose(s, Rf, k, k, k, (double2*)Vh, ldvh, 1));  // Vh = Rf^H
+  } else {
+    QR_TRY(ztranspose(s, Lf, ldl, rows, k, (double2*)Vh, ldvh, 1));  // Vh = L^H
+  }
+  QR_CUDA(cudaStreamSynchronize(s));
+  return QR_OK;
+}
+
+namespace qr {
 }  // namespace qr
