@@ -50,10 +50,12 @@ typedef struct qr_mpo qr_mpo;     /* one open-boundary MPO resident in device me
 #define QR_ENODEV 7       /* no CUDA device */
 #define QR_ENOCONV 8      /* SVD sweeps did not converge */
 
-/* Precision of a chain's arithmetic (qr_chain_set_precision). */
-#define QR_FP64 0  /* plain: all ComplexF64 */
-#define QR_MIXED 1 /* FP32 Jacobi preconditioner + FP64 refinement for SVD; split-precision
-                      tensor-core contractions for environment sweeps */
+/* Precision of a chain's arithmetic (qr_chain_set_precision), a bit mask. */
+#define QR_FP64 0           /* plain: all ComplexF64 */
+#define QR_MIXED 1          /* SVD: FP32 Jacobi preconditioner + FP64 Newton-Schulz and Jacobi polish
+                               (singular values/vectors and the truncation cutoff stay FP64) */
+#define QR_SPLIT_CONTRACT 2 /* environment contractions (expect, overlap, norm, MPO expectation) on
+                               the BF16 tensor cores with 3-way BF16 splits, FP32 accumulation */
 
 #define QR_DIR_LEFT 0
 #define QR_DIR_RIGHT 1
@@ -69,7 +71,8 @@ int qr_set_device(int device);
 int qr_launch_count(uint64_t* count);
 
 /* per-kernel-class CUDA-event timing, for benchmarks: kinds 0 zgemm (FP64 DMMA), 1 Jacobi FP64,
-   2 Jacobi FP32, 3 Householder QR, 4 environment mixing.  No reference counterpart. */
+   2 Jacobi FP32, 3 Householder QR, 4 environment mixing, 5 split-precision tensor-core zgemm.
+   No reference counterpart. */
 int qr_prof_enable(int on);
 int qr_prof_read(int kind, double* ms, uint64_t* launches, double* flops, double* bytes);
 /* peak of one pipe measured now: 0 FP64 tensor (DMMA), 1 FP32 FFMA, 2 FP64 DFMA (TFLOP/s) */
@@ -149,6 +152,8 @@ int qr_svd_noalloc(int m, int n, const double* A, long lda, double* U, long ldu,
 int qr_test_zgemm(int opA, int opB, int M, int N, int K, const double* alpha, const double* A, long lda,
                   const double* B, long ldb, const double* beta, double* C, long ldc, const double* dk,
                   int iters, double* ms_per_iter);
+int qr_test_zgemm_split(int opA, int opB, int M, int N, int K, const double* A, long lda, const double* B,
+                        long ldb, double* C, long ldc, int iters, double* ms_per_iter);
 int qr_test_svd(int mode, int m, int n, const double* A, double* U, double* S, double* Vh, double* ms);
 int qr_test_qr(int m, int n, const double* A, double* Q, double* R, double* ms);
 

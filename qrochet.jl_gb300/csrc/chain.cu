@@ -170,6 +170,8 @@ Perm make_perm(const std::string& hord, const std::string& iord, const long* idi
   return p;
 }
 
+inline int svd_mode(const qr_chain* h) { return (h->precision & QR_MIXED) ? QR_MIXED : QR_FP64; }
+
 int check_site(const qr_chain* h, int i) {
   if (!h) return fail(QR_EINVAL, "null chain");
   if (i < 0 || i >= h->n) return fail(QR_EINVAL, "site out of range");
@@ -205,7 +207,7 @@ int canonize_site_impl(qr_chain* h, int i, int dir, int method) {
       QR_CUDA(cudaMemcpyAsync(W, h->site[i], sizeof(double2) * (size_t)m * nn, cudaMemcpyDeviceToDevice, s));
       QR_TRY(zqr_thin(s, W, m, nn, m, Q, m, Rr, k, tau));
     } else {
-      QR_TRY(zsvd_thin(s, h->svd, h->precision, h->site[i], m, nn, m, Q, m, S, Rr, k));
+      QR_TRY(zsvd_thin(s, h->svd, svd_mode(h), h->site[i], m, nn, m, Q, m, S, Rr, k));
     }
     // next site <- R diag(Lambda_i) A_{i+1}
     double2* nxt = nullptr;
@@ -231,7 +233,7 @@ int canonize_site_impl(qr_chain* h, int i, int dir, int method) {
     if (method == QR_METHOD_QR) {
       QR_TRY(zqr_thin(s, W, m, nn, m, Q, m, Rr, k, tau));
     } else {
-      QR_TRY(zsvd_thin(s, h->svd, h->precision, W, m, nn, m, Q, m, S, Rr, k));
+      QR_TRY(zsvd_thin(s, h->svd, svd_mode(h), W, m, nn, m, Q, m, S, Rr, k));
     }
     double2* cur = nullptr;
     QR_TRY(dalloc((void**)&cur, sizeof(double2) * (size_t)k * m, s));
@@ -345,7 +347,7 @@ int evolve2_impl(qr_chain* h, int sl, const double* g, double threshold, int max
   double2 *U = nullptr, *Vh = nullptr;
   QR_TRY(dalloc((void**)&U, sizeof(double2) * (size_t)m * k, s));
   QR_TRY(dalloc((void**)&Vh, sizeof(double2) * (size_t)k * nn, s));
-  QR_TRY(zsvd_thin(s, h->svd, h->precision, th, m, nn, m, U, m, S, Vh, k, maxdim >= 0 ? maxdim : 0));
+  QR_TRY(zsvd_thin(s, h->svd, svd_mode(h), th, m, nn, m, U, m, S, Vh, k, maxdim >= 0 ? maxdim : 0));
   set_site(h, sl, U);
   set_site(h, sr, Vh);
   h->bd[sl] = k;
@@ -404,8 +406,12 @@ struct EnvOps {
   std::vector<int> wl, wr;
 };
 
+// In QR_MIXED the two contractions of every site step run on the BF16 tensor cores
+// (zgemm_split, ~FP32 accuracy); the operator mixing, Lambda scaling and the stored environments
+// stay FP64.
 int env_sweep(const qr_chain* a, const qr_chain* b, const EnvOps* ops, cudaStream_t s, double out[2]) {
   const int n = a->n, d = a->d;
+  const bool split = (a->precision & QR_SPLIT_CONTRACT) != 0;
   // largest buffers
   size_t maxE = 1, maxX = 1;
   for (int i = 0; i < n; i++) {
@@ -437,7 +443,9 @@ int env_sweep(const qr_chain* a, const qr_chain* b, const EnvOps* ops, cudaStrea
       count_launch();
     }
     // X[(w,b) x (i,a')] = E^T A
-    rc = zgemm(s, OP_T, OP_N, wl * cb, d * ca2, ca, one, E0, ca, 0, a->site[i], ca, 0, zero, X, wl * cb, 0, 1, nullptr);
+    rc = split ? zgemm_split(s, OP_T, OP_N, wl * cb, d * ca2, ca, E0, ca, 0, a->site[i], ca, 0, X, wl * cb, 0, 1)
+               : zgemm(s, OP_T, OP_N, wl * cb, d * ca2, ca, one, E0, ca, 0, a->site[i], ca, 0, zero, X, wl * cb, 0, 1,
+                       nullptr);
     if (rc) break;
     const double2* Yp = X;
     if (W) {
@@ -448,8 +456,10 @@ int env_sweep(const qr_chain* a, const qr_chain* b, const EnvOps* ops, cudaStrea
       Yp = Y;
     }
     // E'_w' = Y_w'^T conj(B)
-    rc = zgemm(s, OP_T, OP_R, ca2, cb2, cb * d, one, Yp, (long)cb * d * wr, (long)cb * d, b->site[i], (long)cb * d, 0,
-               zero, E1, (long)ca2 * wr, ca2, wr, nullptr);
+    rc = split ? zgemm_split(s, OP_T, OP_R, ca2, cb2, cb * d, Yp, (long)cb * d * wr, (long)cb * d, b->site[i],
+                             (long)cb * d, 0, E1, (long)ca2 * wr, ca2, wr)
+               : zgemm(s, OP_T, OP_R, ca2, cb2, cb * d, one, Yp, (long)cb * d * wr, (long)cb * d, b->site[i],
+                       (long)cb * d, 0, zero, E1, (long)ca2 * wr, ca2, wr, nullptr);
     std::swap(E0, E1);
   }
   if (rc == QR_OK) {
@@ -660,7 +670,8 @@ int qr_chain_nsites(const qr_chain* h, int* out) {
 
 int qr_chain_set_precision(qr_chain* h, int mode) {
   if (!h) return fail(QR_EINVAL, "null chain");
-  if (mode != QR_FP64 && mode != QR_MIXED) return fail(QR_EINVAL, "precision must be QR_FP64 or QR_MIXED");
+  if (mode < 0 || mode > (QR_MIXED | QR_SPLIT_CONTRACT))
+    return fail(QR_EINVAL, "precision must be a combination of QR_MIXED and QR_SPLIT_CONTRACT");
   h->precision = mode;
   return QR_OK;
 }

@@ -11,6 +11,10 @@ int zgemm(cudaStream_t s, int opA, int opB, int M, int N, int K, double2 alpha,
           const double2* A, long lda, long sA, const double2* B, long ldb, long sB,
           double2 beta, double2* C, long ldc, long sC, int batch, const double* dk);
 
+// ---- gemm_split.cu: C = op(A) op(B) on the BF16 tensor cores, 3-way BF16 split, FP32 accumulate
+int zgemm_split(cudaStream_t s, int opA, int opB, int M, int N, int K, const double2* A, long lda, long sA,
+                const double2* B, long ldb, long sB, double2* C, long ldc, long sC, int batch);
+
 // ---- misc.cu -----------------------------------------------------------------------------------
 int zscale_matrix(cudaStream_t s, int M, int N, double2 alpha, double2* C, long ldc, long sC,
                   int batch);

@@ -28,7 +28,9 @@ class Periodic:
 
 _DIR = {"left": L.QR_DIR_LEFT, "right": L.QR_DIR_RIGHT}
 _METHOD = {"qr": L.QR_METHOD_QR, "svd": L.QR_METHOD_SVD}
-_PREC = {"fp64": L.QR_FP64, "mixed": L.QR_MIXED}
+# "mixed": FP32-preconditioned SVD with FP64 refinement; "split": environment contractions on the
+# BF16 tensor cores (3-way split, FP32 accumulation); "mixed+split": both
+_PREC = {"fp64": 0, "mixed": 1, "split": 2, "mixed+split": 3}
 
 
 def _norm_order(order, letters):
@@ -468,7 +470,8 @@ def probe_peak(kind):
     return out.value
 
 
-PROF_KINDS = {"zgemm_dmma": 0, "jacobi_fp64": 1, "jacobi_fp32": 2, "householder_qr": 3, "env_mix": 4}
+PROF_KINDS = {"zgemm_dmma": 0, "jacobi_fp64": 1, "jacobi_fp32": 2, "householder_qr": 3, "env_mix": 4,
+              "zgemm_split_bf16": 5}
 
 
 def prof_enable(on=True):

@@ -306,3 +306,34 @@ def test_rank_deficient_and_zero_singular_values():
     O.evolve_2site_(ref, 1, np.eye(4))
     _check_same(psi, ref)
     assert Q.isleftcanonical(psi, 2)
+
+
+# Split-precision environment contractions (QR_SPLIT_CONTRACT): ~FP32 accuracy per site step.
+SPLIT_RTOL = 1e-5
+
+
+def test_split_contractions_match_fp64():
+    n = 10
+    psi, ref = _pair(n, 24, seed=91)
+    phi, refp = _pair(n, 16, seed=92)
+    for p in (psi, phi):
+        p.set_precision("mixed+split")
+    arrs = R.xxz_mpo_arrays(n, 1.0, 0.7)
+    H = Q.MPO(arrs)
+    ws = []
+    for i, a in enumerate(arrs):
+        a = np.asarray(a)
+        if i == 0:
+            a = a[:, :, None, :]
+        elif i == n - 1:
+            a = a[:, :, :, None]
+        ws.append(np.transpose(a, (2, 0, 1, 3)))
+    e_ref = O.mpo_expect(ref, ws)
+    assert abs(Q.mpo_expect(psi, H) - e_ref) <= SPLIT_RTOL * abs(O.norm(ref)) ** 2 * 10
+    assert abs(Q.overlap(psi, phi) - O.overlap(ref, refp)) <= SPLIT_RTOL * O.norm(ref) * O.norm(refp)
+    assert abs(Q.norm(psi) - O.norm(ref)) <= SPLIT_RTOL * O.norm(ref)
+    zz = np.kron(R.PAULI["Z"], R.PAULI["Z"])
+    e = Q.expect(psi, [Q.gate_from_matrix(zz, [4, 5])])
+    e_o = O.expect(ref, [O.ODense(zz.reshape(2, 2, 2, 2), (O.OSite(4), O.OSite(5), O.OSite(4, True),
+                                                           O.OSite(5, True)))])
+    assert abs(e - e_o) <= SPLIT_RTOL * abs(O.norm(ref)) ** 2
