@@ -134,6 +134,27 @@ int qr_mpo_free(qr_mpo* w);
 int qr_mpo_upload_site(qr_mpo* w, int site, const double* host, const char* order);
 int qr_mpo_expect(const qr_chain* h, const qr_mpo* w, double* out);
 
+/* ---- request server: continuous batching of simulate-and-measure requests (no reference
+   counterpart; the reference has no serving layer).  A request is a circuit of two-site gates on
+   |0...0> (evolve! with `threshold` and maxdim = chi_max; gate g acts on sites gate_site[g] and
+   gate_site[g]+1 with the 4x4 row-major complex matrix at gate_mats + 32 g) followed by Pauli
+   strings (string j: obs_weight[j] entries of (site, code 0 I / 1 X / 2 Y / 3 Z), packed).  Requests
+   are admitted FIFO when their device-memory footprint (qr_server_footprint) fits the budget;
+   each of `workers` threads runs one admitted request on its own chain and stream, so admitted
+   requests overlap on the GPU.  Results are the unnormalised <psi|P|psi> per string (re, im). */
+typedef struct qr_server qr_server;
+int qr_server_create(int device, int workers, uint64_t hbm_budget_bytes, int precision, qr_server** out);
+int qr_server_free(qr_server* s); /* finishes queued work, then joins the workers */
+int qr_server_footprint(int n, int chi_max, uint64_t* bytes);
+int qr_server_submit(qr_server* s, int n, int chi_max, double threshold, int ngates, const int* gate_site,
+                     const double* gate_mats, int nobs, const int* obs_weight, const int* obs_sites,
+                     const int* obs_paulis, uint64_t* ticket);
+/* timeout_s < 0 waits forever; *done = 0 on timeout.  *status is the request's own status. */
+int qr_server_wait(qr_server* s, uint64_t ticket, double timeout_s, int* done, int* status, double* results,
+                   double* latency_ms, double* queue_ms);
+int qr_server_stats(qr_server* s, uint64_t* submitted, uint64_t* completed, int* in_flight, uint64_t* hbm_in_use,
+                    int* queued);
+
 /* ---- allocation-free thin SVD (no counterpart in the reference) ----------------------------
    For callers that must not have a library allocate device memory (a Julia process whose CUDA.jl
    pool owns the device, a serving loop that allocates only at start-up).  Plain FP64 Jacobi SVD

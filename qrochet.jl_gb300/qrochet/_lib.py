@@ -88,6 +88,12 @@ SIGNATURES = {
     "qr_mpo_free": [_P],
     "qr_mpo_upload_site": [_P, _I, _PD, _S],
     "qr_mpo_expect": [_P, _P, _PD],
+    "qr_server_create": [_I, _I, C.c_uint64, _I, C.POINTER(_P)],
+    "qr_server_free": [_P],
+    "qr_server_footprint": [_I, _I, C.POINTER(C.c_uint64)],
+    "qr_server_submit": [_P, _I, _I, _D, _I, _PI, _PD, _I, _PI, _PI, _PI, C.POINTER(C.c_uint64)],
+    "qr_server_wait": [_P, C.c_uint64, _D, _PI, _PI, _PD, _PD, _PD],
+    "qr_server_stats": [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), _PI, C.POINTER(C.c_uint64), _PI],
     "qr_svd_noalloc": [_I, _I, _P, C.c_long, _P, C.c_long, _P, _P, C.c_long, _P],
     "qr_test_zgemm": [_I, _I, _I, _I, _I, _PD, _PD, C.c_long, _PD, C.c_long, _PD, _PD, C.c_long, _PD, _I, _PD],
     "qr_test_zgemm_split": [_I, _I, _I, _I, _I, _PD, C.c_long, _PD, C.c_long, _PD, C.c_long, _I, _PD],
