@@ -50,6 +50,10 @@ def parse():
     p.add_argument("--quick", action="store_true", help="small chi for a fast functional run")
     p.add_argument("--launch-list", action="store_true",
                    help="only the warm-up and timed steps of the mixed path (for ncu launch lists)")
+    p.add_argument("--batched", type=int, default=32, help="requests in the batched sample (0: skip)")
+    p.add_argument("--serve", type=int, default=32, help="requests in the serving sample (0: skip)")
+    p.add_argument("--mpo-sites", type=int, default=128, help="sites of the MPO environment sweep (0: skip)")
+    p.add_argument("--workers", type=int, default=16)
     return p.parse_args()
 
 
@@ -159,6 +163,103 @@ def cpu_gate_step(al, ar, lam, u, maxdim):
     ch.lam[1] = lam
     O.evolve_2site_(ch, 1, u, threshold=CUTOFF, maxdim=maxdim)
     return ch
+
+
+def run_batched(args, Q):
+    """Batched solves/s: requests of the batched distribution (n ~ U[8,96], depth ~ U[4,32],
+    cutoff 1e-10, mixed precision) all submitted at once to the continuous-batching server.
+    chi_max is drawn log-uniformly from {16, 32, 64} (a bounded sample of the {16..512} range:
+    chi_max = 512 requests take minutes each at this part's FP64 rate)."""
+    from qrochet import serve as S
+
+    reqs = S.batched_requests(args.batched, seed=4, chi_log2=(4, 6), nobs=1)
+    gates = sum(len(r.gates) for r in reqs)
+    with S.Server(workers=args.workers, precision="mixed") as sv:
+        t0 = time.perf_counter()
+        tickets = [sv.submit(r) for r in reqs]
+        lat = [sv.wait(t)["latency_ms"] for t in tickets]
+        dt = time.perf_counter() - t0
+    return {"requests": len(reqs), "solves_per_s": len(reqs) / dt, "gate_steps_per_s": gates / dt,
+            "wall_s": dt, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "workers": args.workers, "precision": "mixed",
+            "sample": "n~U[8,96], depth~U[4,32], chi_max log-uniform in {16,32,64}, cutoff 1e-10, seed 4"}
+
+
+def run_serving(args, Q):
+    """Serving: Poisson arrivals at 200 req/s of random brick-wall circuits with 8 Pauli strings of
+    weight 1-4; p50/p99 latency and solves/s for the FP64 and mixed forms.  Bounded sample:
+    n ~ U[16,64], depth ~ U[4,16], chi_max in {32, 128}."""
+    from qrochet import serve as S
+    from qrochet import random as R
+
+    out = {}
+    for prec in ("fp64", "mixed"):
+        g = R.rng(5)
+        reqs = [S.random_request(g, n_range=(16, 64), depth_range=(4, 16), chi_choices=(32, 128), nobs=8)
+                for _ in range(args.serve)]
+        gaps = g.exponential(1.0 / 200.0, size=len(reqs))
+        with S.Server(workers=args.workers, precision=prec) as sv:
+            tickets = []
+            t0 = time.perf_counter()
+            for r, gap in zip(reqs, gaps):
+                time.sleep(gap)
+                tickets.append(sv.submit(r))
+            res = [sv.wait(t) for t in tickets]
+            dt = time.perf_counter() - t0
+        lat = np.array([x["latency_ms"] for x in res])
+        out[prec] = {"requests": len(reqs), "solves_per_s": len(reqs) / dt, "p50_ms": float(np.percentile(lat, 50)),
+                     "p99_ms": float(np.percentile(lat, 99)),
+                     "p99_over_p50": float(np.percentile(lat, 99) / np.percentile(lat, 50)),
+                     "values": [x["values"] for x in res]}
+    err = max(float(np.max(np.abs(a - b))) for a, b in zip(out["fp64"]["values"], out["mixed"]["values"]))
+    for prec in out:
+        del out[prec]["values"]
+    out["max_abs_expectation_diff_mixed_vs_fp64"] = err
+    out["arrival_rate_per_s"] = 200
+    out["workers"] = args.workers
+    out["sample"] = "n~U[16,64], depth~U[4,16], chi_max in {32,128}, 8 Pauli strings of weight 1-4, seed 5"
+    return out
+
+
+def run_mpo_env(args, Q):
+    """MPS-MPO expectation of the Heisenberg XXZ MPO (Jz=1, Jxy=0.7, w=5) on an n-site chi=1024
+    MPS: one left-to-right environment sweep in split precision (BF16x3 tensor cores) and in FP64.
+    The state has complex Gaussian sites scaled by 1/sqrt(2 chi) (norm O(1)); canonize! is not
+    timed (the sweep's cost does not depend on the gauge).  Each site is scaled by
+    1/sqrt(2 chi_l) so the transfer operator keeps the environments O(1) along the chain."""
+    from qrochet import random as R
+
+    n, chi = args.mpo_sites, 1024
+    g = R.rng(3)
+    arrays = []
+    for i in range(n):
+        cl = 1 if i == 0 else min(chi, 2 ** i, 2 ** (n - i))
+        cr = 1 if i == n - 1 else min(chi, 2 ** (i + 1), 2 ** (n - i - 1))
+        a = (g.standard_normal((2, cl, cr), dtype=np.float32) + 1j * g.standard_normal((2, cl, cr),
+                                                                                   dtype=np.float32))
+        a = (a.astype(np.complex128) * (1.0 / np.sqrt(2.0 * 2 * cl)))
+        arrays.append(np.asfortranarray(a[:, 0, :] if i == 0 else a[:, :, 0] if i == n - 1 else a))
+    psi = Q.MPS(arrays)
+    del arrays
+    H = Q.MPO(R.xxz_mpo_arrays(n, 1.0, 0.7))
+    res = {}
+    for prec in ("mixed+split", "fp64"):
+        psi.set_precision(prec)
+        Q.mpo_expect(psi, H) if prec == "mixed+split" else None  # warm-up of the split path
+        psi.sync()
+        t0 = time.perf_counter()
+        e = Q.mpo_expect(psi, H)
+        res[prec] = (time.perf_counter() - t0, e)
+    (ts, es), (td, ed) = res["mixed+split"], res["fp64"]
+    bonds = [1] + [min(chi, 2 ** (i + 1), 2 ** (n - i - 1)) for i in range(n - 1)] + [1]
+    wdim = [1] + [5] * (n - 1) + [1]
+    flops = sum(8.0 * (wdim[i] * bonds[i] * 2 * bonds[i + 1] * bonds[i] + bonds[i + 1] * bonds[i + 1] * 2 * bonds[i] *
+                       wdim[i + 1]) for i in range(n))
+    return {"n": n, "chi": chi, "w": 5, "split_ms_per_sweep": 1e3 * ts, "fp64_ms_per_sweep": 1e3 * td,
+            "split_over_fp64": td / ts, "rel_err_split_vs_fp64": abs(es - ed) / abs(ed),
+            "energy_fp64": [ed.real, ed.imag], "split_tflops_complex_equiv": flops / ts / 1e12,
+            "note": "sites complex Gaussian / sqrt(2 chi_l); bond dims min(1024, 2^i) mirrored; "
+                    "flops = algorithmic count of both contractions over the actual bond dims"}
 
 
 def run_reference(args, chi):
@@ -328,6 +429,10 @@ def run_ours(args, chi):
                "sample": f"{args.cpu_steps} gate-steps at chi={chi} (NumPy/LAPACK zgesdd restatement, all host "
                          f"threads)"}
 
+    batched = run_batched(args, Q) if (args.batched > 0 and not args.quick) else None
+    serving = run_serving(args, Q) if (args.serve > 0 and not args.quick) else None
+    mpo_env = run_mpo_env(args, Q) if (args.mpo_sites > 0 and not args.quick) else None
+
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "gate-steps/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1e3 * dt_max / args.steps, "higher_is_better": True,
@@ -340,7 +445,8 @@ def run_ours(args, chi):
                            "l2": "inputs larger than L2 (>129 MB touched per step)"},
                 "fp64": fp64, "mixed_over_fp64": (value / fp64["value"]) if fp64 else None,
                 "gflop_per_step": gate_flops(chi) / 1e9, "e2e": e2e, "gpu_launches": launches,
-                "roofline": roofline, "cpu_baseline": cpu, "clocks": clk}
+                "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
+                "batched": batched, "serving": serving, "mpo_env": mpo_env}
         print(json.dumps(line), flush=True)
 
 

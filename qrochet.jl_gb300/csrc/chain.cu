@@ -41,6 +41,12 @@ static void init_pool() {
   if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
     uint64_t thr = UINT64_MAX;
     cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    // Chains run concurrently on their own streams (the request server's workers).  Memory freed
+    // on one stream is only reused by another once the free has completed, instead of through an
+    // inserted cross-stream dependency that would chain the workers' streams together.
+    int off = 0;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolReuseAllowInternalDependencies, &off);
+    cudaMemPoolSetAttribute(pool, cudaMemPoolReuseAllowOpportunistic, &off);
   }
 }
 
@@ -57,6 +63,7 @@ struct qr_chain {
   std::vector<int> lamlen;
   SvdWork* svd = nullptr;
   double2* gate = nullptr;        // d^4 complex scratch for gate matrices
+  double2* gate_host = nullptr;   // pinned staging for gate uploads (async H2D)
   double2* ws = nullptr;          // theta / factorisation workspace
   size_t ws_cap = 0;
   double* scal = nullptr;         // small device scalars
@@ -118,8 +125,11 @@ int put_lambda(qr_chain* h, int b, const double* src, int len) {
   return QR_OK;
 }
 
+// Gates are staged through a pinned buffer so the copy does not wait for the stream; every
+// entry point synchronises before returning, so the buffer is free again on the next call.
 int upload_gate(qr_chain* h, const double* g, int dim) {
-  QR_CUDA(cudaMemcpyAsync(h->gate, g, sizeof(double2) * dim * dim, cudaMemcpyHostToDevice, h->stream));
+  std::memcpy(h->gate_host, g, sizeof(double2) * dim * dim);
+  QR_CUDA(cudaMemcpyAsync(h->gate, h->gate_host, sizeof(double2) * dim * dim, cudaMemcpyHostToDevice, h->stream));
   return QR_OK;
 }
 
@@ -529,6 +539,7 @@ int qr_chain_create(int n, int d, const int* bond_dims, qr_chain** out) {
   if (e != cudaSuccess) { delete h; return cuda_fail(e, "cudaStreamCreate"); }
   h->svd = svd_work_create();
   int rc = dalloc((void**)&h->gate, sizeof(double2) * 256, h->stream);
+  if (!rc) rc = cuda_ok(cudaHostAlloc((void**)&h->gate_host, sizeof(double2) * 256, cudaHostAllocDefault), "cudaHostAlloc");
   if (!rc) rc = dalloc((void**)&h->scal, sizeof(double) * 16, h->stream);
   for (int i = 0; i < n && !rc; i++) {
     rc = dalloc((void**)&h->site[i], sizeof(double2) * h->elems(i), h->stream);
@@ -545,6 +556,7 @@ int qr_chain_free(qr_chain* h) {
   for (auto p : h->site) if (p) cudaFree(p);
   for (auto p : h->lam) if (p) cudaFree(p);
   if (h->gate) cudaFree(h->gate);
+  if (h->gate_host) cudaFreeHost(h->gate_host);
   if (h->scal) cudaFree(h->scal);
   if (h->ws) cudaFree(h->ws);
   svd_work_free(h->svd);

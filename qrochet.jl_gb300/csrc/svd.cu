@@ -160,10 +160,12 @@ __device__ __forceinline__ void jacobi_pair(cplx_t<T>* __restrict__ B, long ldb,
   }
   block_sum4<T, NT>(a, b, gr, gi);
   T g = sqrt(gr * gr + gi * gi);
-  // rotate when the coupling exceeds tol * sigma_max * sigma_min(pair): columns end orthogonal to
-  // the backward-stable (LAPACK-level) accuracy eps * ||A||, without chasing relative accuracy
-  // among columns far below sigma_max
-  if (!(a > 0) || !(b > 0) || !(g > tol * smax * sqrt(a < b ? a : b))) return;
+  // rotate when the coupling exceeds tol * sigma_max * sigma_min(pair) plus a floor at the
+  // rounding level (4 eps sigma_max)^2: columns end orthogonal to the backward-stable
+  // (LAPACK-level) accuracy eps * ||A||, without chasing relative accuracy among columns far below
+  // sigma_max, and pairs of columns that are rounding noise (rank-deficient blocks) stop rotating
+  const T fl = T(4) * Eps<T>::v * smax;
+  if (!(a > 0) || !(b > 0) || !(g > tol * smax * sqrt(a < b ? a : b) + fl * fl)) return;
   T zeta = (b - a) / (2 * g);
   T t = (zeta >= 0 ? T(1) : T(-1)) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
   T c = T(1) / sqrt(T(1) + t * t);
@@ -242,6 +244,259 @@ __global__ void __launch_bounds__(NT) jacobi_sweep_k(cplx_t<T>* __restrict__ B, 
 
 
 
+// Rotation of the pair (p, q) from its Gram entries a = |b_p|^2, b = |b_q|^2, gamma = b_p^H b_q,
+// for columns pre-scaled so that sigma_max ~ 1.  The angle is computed in FP32 (b - a first in
+// the working precision, so near-degenerate pairs do not cancel); c = 1/sqrt(1 + t^2) and the unit
+// phase gamma/|gamma| are then formed in the working precision from FP32 seeds and two Newton
+// steps, so the rotation is unitary to working precision while FP64 square roots and divisions --
+// expensive on this part -- are avoided.  A slightly inexact angle only leaves a coupling a
+// factor ~1e-7 smaller, which the next sweep removes.
+template <typename T>
+__device__ __forceinline__ bool rotation_params(T a, T b, T gr, T gi, T tol, T smax, T& c, T& sr, T& si, float& tabs) {
+  const T g2 = gr * gr + gi * gi;
+  const T fl = T(4) * Eps<T>::v * smax;
+  const T mn = a < b ? a : b;
+  // g > tol smax sqrt(min(a, b)) + fl^2, compared in squares
+  if (!(a > 0) || !(b > 0) || !(g2 > tol * tol * smax * smax * mn + fl * fl * fl * fl)) return false;
+  // 1/|gamma| in working precision: FP32 seed of the exponent-normalised g2 (exact scaling), then
+  // two Newton steps; gamma may be far below FP32 range while still above the rotation floor
+  int e2 = 0;
+  const T g2n = frexp(g2, &e2);  // g2 = g2n * 2^e2, g2n in [0.5, 1)
+  const int h = e2 / 2;
+  const T g2s = ldexp(g2n, e2 - 2 * h);  // in [0.25, 2)
+  T rg = (T)rsqrtf((float)g2s);
+  rg = rg * (T(1.5) - T(0.5) * g2s * rg * rg);
+  rg = rg * (T(1.5) - T(0.5) * g2s * rg * rg);
+  rg = ldexp(rg, -h);
+  const float zeta = (float)(T(0.5) * (b - a) * rg);
+  const float tf = (zeta >= 0.f ? 1.f : -1.f) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
+  if (!(tf != 0.f)) return false;  // angle below FP32 resolution of the tangent: nothing to do
+  const T t = (T)tf;
+  const T u = T(1) + t * t;
+  T cc = (T)rsqrtf((float)u);
+  cc = cc * (T(1.5) - T(0.5) * u * cc * cc);
+  cc = cc * (T(1.5) - T(0.5) * u * cc * cc);
+  const T sc = t * cc;
+  c = cc;
+  sr = sc * gr * rg;
+  si = sc * gi * rg;
+  tabs = fabsf(tf);
+  return true;
+}
+
+template <typename T, int NT, int RPT>
+__device__ __forceinline__ void jacobi_pair_fast(cplx_t<T>* __restrict__ B, long ldb, int m, int n,
+                                                 cplx_t<T>* __restrict__ V, long ldv, int nv, int np,
+                                                 int round, int pair, T tol, T smax,
+                                                 unsigned* __restrict__ count) {
+  using C = cplx_t<T>;
+  const int np1 = np - 1;
+  int p, q;
+  if (pair == 0) { p = round; q = np1; }
+  else { p = (round + pair) % np1; q = (round - pair + np1) % np1; }
+  if (p >= n || q >= n) return;
+  if (p > q) { int t = p; p = q; q = t; }
+  C* bp = B + (long)p * ldb;
+  C* bq = B + (long)q * ldb;
+  const bool fits = m <= NT * RPT;
+  C x[RPT], y[RPT];
+  T a = 0, b = 0, gr = 0, gi = 0;
+  if (fits) {
+#pragma unroll
+    for (int j = 0; j < RPT; j++) {
+      int r = threadIdx.x + j * NT;
+      if (r < m) { x[j] = __ldcg(bp + r); y[j] = __ldcg(bq + r); }
+      else { x[j].x = x[j].y = y[j].x = y[j].y = T(0); }
+    }
+#pragma unroll
+    for (int j = 0; j < RPT; j++) {
+      a += x[j].x * x[j].x + x[j].y * x[j].y;
+      b += y[j].x * y[j].x + y[j].y * y[j].y;
+      gr += x[j].x * y[j].x + x[j].y * y[j].y;
+      gi += x[j].x * y[j].y - x[j].y * y[j].x;
+    }
+  } else {
+    for (int r = threadIdx.x; r < m; r += NT) {
+      C u = __ldcg(bp + r), w = __ldcg(bq + r);
+      a += u.x * u.x + u.y * u.y;
+      b += w.x * w.x + w.y * w.y;
+      gr += u.x * w.x + u.y * w.y;
+      gi += u.x * w.y - u.y * w.x;
+    }
+  }
+  block_sum4<T, NT>(a, b, gr, gi);
+  T c, sr, si;
+  float tabs;
+  if (!rotation_params<T>(a, b, gr, gi, tol, smax, c, sr, si, tabs)) return;
+  if (fits) {
+#pragma unroll
+    for (int j = 0; j < RPT; j++) {
+      int r = threadIdx.x + j * NT;
+      rot(x[j], y[j], c, sr, si);
+      if (r < m) { __stcg(bp + r, x[j]); __stcg(bq + r, y[j]); }
+    }
+  } else {
+    for (int r = threadIdx.x; r < m; r += NT) {
+      C u = __ldcg(bp + r), w = __ldcg(bq + r);
+      rot(u, w, c, sr, si);
+      __stcg(bp + r, u); __stcg(bq + r, w);
+    }
+  }
+  C* vp = V + (long)p * ldv;
+  C* vq = V + (long)q * ldv;
+  for (int r = threadIdx.x; r < nv; r += NT) {
+    C u = __ldcg(vp + r), w = __ldcg(vq + r);
+    rot(u, w, c, sr, si);
+    __stcg(vp + r, u); __stcg(vq + r, w);
+  }
+  if (threadIdx.x == 0) {
+    atomicAdd(count, 1u);
+    atomicMax(count + 1, __float_as_uint(tabs));
+  }
+}
+
+// B *= 2^-e with 2^(e-1) <= max column norm < 2^e (exact), so sigma_max ~ 1 inside the sweeps;
+// scale_out[0] = 2^e for the caller to undo it.  One block per column chunk reads the same max.
+template <typename C>
+__global__ void pow2_scale_k(C* __restrict__ B, long ldb, int rows, int k, double* __restrict__ smax_io,
+                             double* __restrict__ scale_out, int undo) {
+  const double sm = *smax_io;
+  int e = 0;
+  if (sm > 0.0) frexp(sm, &e);
+  const double f = undo ? ldexp(1.0, e) : ldexp(1.0, -e);
+  long total = (long)rows * k;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+    long i = t % rows, j = t / rows;
+    C v = B[i + j * ldb];
+    v.x = (decltype(v.x))(v.x * f);
+    v.y = (decltype(v.y))(v.y * f);
+    B[i + j * ldb] = v;
+  }
+  if (!undo && blockIdx.x == 0 && threadIdx.x == 0) scale_out[0] = ldexp(1.0, e);
+}
+
+// Sweep `sweep` of a Jacobi whose convergence is decided on the device, so the host enqueues
+// all sweeps at once and synchronises only at the end.  state[0] = converged flag (set by the
+// sweep that finds no rotation, or, in FP64, whose largest rotation tangent is < 1e-8; later
+// sweeps then return at once), state[1] = sweeps run, state[2..4] = grid barrier,
+// state[8 + 2 s] / [9 + 2 s] = rotations / largest tangent (float bits) of sweep s.
+template <typename T, int NT, int RPT>
+__global__ void __launch_bounds__(NT) jacobi_sweep_dev_k(cplx_t<T>* __restrict__ B, long ldb, int m, int n,
+                                                         cplx_t<T>* __restrict__ V, long ldv, int np, T tol,
+                                                         const double* __restrict__ smax_p,
+                                                         unsigned* __restrict__ state, int sweep) {
+  if (((volatile unsigned*)state)[0]) return;
+  const T smax = (T)(smax_p[0] / smax_p[1]);  // sigma_max of the pre-scaled columns (~1)
+  unsigned* cnt = state + 8 + 2 * sweep;
+  const int npairs = np / 2;
+  for (int round = 0; round < np - 1; round++) {
+    for (int pair = blockIdx.x; pair < npairs; pair += gridDim.x)
+      jacobi_pair_fast<T, NT, RPT>(B, ldb, m, n, V, ldv, n, np, round, pair, tol, smax, cnt);
+    if (!grid_barrier(state + 2)) return;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    const unsigned h = ((volatile unsigned*)cnt)[0];
+    const float tmax = __uint_as_float(((volatile unsigned*)cnt)[1]);
+    state[1] = sweep + 1;
+    if (h == 0 || (sizeof(T) == 8 && tmax < 1e-8f)) state[0] = 1;
+  }
+}
+
+// Small problems (k <= 128 columns): the whole Jacobi iteration in one thread-block cluster of
+// up to 16 CTAs.  Each warp owns a pair of the round (1-4 warps per CTA, so a round's FP64 work
+// spreads over as many SMs as the cluster allows), the hardware cluster
+// barrier separates rounds, and sweeps repeat inside the kernel until one rotates nothing (FP64:
+// or rotates by less than 1e-8).  Cluster CTAs are co-scheduled by the hardware, so the barrier
+// needs no co-residency argument; column reads go to L2 (ld.global.cg) so a CTA always sees the
+// rotations other CTAs made in the previous round.  state[0] = converged, state[1] = sweeps,
+// state[8 + s] = rotations of sweep s (global counters, shared by the cluster).
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
+  asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) jacobi_cluster_k(cplx_t<T>* __restrict__ B, long ldb, int m, int n,
+                                                        cplx_t<T>* __restrict__ V, long ldv, T tol,
+                                                        const double* __restrict__ smax_p, int max_sweeps,
+                                                        unsigned* __restrict__ state) {
+  using C = cplx_t<T>;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpc = blockDim.x >> 5;
+  const int gw = blockIdx.x * wpc + warp, nw = gridDim.x * wpc;
+  const int np = n + (n & 1), np1 = np - 1, npairs = np / 2;
+  const T smax = (T)(smax_p[0] / smax_p[1]);
+  int sweep = 0;
+  bool conv = false;
+  for (; sweep < max_sweeps && !conv; sweep++) {
+    unsigned* cnt = state + 8 + 2 * sweep;
+    for (int round = 0; round < np1; round++) {
+      for (int pair = gw; pair < npairs; pair += nw) {
+        int p, q;
+        if (pair == 0) { p = round; q = np1; }
+        else { p = (round + pair) % np1; q = (round - pair + np1) % np1; }
+        if (p >= n || q >= n) continue;
+        if (p > q) { int t = p; p = q; q = t; }
+        C* bp = B + (long)p * ldb;
+        C* bq = B + (long)q * ldb;
+        T a = 0, b = 0, gr = 0, gi = 0;
+        for (int r = lane; r < m; r += 32) {
+          C x = __ldcg(bp + r), y = __ldcg(bq + r);
+          a += x.x * x.x + x.y * x.y;
+          b += y.x * y.x + y.y * y.y;
+          gr += x.x * y.x + x.y * y.y;
+          gi += x.x * y.y - x.y * y.x;
+        }
+        a = warp_sum(a); b = warp_sum(b); gr = warp_sum(gr); gi = warp_sum(gi);
+        T c, sr, si;
+        float tabs;
+        if (!rotation_params<T>(a, b, gr, gi, tol, smax, c, sr, si, tabs)) continue;
+        for (int r = lane; r < m; r += 32) {
+          C x = __ldcg(bp + r), y = __ldcg(bq + r);
+          rot(x, y, c, sr, si);
+          __stcg(bp + r, x);
+          __stcg(bq + r, y);
+        }
+        C* vp = V + (long)p * ldv;
+        C* vq = V + (long)q * ldv;
+        for (int r = lane; r < n; r += 32) {
+          C x = __ldcg(vp + r), y = __ldcg(vq + r);
+          rot(x, y, c, sr, si);
+          __stcg(vp + r, x);
+          __stcg(vq + r, y);
+        }
+        if (lane == 0) {
+          atomicAdd(cnt, 1u);
+          atomicMax(cnt + 1, __float_as_uint(tabs));
+        }
+      }
+      cluster_sync_all();
+    }
+    const unsigned h = __ldcg(cnt);
+    const float tmax = __uint_as_float(__ldcg(cnt + 1));
+    conv = h == 0 || (sizeof(T) == 8 && tmax < 1e-8f);
+    cluster_sync_all();  // everyone has read this sweep's counters
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    state[0] = conv ? 1u : 0u;
+    state[1] = sweep;
+  }
+}
+
+// out[0] = max_j nrm[j] (one block)
+__global__ void max_reduce_k(const double* __restrict__ nrm, int k, double* __restrict__ out) {
+  __shared__ double red[32];
+  double v = 0.0;
+  for (int j = threadIdx.x; j < k; j += blockDim.x) v = fmax(v, nrm[j]);
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if (threadIdx.x == 0) out[0] = v;
+  }
+}
+
 // nrm[j] = |col_j| in FP64 (one warp per column)
 template <typename C>
 __global__ void col_norms_k(const C* __restrict__ B, long ldb, int m, int n, double* __restrict__ nrm) {
@@ -310,73 +565,119 @@ inline unsigned gs(long n) {
   return (unsigned)(g < 1 ? 1 : g);
 }
 
-// Hestenes sweeps on B (rows x k) accumulating V (k x k), until no rotation happens.
+// Hestenes sweeps on B (rows x k) accumulating V (k x k).  Small problems (k <= 32) run the
+// whole iteration in one CTA; larger ones enqueue up to max_sweeps cooperative sweep launches
+// whose convergence is decided on the device.  One host synchronisation per call.
 template <typename T>
 int jacobi(cudaStream_t s, SvdWork* w, cplx_t<T>* B, long ldb, int rows, int k, cplx_t<T>* V,
            long ldv, int max_sweeps, T tol, bool must_converge = true) {
   const int np = k + (k & 1);
-  unsigned* cnt = w->cnt.as<unsigned>();
-  unsigned* bar = cnt + 4;
   constexpr int NT = sizeof(T) == 8 ? 256 : 128;
   constexpr int RPT = sizeof(T) == 8 ? 8 : 16;
-  // persistent cooperative grid: as many CTAs as can be resident, at most one per pair
-  int dev = 0, sms = 0, per_sm = 0;
-  QR_CUDA(cudaGetDevice(&dev));
-  QR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  QR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, jacobi_sweep_k<T, NT, RPT>, NT, 0));
-  if (per_sm < 1) return fail(QR_ECUDA, "Jacobi sweep kernel cannot be resident");
-  int grid = per_sm * sms;
-  if (grid > np / 2) grid = np / 2;
-  if (grid < 1) grid = 1;
   const int kind = sizeof(T) == 8 ? PK_JACOBI64 : PK_JACOBI32;
   const double pairs = 0.5 * (double)k * (k - 1);
-  // sigma_max from the largest column norm (the column norms' maximum never exceeds it and is
-  // within a factor sqrt(k) of it; the criterion only needs its scale)
+  const int nstate = 8 + 2 * max_sweeps;
+  QR_TRY(w->cnt.ensure(sizeof(unsigned) * nstate + 128, s));
+  unsigned* state = w->cnt.as<unsigned>();
   double* nrm = w->nrm.as<double>();
+  double* smax_d = reinterpret_cast<double*>(state + nstate + (nstate & 1));
+  QR_CUDA(cudaMemsetAsync(state, 0, sizeof(unsigned) * nstate, s));
+  // sigma_max scale from the largest column norm, on the device
   col_norms_k<cplx_t<T>><<<ceil_div((long)k * 32, TPB), TPB, 0, s>>>(B, ldb, rows, k, nrm);
   QR_CHECK_LAUNCH("col_norms_k");
-  w->hs.resize(k);
-  QR_CUDA(cudaMemcpyAsync(w->hs.data(), nrm, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
-  QR_CUDA(cudaStreamSynchronize(s));
-  double smax_h = 0.0;
-  for (int j = 0; j < k; j++) smax_h = w->hs[j] > smax_h ? w->hs[j] : smax_h;
-  const T smax = (T)smax_h;
-  for (int sweep = 0; sweep < max_sweeps; sweep++) {
-    QR_CUDA(cudaMemsetAsync(cnt, 0, 8 * sizeof(unsigned), s));
-    int pr = prof_begin(s, kind, 0.0, 0.0);
-    {
+  max_reduce_k<<<1, 256, 0, s>>>(nrm, k, smax_d);
+  QR_CHECK_LAUNCH("max_reduce_k");
+  {
+    long tot = (long)rows * k;
+    unsigned g = (unsigned)((tot + TPB - 1) / TPB);
+    pow2_scale_k<cplx_t<T>><<<g > 4864 ? 4864 : g, TPB, 0, s>>>(B, ldb, rows, k, smax_d, smax_d + 1, 0);
+    QR_CHECK_LAUNCH("pow2_scale_k");
+  }
+  int pr = prof_begin(s, kind, 0.0, 0.0);
+  const bool small = k <= 128;
+  if (small) {
+    // one cluster of up to 16 CTAs with one warp per pair of a round: as many CTAs as pairs (up
+    // to 16), then 2-4 warps per CTA
+    const int npairs = np / 2 > 0 ? np / 2 : 1;
+    const int cl = npairs < 16 ? npairs : 16;
+    const int wpc = (npairs + cl - 1) / cl;
+    static bool nonportable_set[2] = {false, false};
+    if (cl > 8 && !nonportable_set[sizeof(T) == 8]) {
+      QR_CUDA(cudaFuncSetAttribute(jacobi_cluster_k<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+      nonportable_set[sizeof(T) == 8] = true;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(cl);
+    cfg.blockDim = dim3(32 * wpc);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = cl;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    QR_CUDA(cudaLaunchKernelEx(&cfg, jacobi_cluster_k<T>, B, ldb, rows, k, V, ldv, tol, (const double*)smax_d,
+                               max_sweeps, state));
+    count_launch();
+  } else {
+    static int per_sm_cache[2] = {0, 0};
+    static int sms_cache = 0;
+    int& per_sm = per_sm_cache[sizeof(T) == 8 ? 1 : 0];
+    if (per_sm == 0 || sms_cache == 0) {
+      int dev = 0;
+      QR_CUDA(cudaGetDevice(&dev));
+      QR_CUDA(cudaDeviceGetAttribute(&sms_cache, cudaDevAttrMultiProcessorCount, dev));
+      QR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, jacobi_sweep_dev_k<T, NT, RPT>, NT, 0));
+      if (per_sm < 1) return fail(QR_ECUDA, "Jacobi sweep kernel cannot be resident");
+    }
+    int grid = per_sm * sms_cache;
+    if (grid > np / 2) grid = np / 2;
+    if (grid < 1) grid = 1;
+    for (int sweep = 0; sweep < max_sweeps; sweep++) {
       cplx_t<T>* Bp = B;
       cplx_t<T>* Vp = V;
-      int mm = rows, kk2 = k, npp = np;
+      int mm = rows, kk2 = k, npp = np, sw = sweep;
       long ldbb = ldb, ldvv = ldv;
-      T tl = tol, sm = smax;
-      void* args[] = {&Bp, &ldbb, &mm, &kk2, &Vp, &ldvv, &npp, &tl, &sm, &cnt, &bar};
-      QR_CUDA(cudaLaunchCooperativeKernel((const void*)jacobi_sweep_k<T, NT, RPT>, dim3(grid), dim3(NT), args, 0, s));
+      T tl = tol;
+      const double* sm = smax_d;
+      unsigned* st = state;
+      void* args[] = {&Bp, &ldbb, &mm, &kk2, &Vp, &ldvv, &npp, &tl, &sm, &st, &sw};
+      QR_CUDA(cudaLaunchCooperativeKernel((const void*)jacobi_sweep_dev_k<T, NT, RPT>, dim3(grid), dim3(NT), args, 0, s));
       count_launch();
     }
-    prof_end(s, pr);
-    unsigned hh[3] = {0, 0, 0};
-    QR_CUDA(cudaMemcpyAsync(hh, cnt, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, s));
-    QR_CUDA(cudaMemcpyAsync(hh + 2, bar + 2, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
-    QR_CUDA(cudaStreamSynchronize(s));
-    if (hh[2]) return fail(QR_ECUDA, "Jacobi sweep: grid barrier timed out");
-    const unsigned h = hh[0];
-    float tmax;
-    memcpy(&tmax, &hh[1], sizeof(float));
-    // algorithmic work of the sweep: three inner products per pair (16 real flops per row) and
-    // two column rotations of B and V for every rotated pair (20 flops per row and column)
-    prof_account(pr, 16.0 * rows * pairs + 20.0 * (double)h * (rows + k) * 2.0,
-                 sizeof(cplx_t<T>) * ((double)rows + k) * 2.0 * (pairs + h));
-    if (debug_on())
-      fprintf(stderr, "[qr] jacobi<%s> %dx%d sweep %d rotations %u max tan %.2e\n", sizeof(T) == 8 ? "f64" : "f32",
-              rows, k, sweep, h, tmax);
-    if (h == 0) return QR_OK;
-    // a sweep whose rotations were all below tau leaves couplings O(tau^2): with tau < 1e-8 in
-    // FP64 the next sweep would find nothing above the tolerance, so it is skipped
-    if (sizeof(T) == 8 && tmax < 1e-8f) return QR_OK;
   }
-  if (!must_converge) return QR_OK;
-  return fail(QR_ENOCONV, "Jacobi SVD did not converge");
+  prof_end(s, pr);
+  {
+    long tot = (long)rows * k;
+    unsigned g = (unsigned)((tot + TPB - 1) / TPB);
+    pow2_scale_k<cplx_t<T>><<<g > 4864 ? 4864 : g, TPB, 0, s>>>(B, ldb, rows, k, smax_d, smax_d + 1, 1);
+    QR_CHECK_LAUNCH("pow2_scale_k");
+  }
+  std::vector<unsigned>& hs = w->hc;
+  hs.assign(nstate, 0u);
+  QR_CUDA(cudaMemcpyAsync(hs.data(), state, sizeof(unsigned) * nstate, cudaMemcpyDeviceToHost, s));
+  QR_CUDA(cudaStreamSynchronize(s));
+  if (hs[4]) return fail(QR_ECUDA, "Jacobi sweep: grid barrier timed out");
+  const int ran = (int)hs[1];
+  double rotated = 0;
+  for (int sw = 0; sw < ran; sw++) {
+    rotated += hs[8 + 2 * sw];
+    if (debug_on()) {
+      float tmax;
+      memcpy(&tmax, &hs[9 + 2 * sw], sizeof(float));
+      fprintf(stderr, "[qr] jacobi<%s> %dx%d sweep %d rotations %u max tan %.2e\n", sizeof(T) == 8 ? "f64" : "f32",
+              rows, k, sw, hs[8 + 2 * sw], tmax);
+    }
+  }
+  if (debug_on() && small) fprintf(stderr, "[qr] jacobi_cluster<%s> %dx%d sweeps %d\n", sizeof(T) == 8 ? "f64" : "f32", rows, k, ran);
+  // algorithmic work: three inner products per pair and sweep (16 real flops per row) and two
+  // column rotations of B and V per rotated pair (20 flops per row and column)
+  prof_account(pr, 16.0 * rows * pairs * ran + 40.0 * rotated * (rows + k),
+               sizeof(cplx_t<T>) * ((double)rows + k) * 2.0 * (pairs * ran + rotated));
+  if (!hs[0] && must_converge) return fail(QR_ENOCONV, "Jacobi SVD did not converge");
+  return QR_OK;
 }
 
 }  // namespace
@@ -421,10 +722,13 @@ int zsvd_thin(cudaStream_t s, SvdWork* w, int mode, const double2* A, int m, int
     QR_TRY(ztranspose(s, A, lda, m, n, B, rows, 1));
   }
 
-  if (mode == QR_FP64) {
+  // The FP32-preconditioned path pays off only for larger blocks: below k = 128 its DMMA
+  // Newton-Schulz GEMMs run on a handful of SMs at the per-SM FP64 rate and cost more than the
+  // FP64 sweeps they replace, so small blocks take the FP64 Jacobi directly (same accuracy).
+  if (mode == QR_FP64 || k <= 128) {
     QR_TRY(zset_identity(s, V, k, k, k));
     double tol = sqrt((double)rows) * Eps<double>::v;
-    QR_TRY(jacobi<double>(s, w, B, rows, rows, k, V, k, 60, tol));
+    QR_TRY(jacobi<double>(s, w, B, rows, rows, k, V, k, 40, tol));
   } else {
     // ---- FP32 Jacobi preconditioner
     QR_TRY(w->B32.ensure(sizeof(float2) * (size_t)rows * k, s));
@@ -475,7 +779,7 @@ int zsvd_thin(cudaStream_t s, SvdWork* w, int mode, const double2* A, int m, int
     // first-order step leaves alone and certify orthogonality with the FP64 tolerance
     QR_TRY(zgemm(s, OP_N, OP_N, rows, k, k, one, Asrc, rows, 0, X, k, 0, zero, B, rows, 0, 1, nullptr));
     QR_CUDA(cudaMemcpyAsync(V, X, sizeof(double2) * (size_t)k * k, cudaMemcpyDeviceToDevice, s));
-    QR_TRY(jacobi<double>(s, w, B, rows, rows, k, V, k, 60, sqrt((double)rows) * Eps<double>::v));
+    QR_TRY(jacobi<double>(s, w, B, rows, rows, k, V, k, 40, sqrt((double)rows) * Eps<double>::v));
   }
 
   // ---- sigma, ordering, factors
