@@ -437,7 +437,7 @@ def run_ours(args, chi):
         line = {"metric": METRIC, "value": value, "unit": "gate-steps/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1e3 * dt_max / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None,
-                "dtype": "complex64 Jacobi preconditioner + complex128 (FP64 DMMA) refinement; FP64 theta",
+                "dtype": "complex64 Jacobi preconditioner + double-float (FP32-pair) Jacobi polish + complex128 (FP64 DMMA) GEMMs; FP64 theta",
                 "data": "synthetic",
                 "config": {"workload": f"tebd_gate_step_chi{chi}", "chi": chi, "theta": f"{2 * chi}x{2 * chi}",
                            "maxdim": maxdim, "threshold": CUTOFF, "n_sites": N_SITES, "precision": "mixed",

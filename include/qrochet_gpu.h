@@ -71,7 +71,8 @@ int qr_set_device(int device);
 int qr_launch_count(uint64_t* count);
 
 /* per-kernel-class CUDA-event timing, for benchmarks: kinds 0 zgemm (FP64 DMMA), 1 Jacobi FP64,
-   2 Jacobi FP32, 3 Householder QR, 4 environment mixing, 5 split-precision tensor-core zgemm.
+   2 Jacobi FP32, 3 Householder QR, 4 environment mixing, 5 split-precision tensor-core zgemm,
+   6 double-float Jacobi polish.
    No reference counterpart. */
 int qr_prof_enable(int on);
 int qr_prof_read(int kind, double* ms, uint64_t* launches, double* flops, double* bytes);

@@ -89,6 +89,10 @@ CASES = {
     "graded12": lambda g: _graded(g, 80, 80, 12),
     "zero_cols": lambda g: np.hstack([R.complex_gaussian(g, (40, 10)), np.zeros((40, 6))]),
     "tiny": lambda g: R.complex_gaussian(g, (2, 1)),
+    # above 128 columns the mixed mode takes the FP32-preconditioned path with the polish sweeps
+    "square300": lambda g: R.complex_gaussian(g, (300, 300)),
+    "wide200x400": lambda g: R.complex_gaussian(g, (200, 400)),
+    "graded300": lambda g: _graded(g, 300, 300, 10),
 }
 
 
