@@ -79,14 +79,55 @@ class Dist:
         if self.world > 1:
             self.td.barrier()
 
-    def max(self, x):
+    def _reduce(self, x, op):
         if self.world == 1:
             return x
         import torch
 
         t = torch.tensor([float(x)], dtype=torch.float64)
-        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        self.td.all_reduce(t, op=getattr(self.td.ReduceOp, op))
         return float(t.item())
+
+    def max(self, x):
+        return self._reduce(x, "MAX")
+
+    def sum(self, x):
+        return self._reduce(x, "SUM")
+
+    def gather(self, values):
+        """Concatenation of every rank's list (rank order)."""
+        if self.world == 1:
+            return list(values)
+        out = [None] * self.world
+        self.td.all_gather_object(out, list(values))
+        return [v for part in out for v in part]
+
+
+def shard(items, rank, world):
+    """Replica partition of independent requests: rank r takes items r, r + world, ...  Every item
+    goes to exactly one rank and no data moves between ranks."""
+    return list(items)[rank::world]
+
+
+class DevTimer:
+    """CUDA events recorded on the stream the chain's kernels run on (device time of the timed
+    region; the host-side synchronisations inside a step are part of it)."""
+
+    def __init__(self, stream_handle, device):
+        import torch
+
+        torch.cuda.set_device(device)
+        self.stream = torch.cuda.ExternalStream(stream_handle, device=device)
+        self.e0 = torch.cuda.Event(enable_timing=True)
+        self.e1 = torch.cuda.Event(enable_timing=True)
+
+    def start(self):
+        self.e0.record(self.stream)
+
+    def stop(self):
+        self.e1.record(self.stream)
+        self.e1.synchronize()
+        return self.e0.elapsed_time(self.e1) * 1e-3
 
 
 def workload(chi):
@@ -165,27 +206,29 @@ def cpu_gate_step(al, ar, lam, u, maxdim):
     return ch
 
 
-def run_batched(args, Q):
+def run_batched(args, Q, dist, rank, world):
     """Batched solves/s: requests of the batched distribution (n ~ U[8,96], depth ~ U[4,32],
     cutoff 1e-10, mixed precision) all submitted at once to the continuous-batching server.
     chi_max is drawn log-uniformly from {16, 32, 64} (a bounded sample of the {16..512} range:
     chi_max = 512 requests take minutes each at this part's FP64 rate)."""
     from qrochet import serve as S
 
-    reqs = S.batched_requests(args.batched, seed=4, chi_log2=(4, 6), nobs=1)
-    gates = sum(len(r.gates) for r in reqs)
+    reqs = shard(S.batched_requests(args.batched, seed=4, chi_log2=(4, 6), nobs=1), rank, world)
+    gates = dist.sum(sum(len(r.gates) for r in reqs))
     with S.Server(workers=args.workers, precision="mixed") as sv:
+        dist.barrier()
         t0 = time.perf_counter()
         tickets = [sv.submit(r) for r in reqs]
         lat = [sv.wait(t)["latency_ms"] for t in tickets]
-        dt = time.perf_counter() - t0
-    return {"requests": len(reqs), "solves_per_s": len(reqs) / dt, "gate_steps_per_s": gates / dt,
+        dt = dist.max(time.perf_counter() - t0)
+    lat = dist.gather(lat)
+    return {"requests": len(lat), "solves_per_s": len(lat) / dt, "gate_steps_per_s": gates / dt,
             "wall_s": dt, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
             "workers": args.workers, "precision": "mixed",
             "sample": "n~U[8,96], depth~U[4,32], chi_max log-uniform in {16,32,64}, cutoff 1e-10, seed 4"}
 
 
-def run_serving(args, Q):
+def run_serving(args, Q, dist, rank, world):
     """Serving: Poisson arrivals at 200 req/s of random brick-wall circuits with 8 Pauli strings of
     weight 1-4; p50/p99 latency and solves/s for the FP64 and mixed forms.  Bounded sample:
     n ~ U[16,64], depth ~ U[4,16], chi_max in {32, 128}."""
@@ -197,17 +240,22 @@ def run_serving(args, Q):
         g = R.rng(5)
         reqs = [S.random_request(g, n_range=(16, 64), depth_range=(4, 16), chi_choices=(32, 128), nobs=8)
                 for _ in range(args.serve)]
-        gaps = g.exponential(1.0 / 200.0, size=len(reqs))
+        # arrivals at 200 req/s in total: each replica sees its share of the Poisson stream
+        gaps = shard(g.exponential(1.0 / 200.0, size=len(reqs)).cumsum(), rank, world)
+        reqs = shard(reqs, rank, world)
         with S.Server(workers=args.workers, precision=prec) as sv:
             tickets = []
+            dist.barrier()
             t0 = time.perf_counter()
-            for r, gap in zip(reqs, gaps):
-                time.sleep(gap)
+            for r, at in zip(reqs, gaps):
+                wait = at - (time.perf_counter() - t0)
+                if wait > 0:
+                    time.sleep(wait)
                 tickets.append(sv.submit(r))
             res = [sv.wait(t) for t in tickets]
-            dt = time.perf_counter() - t0
-        lat = np.array([x["latency_ms"] for x in res])
-        out[prec] = {"requests": len(reqs), "solves_per_s": len(reqs) / dt, "p50_ms": float(np.percentile(lat, 50)),
+            dt = dist.max(time.perf_counter() - t0)
+        lat = np.array(dist.gather([x["latency_ms"] for x in res]))
+        out[prec] = {"requests": len(lat), "solves_per_s": len(lat) / dt, "p50_ms": float(np.percentile(lat, 50)),
                      "p99_ms": float(np.percentile(lat, 99)),
                      "p99_over_p50": float(np.percentile(lat, 99) / np.percentile(lat, 50)),
                      "values": [x["values"] for x in res]}
@@ -323,13 +371,13 @@ def run_ours(args, chi):
     clocks = Clocks(local)
     clocks.start()
     l0 = Q.launch_count()
+    timer = DevTimer(psi.stream(), local)
     dist.barrier()
     psi.sync()
-    t0 = time.perf_counter()
+    timer.start()
     for i in range(args.steps):
         step(psi, args.warmup + i)
-    psi.sync()
-    dt = time.perf_counter() - t0
+    dt = timer.stop()
     launches = Q.launch_count() - l0
     dist.barrier()
     clk = clocks.stop()
@@ -347,11 +395,12 @@ def run_ours(args, chi):
         p64 = make("fp64")
         step(p64, 0)
         p64.sync()
-        t1 = time.perf_counter()
+        t64 = DevTimer(p64.stream(), local)
+        dist.barrier()
+        t64.start()
         for i in range(args.fp64_steps):
             step(p64, 1 + i)
-        p64.sync()
-        d64 = dist.max(time.perf_counter() - t1)
+        d64 = dist.max(t64.stop())
         fp64 = {"value": world * args.fp64_steps / d64, "unit": "gate-steps/s",
                 "ms_per_step": 1e3 * d64 / args.fp64_steps, "steps": args.fp64_steps}
         del p64
@@ -366,7 +415,9 @@ def run_ours(args, chi):
     pe = make("mixed")
     h2d = d2h = 0
     pe.sync()
-    t2 = time.perf_counter()
+    te = DevTimer(pe.stream(), local)
+    dist.barrier()
+    te.start()
     for i in range(args.steps):
         b = BONDS[i % len(BONDS)]
         for s in (b, b + 1):
@@ -378,8 +429,7 @@ def run_ours(args, chi):
         if i == 0:
             h2d = 2 * pin[b][0].array.nbytes + 16 * 16
             d2h = 2 * pin[b][1].array.nbytes + lam.nbytes
-    pe.sync()
-    de = dist.max(time.perf_counter() - t2)
+    de = dist.max(te.stop())
     e2e = {"value": world * args.steps / de, "unit": "gate-steps/s", "h2d_bytes_per_step": int(h2d),
            "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * de / args.steps}
     del pe
@@ -395,22 +445,28 @@ def run_ours(args, chi):
     del pr
     dom = max(stats, key=lambda k: stats[k]["ms"])
     peaks = {"zgemm_dmma": ("dmma", "tensor"), "jacobi_fp32": ("ffma", "fp32"), "jacobi_fp64": ("dfma", "fp64"),
-             "householder_qr": ("dfma", "fp64"), "env_mix": ("dfma", "fp64")}
+             "householder_qr": ("dfma", "fp64"), "env_mix": ("dfma", "fp64"), "jacobi_df": ("ffma", "fp32"),
+             "zgemm_split_bf16": ("bf16", "tensor")}
     pk_kind, bound = peaks[dom]
-    peak = Q.probe_peak(pk_kind)
+    try:
+        mp = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        mp = {}
+    if pk_kind == "bf16":  # the split GEMM's products run on the BF16 tensor pipe
+        peak = mp.get("bf16_tflops") or 1900.0
+    else:
+        peak = Q.probe_peak(pk_kind)
     st = stats[dom]
     achieved = st["flops"] / (st["ms"] * 1e-3) / 1e12 if st["ms"] > 0 else 0.0
     shares = {k: round(v["ms"] / max(1e-9, sum(x["ms"] for x in stats.values())), 4) for k, v in stats.items()}
     roofline = {"bound": bound, "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": achieved / peak if peak else None, "traffic": None,
-                "peak_source": f"measured in-process ({pk_kind} loop kernel, best of 3)",
+                "peak_source": ("measured cuBLAS bf16 (MEASURED_PEAKS.json)" if pk_kind == "bf16" else
+                                f"measured in-process ({pk_kind} loop kernel, best of 3)"),
                 "launches": st["launches"], "avg_launch_ms": st["ms"] / max(1, st["launches"]),
                 "time_share": shares}
-    try:
-        mp = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    if mp:
         roofline["measured_peaks_json"] = {"hbm_gbs": mp.get("hbm_gbs"), "bf16_tflops": mp.get("bf16_tflops")}
-    except Exception:
-        pass
 
     # ---- CPU baseline (rank 0, bounded sample) ------------------------------------------------------
     cpu = None
@@ -429,8 +485,8 @@ def run_ours(args, chi):
                "sample": f"{args.cpu_steps} gate-steps at chi={chi} (NumPy/LAPACK zgesdd restatement, all host "
                          f"threads)"}
 
-    batched = run_batched(args, Q) if (args.batched > 0 and not args.quick) else None
-    serving = run_serving(args, Q) if (args.serve > 0 and not args.quick) else None
+    batched = run_batched(args, Q, dist, rank, world) if (args.batched > 0 and not args.quick) else None
+    serving = run_serving(args, Q, dist, rank, world) if (args.serve > 0 and not args.quick) else None
     mpo_env = run_mpo_env(args, Q) if (args.mpo_sites > 0 and not args.quick) else None
 
     if rank == 0:
