@@ -72,7 +72,7 @@ int qr_launch_count(uint64_t* count);
 
 /* per-kernel-class CUDA-event timing, for benchmarks: kinds 0 zgemm (FP64 DMMA), 1 Jacobi FP64,
    2 Jacobi FP32, 3 Householder QR, 4 environment mixing, 5 split-precision tensor-core zgemm,
-   6 double-float Jacobi polish.
+   6 double-float Jacobi polish, 7 double-float zgemm.
    No reference counterpart. */
 int qr_prof_enable(int on);
 int qr_prof_read(int kind, double* ms, uint64_t* launches, double* flops, double* bytes);
@@ -176,6 +176,10 @@ int qr_test_zgemm(int opA, int opB, int M, int N, int K, const double* alpha, co
                   int iters, double* ms_per_iter);
 int qr_test_zgemm_split(int opA, int opB, int M, int N, int K, const double* A, long lda, const double* B,
                         long ldb, double* C, long ldc, int iters, double* ms_per_iter);
+/* Double-float GEMM on the FP32 pipes.  mode 0: C = op(A) B; 1: C = I - op(A) B; 2: C = D + 0.5
+   op(A) B with FP32 products (A, B rounded to FP32).  op(A) in {0 N, 1 T, 2 C}; D used by mode 2. */
+int qr_test_zgemm_df(int mode, int opA, int M, int N, int K, const double* A, long lda, const double* B, long ldb,
+                     const double* D, double* C, long ldc, int iters, double* ms_per_iter);
 int qr_test_svd(int mode, int m, int n, const double* A, double* U, double* S, double* Vh, double* ms);
 int qr_test_qr(int m, int n, const double* A, double* Q, double* R, double* ms);
 

@@ -15,6 +15,20 @@ int zgemm(cudaStream_t s, int opA, int opB, int M, int N, int K, double2 alpha,
 int zgemm_split(cudaStream_t s, int opA, int opB, int M, int N, int K, const double2* A, long lda, long sA,
                 const double2* B, long ldb, long sB, double2* C, long ldc, long sC, int batch);
 
+// ---- gemm_df.cu: complex GEMM in double-float (hi, lo FP32 pairs) on the FP32 pipes
+enum { DF_STORE = 0, DF_I_MINUS = 1, DF_F32_AXPY = 2 };
+// DF_STORE: (Ch, Cl) = op(A) B; DF_I_MINUS: Ch = I - op(A) B (FP32); DF_F32_AXPY: (Ch, Cl) = D +
+// alpha op(A_hi) B_hi with FP32 products.  op(A) in {N, T, C}; B is not transformed.
+int zgemm_df(cudaStream_t s, int mode, int opA, int M, int N, int K, const float2* Ah, const float2* Al, long lda,
+             const float2* Bh, const float2* Bl, long ldb, float2* Ch, float2* Cl, long ldc,
+             const float2* Dh = nullptr, const float2* Dl = nullptr, long ldd = 0, float alpha = 1.f);
+// FP64 <-> double-float split arrays; the optional device scale divides on the way in and
+// multiplies on the way out
+int z2df(cudaStream_t s, const double2* src, long lds, int rows, int cols, const double* scale, float2* hi,
+         float2* lo, long ldd);
+int df2z(cudaStream_t s, const float2* hi, const float2* lo, long lds, int rows, int cols, const double* scale,
+         double2* dst, long ldd);
+
 // ---- misc.cu -----------------------------------------------------------------------------------
 int zscale_matrix(cudaStream_t s, int M, int N, double2 alpha, double2* C, long ldc, long sC,
                   int batch);

@@ -3,7 +3,7 @@
 #include "common.cuh"
 
 namespace qr {
-enum ProfKind { PK_ZGEMM = 0, PK_JACOBI64 = 1, PK_JACOBI32 = 2, PK_QR = 3, PK_ENV = 4, PK_ZGEMM_SPLIT = 5, PK_JACOBI_DF = 6, PK_COUNT = 7 };
+enum ProfKind { PK_ZGEMM = 0, PK_JACOBI64 = 1, PK_JACOBI32 = 2, PK_QR = 3, PK_ENV = 4, PK_ZGEMM_SPLIT = 5, PK_JACOBI_DF = 6, PK_ZGEMM_DF = 7, PK_COUNT = 8 };
 bool prof_on();
 // returns a record index (or -1 when profiling is off); pair with prof_end on the same stream
 int prof_begin(cudaStream_t s, int kind, double flops, double bytes);

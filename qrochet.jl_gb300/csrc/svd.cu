@@ -26,6 +26,7 @@
 #include <cmath>
 #include <mutex>
 #include "kernels.cuh"
+#include "df.cuh"
 #include "prof.cuh"
 
 namespace qr {
@@ -48,7 +49,7 @@ struct DBuf {
 };
 
 struct SvdWork {
-  DBuf B, V, B32, V32, X, Rm, E, T1, nrm, perm, cnt, tau, qtmp, host_sig, Bl, Vl;
+  DBuf B, V, B32, V32, X, Rm, E, T1, nrm, perm, cnt, tau, qtmp, host_sig, Bl;
   std::vector<double> hs;
   std::vector<unsigned> hc;
   cudaStream_t last = nullptr;
@@ -58,7 +59,7 @@ SvdWork* svd_work_create() { return new SvdWork(); }
 void svd_work_free(SvdWork* w) {
   if (!w) return;
   DBuf* all[] = {&w->B, &w->V, &w->B32, &w->V32, &w->X, &w->Rm, &w->E, &w->T1,
-                 &w->nrm, &w->perm, &w->cnt, &w->tau, &w->qtmp, &w->host_sig, &w->Bl, &w->Vl};
+                 &w->nrm, &w->perm, &w->cnt, &w->tau, &w->qtmp, &w->host_sig, &w->Bl};
   for (DBuf* b : all)
     if (b->p) cudaFree(b->p);
   delete w;
@@ -284,12 +285,80 @@ __device__ __forceinline__ bool rotation_params(T a, T b, T gr, T gi, T tol, T s
   return true;
 }
 
+// Warp sum of four values by a transposed butterfly: the first two levels split the values
+// between lane halves, so each lane adds 6 times instead of 20.  Afterwards lane l holds the warp
+// total of value (l >> 3) & 3 (lanes 0, 8, 16 and 24 hold a, b, c and d).
+template <typename T>
+__device__ __forceinline__ T warp_sum4_t(T a, T b, T c, T d) {
+  const int l = threadIdx.x & 31;
+  const bool h16 = (l & 16) != 0, h8 = (l & 8) != 0;
+  T k0 = h16 ? c : a, k1 = h16 ? d : b;
+  const T s0 = h16 ? a : c, s1 = h16 ? b : d;
+  k0 += __shfl_xor_sync(0xffffffffu, s0, 16);
+  k1 += __shfl_xor_sync(0xffffffffu, s1, 16);
+  T k = h8 ? k1 : k0;
+  k += __shfl_xor_sync(0xffffffffu, h8 ? k0 : k1, 8);
+  k += __shfl_xor_sync(0xffffffffu, k, 4);
+  k += __shfl_xor_sync(0xffffffffu, k, 2);
+  k += __shfl_xor_sync(0xffffffffu, k, 1);
+  return k;
+}
+
+// L2-coherent loads that stay behind earlier stores (volatile asm with a memory clobber), used
+// for the second column pair of a rotation so its registers are not live during the first.
+__device__ __forceinline__ float2 ld_cg_ordered(const float2* p) {
+  float2 v;
+  asm volatile("ld.global.cg.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ double2 ld_cg_ordered(const double2* p) {
+  double2 v;
+  asm volatile("ld.global.cg.v2.f64 {%0, %1}, [%2];" : "=d"(v.x), "=d"(v.y) : "l"(p) : "memory");
+  return v;
+}
+
+template <typename T>
+struct RotParams {
+  T c, sr, si;
+  float tabs;
+  int go;
+};
+
+// Rotates rows [0, len) of the column pair (xp, xq) in chunks of NT * RPT rows: each chunk's
+// loads are all issued before its first store, so a chunk costs one L2 round trip.
+template <typename T, int NT, int RPT>
+__device__ __forceinline__ void rot_cols_staged(cplx_t<T>* xp, cplx_t<T>* xq, int len, T c, T sr, T si) {
+  using C = cplx_t<T>;
+  for (int base = 0; base < len; base += NT * RPT) {
+    C* pp = xp + base + threadIdx.x;
+    C* pq = xq + base + threadIdx.x;
+    const int lim = len - base - (int)threadIdx.x;  // row j*NT is valid when j*NT < lim
+    C u[RPT], w[RPT];
+#pragma unroll
+    for (int j = 0; j < RPT; j++)
+      if (j * NT < lim) { u[j] = ld_cg_ordered(pp + j * NT); w[j] = ld_cg_ordered(pq + j * NT); }
+#pragma unroll
+    for (int j = 0; j < RPT; j++)
+      if (j * NT < lim) {
+        rot(u[j], w[j], c, sr, si);
+        __stcg(pp + j * NT, u[j]);
+        __stcg(pq + j * NT, w[j]);
+      }
+  }
+}
+
+// One Hestenes pair (p, q) of a round: inner products, one block reduction, rotation parameters
+// computed once (lane 0 of warp 0) and broadcast through shared memory, then the rotation of the
+// B and V columns.  When a column fits (m <= NT * RPT) it stays in registers between the inner
+// products and the rotation.
 template <typename T, int NT, int RPT>
 __device__ __forceinline__ void jacobi_pair_fast(cplx_t<T>* __restrict__ B, long ldb, int m, int n,
                                                  cplx_t<T>* __restrict__ V, long ldv, int nv, int np,
                                                  int round, int pair, T tol, T smax,
                                                  unsigned* __restrict__ count) {
   using C = cplx_t<T>;
+  __shared__ T red[4][NT / 32];
+  __shared__ RotParams<T> P;
   const int np1 = np - 1;
   int p, q;
   if (pair == 0) { p = round; q = np1; }
@@ -301,11 +370,11 @@ __device__ __forceinline__ void jacobi_pair_fast(cplx_t<T>* __restrict__ B, long
   const bool fits = m <= NT * RPT;
   C x[RPT], y[RPT];
   T a = 0, b = 0, gr = 0, gi = 0;
+  const int lim0 = m - (int)threadIdx.x;
   if (fits) {
 #pragma unroll
     for (int j = 0; j < RPT; j++) {
-      int r = threadIdx.x + j * NT;
-      if (r < m) { x[j] = __ldcg(bp + r); y[j] = __ldcg(bq + r); }
+      if (j * NT < lim0) { x[j] = __ldcg(bp + threadIdx.x + j * NT); y[j] = __ldcg(bq + threadIdx.x + j * NT); }
       else { x[j].x = x[j].y = y[j].x = y[j].y = T(0); }
     }
 #pragma unroll
@@ -316,42 +385,63 @@ __device__ __forceinline__ void jacobi_pair_fast(cplx_t<T>* __restrict__ B, long
       gi += x[j].x * y[j].y - x[j].y * y[j].x;
     }
   } else {
-    for (int r = threadIdx.x; r < m; r += NT) {
-      C u = __ldcg(bp + r), w = __ldcg(bq + r);
-      a += u.x * u.x + u.y * u.y;
-      b += w.x * w.x + w.y * w.y;
-      gr += u.x * w.x + u.y * w.y;
-      gi += u.x * w.y - u.y * w.x;
+    for (int base = 0; base < m; base += NT * RPT) {
+#pragma unroll
+      for (int j = 0; j < RPT; j++) {
+        if (base + j * NT < lim0) { x[j] = __ldcg(bp + base + threadIdx.x + j * NT); y[j] = __ldcg(bq + base + threadIdx.x + j * NT); }
+        else { x[j].x = x[j].y = y[j].x = y[j].y = T(0); }
+      }
+#pragma unroll
+      for (int j = 0; j < RPT; j++) {
+        a += x[j].x * x[j].x + x[j].y * x[j].y;
+        b += y[j].x * y[j].x + y[j].y * y[j].y;
+        gr += x[j].x * y[j].x + x[j].y * y[j].y;
+        gi += x[j].x * y[j].y - x[j].y * y[j].x;
+      }
     }
   }
-  block_sum4<T, NT>(a, b, gr, gi);
-  T c, sr, si;
-  float tabs;
-  if (!rotation_params<T>(a, b, gr, gi, tol, smax, c, sr, si, tabs)) return;
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  const T k = warp_sum4_t<T>(a, b, gr, gi);
+  if ((l & 7) == 0) red[l >> 3][w] = k;
+  __syncthreads();
+  if (w == 0) {
+    T v = 0;
+    if (l < 4) {
+#pragma unroll
+      for (int i = 0; i < NT / 32; i++) v += red[l][i];
+    }
+    const T sa = __shfl_sync(0xffffffffu, v, 0), sb = __shfl_sync(0xffffffffu, v, 1);
+    const T sgr = __shfl_sync(0xffffffffu, v, 2), sgi = __shfl_sync(0xffffffffu, v, 3);
+    if (l == 0) {
+      T c, sr, si;
+      float tabs = 0.f;
+      const bool go = rotation_params<T>(sa, sb, sgr, sgi, tol, smax, c, sr, si, tabs);
+      P.c = c; P.sr = sr; P.si = si; P.tabs = tabs; P.go = go ? 1 : 0;
+    }
+  }
+  __syncthreads();
+  if (!P.go) return;
+  const T c = P.c, sr = P.sr, si = P.si;
   if (fits) {
 #pragma unroll
     for (int j = 0; j < RPT; j++) {
-      int r = threadIdx.x + j * NT;
       rot(x[j], y[j], c, sr, si);
-      if (r < m) { __stcg(bp + r, x[j]); __stcg(bq + r, y[j]); }
+      if (j * NT < lim0) { __stcg(bp + threadIdx.x + j * NT, x[j]); __stcg(bq + threadIdx.x + j * NT, y[j]); }
     }
-  } else {
+  } else {  // rows beyond NT * RPT (rare): reload and rotate row by row
     for (int r = threadIdx.x; r < m; r += NT) {
       C u = __ldcg(bp + r), w = __ldcg(bq + r);
       rot(u, w, c, sr, si);
-      __stcg(bp + r, u); __stcg(bq + r, w);
+      __stcg(bp + r, u);
+      __stcg(bq + r, w);
     }
   }
-  C* vp = V + (long)p * ldv;
-  C* vq = V + (long)q * ldv;
-  for (int r = threadIdx.x; r < nv; r += NT) {
-    C u = __ldcg(vp + r), w = __ldcg(vq + r);
-    rot(u, w, c, sr, si);
-    __stcg(vp + r, u); __stcg(vq + r, w);
-  }
+  // keep the V loads behind the B stores: the B registers die first and occupancy stays high
+  asm volatile("" ::: "memory");
+  rot_cols_staged<T, NT, RPT / 2>(V + (long)p * ldv, V + (long)q * ldv, nv, c, sr, si);
   if (threadIdx.x == 0) {
     atomicAdd(count, 1u);
-    atomicMax(count + 1, __float_as_uint(tabs));
+    atomicMax(count + 1, __float_as_uint(P.tabs));
   }
 }
 
@@ -483,67 +573,28 @@ __global__ void __launch_bounds__(128) jacobi_cluster_k(cplx_t<T>* __restrict__ 
 }
 
 // ---- double-float (FP32 pair) Jacobi polish ----------------------------------------------------
-// A value x is held as hi + lo (two FP32 numbers, ~48 significant bits).  The error-free
-// transformations are the published ones: Knuth's TwoSum, Dekker's FastTwoSum and the FMA form of
-// TwoProd (as in Hida, Li & Bailey's double-double library), so every operation runs on the FP32
-// pipes, which are ~70x faster than the FP64 pipes on this part.
-struct dfl {
-  float h, l;
-};
+__device__ __forceinline__ dfl df_shfl_xor(dfl v, int o) {
+  return {__shfl_xor_sync(0xffffffffu, v.h, o), __shfl_xor_sync(0xffffffffu, v.l, o)};
+}
+__device__ __forceinline__ dfl df_shfl(dfl v, int src) {
+  return {__shfl_sync(0xffffffffu, v.h, src), __shfl_sync(0xffffffffu, v.l, src)};
+}
+__device__ __forceinline__ dfl df_sel(bool t, dfl a, dfl b) { return t ? a : b; }
 
-__device__ __forceinline__ dfl df_two_sum(float a, float b) {
-  const float s = a + b;
-  const float bb = s - a;
-  const float e = (a - (s - bb)) + (b - bb);
-  return {s, e};
-}
-__device__ __forceinline__ dfl df_fast_two_sum(float a, float b) {
-  const float s = a + b;
-  return {s, b - (s - a)};
-}
-__device__ __forceinline__ dfl df_add(dfl a, dfl b) {
-  const dfl s = df_two_sum(a.h, b.h);
-  return df_fast_two_sum(s.h, s.l + a.l + b.l);
-}
-__device__ __forceinline__ dfl df_mul(dfl a, dfl b) {
-  const float p = a.h * b.h;
-  float e = fmaf(a.h, b.h, -p);
-  e = fmaf(a.h, b.l, e);
-  e = fmaf(a.l, b.h, e);
-  return df_fast_two_sum(p, e);
-}
-__device__ __forceinline__ dfl df_fma(dfl acc, dfl a, dfl b) { return df_add(acc, df_mul(a, b)); }
-__device__ __forceinline__ dfl df_neg(dfl a) { return {-a.h, -a.l}; }
-__device__ __forceinline__ dfl df_from(double x) {
-  const float h = (float)x;
-  return {h, (float)(x - (double)h)};
-}
-__device__ __forceinline__ double df_to(dfl a) { return (double)a.h + (double)a.l; }
-
-template <int NT>
-__device__ __forceinline__ void df_block_sum4(dfl& a, dfl& b, dfl& c, dfl& d) {
-  __shared__ float red[8][NT / 32];
-  for (int o = 16; o > 0; o >>= 1) {
-    a = df_add(a, {__shfl_xor_sync(0xffffffffu, a.h, o), __shfl_xor_sync(0xffffffffu, a.l, o)});
-    b = df_add(b, {__shfl_xor_sync(0xffffffffu, b.h, o), __shfl_xor_sync(0xffffffffu, b.l, o)});
-    c = df_add(c, {__shfl_xor_sync(0xffffffffu, c.h, o), __shfl_xor_sync(0xffffffffu, c.l, o)});
-    d = df_add(d, {__shfl_xor_sync(0xffffffffu, d.h, o), __shfl_xor_sync(0xffffffffu, d.l, o)});
-  }
-  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  __syncthreads();
-  if (l == 0) {
-    red[0][w] = a.h; red[1][w] = a.l; red[2][w] = b.h; red[3][w] = b.l;
-    red[4][w] = c.h; red[5][w] = c.l; red[6][w] = d.h; red[7][w] = d.l;
-  }
-  __syncthreads();
-  a = b = c = d = {0.f, 0.f};
-#pragma unroll
-  for (int k = 0; k < NT / 32; k++) {
-    a = df_add(a, {red[0][k], red[1][k]});
-    b = df_add(b, {red[2][k], red[3][k]});
-    c = df_add(c, {red[4][k], red[5][k]});
-    d = df_add(d, {red[6][k], red[7][k]});
-  }
+// warp_sum4_t in double-float arithmetic
+__device__ __forceinline__ dfl df_warp_sum4_t(dfl a, dfl b, dfl c, dfl d) {
+  const int l = threadIdx.x & 31;
+  const bool h16 = (l & 16) != 0, h8 = (l & 8) != 0;
+  dfl k0 = df_sel(h16, c, a), k1 = df_sel(h16, d, b);
+  const dfl s0 = df_sel(h16, a, c), s1 = df_sel(h16, b, d);
+  k0 = df_add(k0, df_shfl_xor(s0, 16));
+  k1 = df_add(k1, df_shfl_xor(s1, 16));
+  dfl k = df_sel(h8, k1, k0);
+  k = df_add(k, df_shfl_xor(df_sel(h8, k0, k1), 8));
+  k = df_add(k, df_shfl_xor(k, 4));
+  k = df_add(k, df_shfl_xor(k, 2));
+  k = df_add(k, df_shfl_xor(k, 1));
+  return k;
 }
 
 // x' = c x - conj(s) y ; y' = s x + c y  on (hi, lo) complex pairs
@@ -559,11 +610,130 @@ __device__ __forceinline__ void df_rot(float2& xh, float2& xl, float2& yh, float
   yl = make_float2(nyr.l, nyi.l);
 }
 
-template <int NT>
+__device__ __forceinline__ void df_dot_acc(const float2& xh, const float2& xl, const float2& yh, const float2& yl,
+                                           DotAcc& a, DotAcc& b, DotAcc& gr, DotAcc& gi) {
+  dot2_step(a, xh.x, xl.x, xh.x, xl.x);
+  dot2_step(a, xh.y, xl.y, xh.y, xl.y);
+  dot2_step(b, yh.x, yl.x, yh.x, yl.x);
+  dot2_step(b, yh.y, yl.y, yh.y, yl.y);
+  dot2_step(gr, xh.x, xl.x, yh.x, yl.x);
+  dot2_step(gr, xh.y, xl.y, yh.y, yl.y);
+  dot2_step(gi, xh.x, xl.x, yh.y, yl.y);
+  dot2_step(gi, -xh.y, -xl.y, yh.x, yl.x);
+}
+// Small-angle rotation (|t| < 2^-24): c = 1 - t^2/2 equals 1 to double-float precision and
+// s y needs only the high part of y (|s| |y_lo| < 2^-48 |y|), so x' = x - conj(s) y_hi and
+// y' = y + s x_hi with FP32 products and one double-float addition per component.
+__device__ __forceinline__ void df_rot_small(float2& xh, float2& xl, float2& yh, float2& yl, float sr, float si) {
+  const float dxr = -(sr * yh.x + si * yh.y), dxi = -(sr * yh.y - si * yh.x);
+  const float dyr = sr * xh.x - si * xh.y, dyi = sr * xh.y + si * xh.x;
+  const dfl nxr = df_add_f({xh.x, xl.x}, dxr), nxi = df_add_f({xh.y, xl.y}, dxi);
+  const dfl nyr = df_add_f({yh.x, yl.x}, dyr), nyi = df_add_f({yh.y, yl.y}, dyi);
+  xh = make_float2(nxr.h, nxi.h);
+  xl = make_float2(nxr.l, nxi.l);
+  yh = make_float2(nyr.h, nyi.h);
+  yl = make_float2(nyr.l, nyi.l);
+}
+
+// Staged double-float rotation of rows [0, len) of a column pair (as rot_cols_staged).
+template <int NT, int RPT>
+__device__ __forceinline__ void df_rot_cols_staged(float2* ph, float2* pl, float2* qh, float2* ql, int len, dfl c,
+                                                   dfl sr, dfl si, bool small) {
+  for (int base = 0; base < len; base += NT * RPT) {
+    float2 xh[RPT], xl[RPT], yh[RPT], yl[RPT];
+#pragma unroll
+    for (int j = 0; j < RPT; j++) {
+      const int r = base + threadIdx.x + j * NT;
+      if (r < len) {
+        xh[j] = ld_cg_ordered(ph + r); xl[j] = ld_cg_ordered(pl + r);
+        yh[j] = ld_cg_ordered(qh + r); yl[j] = ld_cg_ordered(ql + r);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < RPT; j++) {
+      const int r = base + threadIdx.x + j * NT;
+      if (r < len) {
+        if (small) df_rot_small(xh[j], xl[j], yh[j], yl[j], sr.h, si.h);
+        else df_rot(xh[j], xl[j], yh[j], yl[j], c, sr, si);
+        __stcg(ph + r, xh[j]); __stcg(pl + r, xl[j]); __stcg(qh + r, yh[j]); __stcg(ql + r, yl[j]);
+      }
+    }
+  }
+}
+
+struct DfParams {
+  dfl c, sr, si;
+  float tabs;
+  int go;
+};
+
+// 1 / sqrt(u) in double-float for u in [1/4, 4]: FP32 seed and two Newton steps with the
+// residual 1 - u c^2 formed in double-float.
+__device__ __forceinline__ dfl df_rsqrt(dfl u) {
+  float c0 = rsqrtf(u.h);
+  dfl c{c0, 0.f};
+#pragma unroll
+  for (int it = 0; it < 2; it++) {
+    const dfl c2 = df_mul(c, c);
+    const dfl r = df_add({1.f, 0.f}, df_neg(df_mul(u, c2)));  // ~2^-23, then ~2^-46
+    c = df_add(c, {0.5f * c.h * r.h, 0.f});
+  }
+  return c;
+}
+
+// Rotation parameters of a pair from double-float sums, on the FP32 pipes (the FP64 pipe of this
+// part is slow even for a single lane).  Same criterion as rotation_params: rotate when
+// |g| > tol sigma_max sqrt(min(a, b)) + (4 eps sigma_max)^2.  The tangent t comes from FP32
+// (zeta from the double-float difference b - a); c = 1 / sqrt(1 + t^2), s = t c and the phase
+// g / |g| are formed in double-float, so the rotation is unitary to ~2^-46 whatever t's rounding.
+// For |t| < 2^-24, c = 1 and s is kept in FP32 (the small-angle rotation uses only s.h).
+__device__ __forceinline__ bool rotation_params_df(dfl a, dfl b, dfl gr, dfl gi, float tol, float smax, DfParams& P) {
+  if (!(a.h > 0.f) || !(b.h > 0.f)) return false;
+  const float fl = 4.f * 2.220446049250313e-16f * smax;
+  const float mg = fmaxf(fabsf(gr.h), fabsf(gi.h));
+  if (!(mg > 0.5f * fl * fl)) return false;  // |g| <= sqrt(2) mg is below the rounding floor
+  // exact power-of-two scaling of g so |g'| is in [1, 2)
+  int e = 0;
+  frexpf(mg, &e);
+  const float sc = ldexpf(1.f, 1 - e);
+  const dfl grs{gr.h * sc, gr.l * sc}, gis{gi.h * sc, gi.l * sc};
+  const dfl n2 = df_add(df_mul(grs, grs), df_mul(gis, gis));  // [1, 8)
+  const float gabs = sqrtf(n2.h) / sc;                        // |g| in FP32
+  const float mn = fminf(a.h, b.h);
+  if (!(gabs > tol * smax * sqrtf(mn) + fl * fl)) return false;
+  const dfl d = df_add(b, df_neg(a));
+  const float zeta = (0.5f * d.h) / gabs;
+  const float az = fabsf(zeta);
+  float t = az > 1e18f ? 0.5f / az : 1.f / (az + sqrtf(1.f + az * az));
+  t = zeta >= 0.f ? t : -t;
+  if (!(t != 0.f)) return false;
+  // phase e^{i phi} = g / |g| in double-float
+  const dfl rg = df_rsqrt(n2);
+  const dfl er = df_mul(grs, rg), ei = df_mul(gis, rg);
+  P.tabs = fabsf(t);
+  if (fabsf(t) < 0x1p-24f) {
+    P.c = {1.f, 0.f};
+    P.sr = {t * er.h, 0.f};
+    P.si = {t * ei.h, 0.f};
+    return true;
+  }
+  const float tt = __fmul_rn(t, t);
+  const dfl u = df_add({1.f, 0.f}, {tt, fmaf(t, t, -tt)});  // 1 + t^2, t^2 exact as a pair
+  const dfl c = df_rsqrt(u);
+  const dfl sabs = df_mul(c, {t, 0.f});
+  P.c = c;
+  P.sr = df_mul(sabs, er);
+  P.si = df_mul(sabs, ei);
+  return true;
+}
+
+template <int NT, int RPT>
 __device__ __forceinline__ void jacobi_pair_df(float2* __restrict__ Bh, float2* __restrict__ Bl, long ldb, int m,
                                                int n, float2* __restrict__ Vh, float2* __restrict__ Vl, long ldv,
                                                int np, int round, int pair, double tol, double smax,
                                                unsigned* __restrict__ count) {
+  __shared__ float red[8][NT / 32];
+  __shared__ DfParams P;
   const int np1 = np - 1;
   int p, q;
   if (pair == 0) { p = round; q = np1; }
@@ -572,42 +742,65 @@ __device__ __forceinline__ void jacobi_pair_df(float2* __restrict__ Bh, float2* 
   if (p > q) { int t = p; p = q; q = t; }
   float2 *bph = Bh + (long)p * ldb, *bpl = Bl + (long)p * ldb;
   float2 *bqh = Bh + (long)q * ldb, *bql = Bl + (long)q * ldb;
-  dfl a{0.f, 0.f}, b{0.f, 0.f}, gr{0.f, 0.f}, gi{0.f, 0.f};
-  for (int r = threadIdx.x; r < m; r += NT) {
-    const float2 xh = __ldcg(bph + r), xl = __ldcg(bpl + r), yh = __ldcg(bqh + r), yl = __ldcg(bql + r);
-    const dfl xr{xh.x, xl.x}, xi{xh.y, xl.y}, yr{yh.x, yl.x}, yi{yh.y, yl.y};
-    a = df_fma(df_fma(a, xr, xr), xi, xi);
-    b = df_fma(df_fma(b, yr, yr), yi, yi);
-    gr = df_fma(df_fma(gr, xr, yr), xi, yi);
-    gi = df_fma(df_fma(gi, xr, yi), df_neg(xi), yr);
+  const bool fits = m <= NT * RPT;
+  float2 xh[RPT], xl[RPT], yh[RPT], yl[RPT];
+  DotAcc a{0.f, 0.f}, b{0.f, 0.f}, gr{0.f, 0.f}, gi{0.f, 0.f};
+  for (int base = 0; base < m; base += NT * RPT) {
+#pragma unroll
+    for (int j = 0; j < RPT; j++) {
+      const int r = base + threadIdx.x + j * NT;
+      if (r < m) { xh[j] = __ldcg(bph + r); xl[j] = __ldcg(bpl + r); yh[j] = __ldcg(bqh + r); yl[j] = __ldcg(bql + r); }
+      else { xh[j] = xl[j] = yh[j] = yl[j] = make_float2(0.f, 0.f); }
+    }
+#pragma unroll
+    for (int j = 0; j < RPT; j++) df_dot_acc(xh[j], xl[j], yh[j], yl[j], a, b, gr, gi);
   }
-  df_block_sum4<NT>(a, b, gr, gi);
-  double c, sr, si;
-  float tabs;
-  if (!rotation_params<double>(df_to(a), df_to(b), df_to(gr), df_to(gi), tol, smax, c, sr, si, tabs)) return;
-  const dfl cd = df_from(c), srd = df_from(sr), sid = df_from(si);
-  for (int r = threadIdx.x; r < m; r += NT) {
-    float2 xh = __ldcg(bph + r), xl = __ldcg(bpl + r), yh = __ldcg(bqh + r), yl = __ldcg(bql + r);
-    df_rot(xh, xl, yh, yl, cd, srd, sid);
-    __stcg(bph + r, xh); __stcg(bpl + r, xl); __stcg(bqh + r, yh); __stcg(bql + r, yl);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  const dfl k = df_warp_sum4_t(dot_final(a), dot_final(b), dot_final(gr), dot_final(gi));
+  if ((l & 7) == 0) { red[2 * (l >> 3)][w] = k.h; red[2 * (l >> 3) + 1][w] = k.l; }
+  __syncthreads();
+  if (w == 0) {
+    dfl v{0.f, 0.f};
+    if (l < 4) {
+#pragma unroll
+      for (int i = 0; i < NT / 32; i++) v = df_add(v, {red[2 * l][i], red[2 * l + 1][i]});
+    }
+    const dfl sa = df_shfl(v, 0), sb = df_shfl(v, 1), sgr = df_shfl(v, 2), sgi = df_shfl(v, 3);
+    if (l == 0) P.go = rotation_params_df(sa, sb, sgr, sgi, (float)tol, (float)smax, P) ? 1 : 0;
   }
-  float2 *vph = Vh + (long)p * ldv, *vpl = Vl + (long)p * ldv;
-  float2 *vqh = Vh + (long)q * ldv, *vql = Vl + (long)q * ldv;
-  for (int r = threadIdx.x; r < n; r += NT) {
-    float2 xh = __ldcg(vph + r), xl = __ldcg(vpl + r), yh = __ldcg(vqh + r), yl = __ldcg(vql + r);
-    df_rot(xh, xl, yh, yl, cd, srd, sid);
-    __stcg(vph + r, xh); __stcg(vpl + r, xl); __stcg(vqh + r, yh); __stcg(vql + r, yl);
+  __syncthreads();
+  if (!P.go) return;
+  const dfl cd = P.c, srd = P.sr, sid = P.si;
+  const bool small = P.tabs < 0x1p-24f;
+  if (fits) {
+#pragma unroll
+    for (int j = 0; j < RPT; j++) {
+      const int r = threadIdx.x + j * NT;
+      if (small) df_rot_small(xh[j], xl[j], yh[j], yl[j], srd.h, sid.h);
+      else df_rot(xh[j], xl[j], yh[j], yl[j], cd, srd, sid);
+      if (r < m) { __stcg(bph + r, xh[j]); __stcg(bpl + r, xl[j]); __stcg(bqh + r, yh[j]); __stcg(bql + r, yl[j]); }
+    }
+  } else {  // rows beyond NT * RPT (rare): reload and rotate row by row
+    for (int r = threadIdx.x; r < m; r += NT) {
+      float2 uh = __ldcg(bph + r), ul = __ldcg(bpl + r), wh = __ldcg(bqh + r), wl = __ldcg(bql + r);
+      if (small) df_rot_small(uh, ul, wh, wl, srd.h, sid.h);
+      else df_rot(uh, ul, wh, wl, cd, srd, sid);
+      __stcg(bph + r, uh); __stcg(bpl + r, ul); __stcg(bqh + r, wh); __stcg(bql + r, wl);
+    }
   }
+  asm volatile("" ::: "memory");
+  df_rot_cols_staged<NT, RPT / 2>(Vh + (long)p * ldv, Vl + (long)p * ldv, Vh + (long)q * ldv, Vl + (long)q * ldv, n, cd,
+                              srd, sid, small);
   if (threadIdx.x == 0) {
     atomicAdd(count, 1u);
-    atomicMax(count + 1, __float_as_uint(tabs));
+    atomicMax(count + 1, __float_as_uint(P.tabs));
   }
 }
 
 // One polish sweep in double-float, convergence decided on the device (state layout as in
 // jacobi_sweep_dev_k; sigma_max of the pre-scaled columns is smax_p[0] / smax_p[1]).
-template <int NT>
-__global__ void __launch_bounds__(NT) jacobi_sweep_df_k(float2* __restrict__ Bh, float2* __restrict__ Bl, long ldb,
+template <int NT, int RPT>
+__global__ void __launch_bounds__(NT, 2) jacobi_sweep_df_k(float2* __restrict__ Bh, float2* __restrict__ Bl, long ldb,
                                                         int m, int n, float2* __restrict__ Vh, float2* __restrict__ Vl,
                                                         long ldv, int np, double tol, const double* __restrict__ smax_p,
                                                         unsigned* __restrict__ state, int sweep) {
@@ -617,7 +810,7 @@ __global__ void __launch_bounds__(NT) jacobi_sweep_df_k(float2* __restrict__ Bh,
   const int npairs = np / 2;
   for (int round = 0; round < np - 1; round++) {
     for (int pair = blockIdx.x; pair < npairs; pair += gridDim.x)
-      jacobi_pair_df<NT>(Bh, Bl, ldb, m, n, Vh, Vl, ldv, np, round, pair, tol, smax, cnt);
+      jacobi_pair_df<NT, RPT>(Bh, Bl, ldb, m, n, Vh, Vl, ldv, np, round, pair, tol, smax, cnt);
     if (!grid_barrier(state + 2)) return;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -628,27 +821,18 @@ __global__ void __launch_bounds__(NT) jacobi_sweep_df_k(float2* __restrict__ Bh,
   }
 }
 
-__global__ void to_df_k(const double2* __restrict__ src, long lds, int rows, int cols, float2* __restrict__ hi,
-                        float2* __restrict__ lo, long ldd) {
-  long total = (long)rows * cols;
+// Xh[:, j] = src[:, perm[j]], Xl = 0 (an FP32 matrix as a double-float one, columns permuted)
+__global__ void gather_cols_f2_k(const float2* __restrict__ src, long lds, int rows, int cols,
+                                 const int* __restrict__ perm, float2* __restrict__ hi, float2* __restrict__ lo,
+                                 long ldd) {
+  const long total = (long)rows * cols;
   for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
-    long i = t % rows, j = t / rows;
-    const double2 v = src[i + j * lds];
-    const dfl re = df_from(v.x), im = df_from(v.y);
-    hi[i + j * ldd] = make_float2(re.h, im.h);
-    lo[i + j * ldd] = make_float2(re.l, im.l);
+    const long i = t % rows, j = t / rows;
+    hi[i + j * ldd] = src[i + (long)perm[j] * lds];
+    lo[i + j * ldd] = make_float2(0.f, 0.f);
   }
 }
 
-__global__ void from_df_k(const float2* __restrict__ hi, const float2* __restrict__ lo, long lds, int rows, int cols,
-                          double2* __restrict__ dst, long ldd) {
-  long total = (long)rows * cols;
-  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
-    long i = t % rows, j = t / rows;
-    const float2 h = hi[i + j * lds], l = lo[i + j * lds];
-    dst[i + j * ldd] = make_double2((double)h.x + (double)l.x, (double)h.y + (double)l.y);
-  }
-}
 
 // out[0] = max_j nrm[j] (one block)
 __global__ void max_reduce_k(const double* __restrict__ nrm, int k, double* __restrict__ out) {
@@ -710,10 +894,6 @@ __global__ void gather_cols_k(const CS* __restrict__ src, long lds, int rows, in
   }
 }
 
-__global__ void add_identity_k(double2* A, int n, long lda, double alpha) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) A[i + (long)i * lda].x += alpha;
-}
 
 // Q[:, j] *= phase(R_jj) (R_jj == 0 -> 1): keeps Q as close to the input columns as possible
 __global__ void phase_fix_k(double2* Q, long ldq, int m, int k, const double2* R, long ldr) {
@@ -848,44 +1028,25 @@ int jacobi(cudaStream_t s, SvdWork* w, cplx_t<T>* B, long ldb, int rows, int k, 
   return QR_OK;
 }
 
-// FP64-accurate polish of (B, V) in double-float on the FP32 pipes: B is scaled by a power of
-// two so sigma_max ~ 1, both are converted to (hi, lo) pairs, the sweeps run with device-side
-// convergence, and the result is converted back (one host synchronisation).
-int jacobi_df(cudaStream_t s, SvdWork* w, double2* B, long ldb, int rows, int k, double2* V, long ldv,
-              int max_sweeps, double tol) {
-  constexpr int NT = 128;
+// FP64-accurate polish of (B, V) in double-float on the FP32 pipes.  B (rows x k) and V (k x k)
+// arrive as split (hi, lo) arrays with B's columns pre-scaled by a power of two; smax_d[0] /
+// smax_d[1] is sigma_max of the scaled columns.  Sweeps run with device-side convergence and one
+// host synchronisation at the end.
+int jacobi_df(cudaStream_t s, SvdWork* w, float2* Bh, float2* Bl, long ldb, int rows, int k, float2* Vh,
+              float2* Vl, long ldv, int max_sweeps, double tol, const double* smax_d) {
+  constexpr int NT = 256, RPT = 8;
   const int np = k + (k & 1);
   const double pairs = 0.5 * (double)k * (k - 1);
   const int nstate = 8 + 2 * max_sweeps;
   QR_TRY(w->cnt.ensure(sizeof(unsigned) * nstate + 128, s));
-  QR_TRY(w->B32.ensure(sizeof(float2) * (size_t)rows * k, s));
-  QR_TRY(w->Bl.ensure(sizeof(float2) * (size_t)rows * k, s));
-  QR_TRY(w->V32.ensure(sizeof(float2) * (size_t)k * k, s));
-  QR_TRY(w->Vl.ensure(sizeof(float2) * (size_t)k * k, s));
-  float2 *Bh = w->B32.as<float2>(), *Bl = w->Bl.as<float2>();
-  float2 *Vh = w->V32.as<float2>(), *Vl = w->Vl.as<float2>();
   unsigned* state = w->cnt.as<unsigned>();
-  double* nrm = w->nrm.as<double>();
-  double* smax_d = reinterpret_cast<double*>(state + nstate + (nstate & 1));
   QR_CUDA(cudaMemsetAsync(state, 0, sizeof(unsigned) * nstate, s));
-  col_norms_k<double2><<<ceil_div((long)k * 32, TPB), TPB, 0, s>>>(B, ldb, rows, k, nrm);
-  QR_CHECK_LAUNCH("col_norms_k");
-  max_reduce_k<<<1, 256, 0, s>>>(nrm, k, smax_d);
-  QR_CHECK_LAUNCH("max_reduce_k");
-  const long totb = (long)rows * k;
-  const unsigned gb = (unsigned)std::min<long>((totb + TPB - 1) / TPB, 4864);
-  pow2_scale_k<double2><<<gb, TPB, 0, s>>>(B, ldb, rows, k, smax_d, smax_d + 1, 0);
-  QR_CHECK_LAUNCH("pow2_scale_k");
-  to_df_k<<<gb, TPB, 0, s>>>(B, ldb, rows, k, Bh, Bl, rows);
-  QR_CHECK_LAUNCH("to_df_k");
-  to_df_k<<<gs((long)k * k), TPB, 0, s>>>(V, ldv, k, k, Vh, Vl, k);
-  QR_CHECK_LAUNCH("to_df_k");
   static int per_sm = 0, sms = 0;
   if (per_sm == 0) {
     int dev = 0;
     QR_CUDA(cudaGetDevice(&dev));
     QR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    QR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, jacobi_sweep_df_k<NT>, NT, 0));
+    QR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, jacobi_sweep_df_k<NT, RPT>, NT, 0));
     if (per_sm < 1) return fail(QR_ECUDA, "double-float sweep kernel cannot be resident");
   }
   int grid = std::min(per_sm * sms, np / 2);
@@ -893,22 +1054,16 @@ int jacobi_df(cudaStream_t s, SvdWork* w, double2* B, long ldb, int rows, int k,
   int pr = prof_begin(s, PK_JACOBI_DF, 0.0, 0.0);
   for (int sweep = 0; sweep < max_sweeps; sweep++) {
     float2 *a1 = Bh, *a2 = Bl, *a3 = Vh, *a4 = Vl;
-    long l1 = rows, l2 = k;
+    long l1 = ldb, l2 = ldv;
     int mm = rows, kk = k, npp = np, sw = sweep;
     double tl = tol;
     const double* sm = smax_d;
     unsigned* st = state;
     void* args[] = {&a1, &a2, &l1, &mm, &kk, &a3, &a4, &l2, &npp, &tl, &sm, &st, &sw};
-    QR_CUDA(cudaLaunchCooperativeKernel((const void*)jacobi_sweep_df_k<NT>, dim3(grid), dim3(NT), args, 0, s));
+    QR_CUDA(cudaLaunchCooperativeKernel((const void*)jacobi_sweep_df_k<NT, RPT>, dim3(grid), dim3(NT), args, 0, s));
     count_launch();
   }
   prof_end(s, pr);
-  from_df_k<<<gb, TPB, 0, s>>>(Bh, Bl, rows, rows, k, B, ldb);
-  QR_CHECK_LAUNCH("from_df_k");
-  from_df_k<<<gs((long)k * k), TPB, 0, s>>>(Vh, Vl, k, k, k, V, ldv);
-  QR_CHECK_LAUNCH("from_df_k");
-  pow2_scale_k<double2><<<gb, TPB, 0, s>>>(B, ldb, rows, k, smax_d, smax_d + 1, 1);
-  QR_CHECK_LAUNCH("pow2_scale_k");
   std::vector<unsigned>& hs = w->hc;
   hs.assign(nstate, 0u);
   QR_CUDA(cudaMemcpyAsync(hs.data(), state, sizeof(unsigned) * nstate, cudaMemcpyDeviceToHost, s));
@@ -924,8 +1079,9 @@ int jacobi_df(cudaStream_t s, SvdWork* w, double2* B, long ldb, int rows, int k,
       fprintf(stderr, "[qr] jacobi<df> %dx%d sweep %d rotations %u max tan %.2e\n", rows, k, sw, hs[8 + 2 * sw], tmax);
     }
   }
-  // FP32 operations: ~152 per row per inner-product pass and ~184 per row and column rotated
-  prof_account(pr, 152.0 * rows * pairs * ran + 368.0 * rotated * (rows + k),
+  // FP32 operations: ~96 per row per inner-product pass (compensated sums) and ~100-340 per row
+  // and column rotated (small-angle / general rotation); the count takes the general form
+  prof_account(pr, 96.0 * rows * pairs * ran + 344.0 * rotated * (rows + k),
                sizeof(float2) * 2.0 * ((double)rows + k) * 2.0 * (pairs * ran + rotated));
   if (!hs[0]) return fail(QR_ENOCONV, "double-float Jacobi polish did not converge");
   return QR_OK;
@@ -992,40 +1148,53 @@ int zsvd_thin(cudaStream_t s, SvdWork* w, int mode, const double2* A, int m, int
     // above the FP32 rounding floor (~sqrt(m) eps32) so sweeps stop once rotations are noise
     float tol32 = fmaxf(4e-6f, 2.0f * sqrtf((float)rows) * Eps<float>::v);
     QR_TRY(jacobi<float>(s, w, B32, rows, rows, k, V32, k, 20, tol32, false));
-    // X = V32 sorted by the FP32 column norms (descending), promoted to FP64
+    // X = V32 with columns sorted by the FP32 column norms (descending), as a double-float
+    // matrix (low parts zero); the Newton-Schulz steps and B = A X run in double-float on the
+    // FP32 pipes and B goes straight into the double-float polish
     col_norms_k<float2><<<ceil_div((long)k * 32, TPB), TPB, 0, s>>>(B32, rows, rows, k, nrm);
     QR_CHECK_LAUNCH("col_norms_k");
     rank_sort_k<<<ceil_div(k, TPB), TPB, 0, s>>>(nrm, k, perm, nullptr);
     QR_CHECK_LAUNCH("rank_sort_k");
-    QR_TRY(w->X.ensure(sizeof(double2) * (size_t)k * k, s));
-    QR_TRY(w->Rm.ensure(sizeof(double2) * (size_t)k * k, s));
-    double2* X = w->X.as<double2>();
-    double2* Rm = w->Rm.as<double2>();
-    gather_cols_k<float2><<<gs((long)k * k), TPB, 0, s>>>(V32, k, k, k, perm, nullptr, X, k);
-    QR_CHECK_LAUNCH("gather_cols_k");
-    const double2 one = make_double2(1.0, 0.0), zero = make_double2(0.0, 0.0), mone = make_double2(-1.0, 0.0);
-    const double2* Bsrc = B;  // A (tall) or A^H (wide) in FP64, rows x k
-    // B is reused below as the product A X, so keep the FP64 source in T1
-    QR_TRY(w->T1.ensure(sizeof(double2) * (size_t)rows * k, s));
-    double2* Asrc = w->T1.as<double2>();
-    QR_CUDA(cudaMemcpyAsync(Asrc, Bsrc, sizeof(double2) * (size_t)rows * k, cudaMemcpyDeviceToDevice, s));
-    // X must be unitary to FP64 before it can carry the polish rotations: two Newton-Schulz
-    // steps X <- X + X (I - X^H X) / 2 square the FP32-level error twice (1e-5 -> 1e-10 -> 1e-20)
-    const double2 half = make_double2(0.5, 0.0);
+    const size_t kk2 = (size_t)k * k, rk = (size_t)rows * k;
+    QR_TRY(w->X.ensure(sizeof(float2) * 2 * kk2, s));   // X (hi, lo)
+    QR_TRY(w->Rm.ensure(sizeof(float2) * 2 * kk2, s));  // Newton-Schulz output (hi, lo)
+    QR_TRY(w->E.ensure(sizeof(float2) * kk2, s));       // R = I - X^H X (FP32)
+    QR_TRY(w->T1.ensure(sizeof(float2) * 2 * rk, s));   // A (hi, lo)
+    QR_TRY(w->Bl.ensure(sizeof(float2) * rk, s));       // B low parts (high parts reuse B32)
+    float2 *Xh = w->X.as<float2>(), *Xl = Xh + kk2;
+    float2 *Yh = w->Rm.as<float2>(), *Yl = Yh + kk2;
+    float2* R = w->E.as<float2>();
+    float2 *Ah = w->T1.as<float2>(), *Al = Ah + rk;
+    float2 *Bh = B32, *Bl = w->Bl.as<float2>();
+    gather_cols_f2_k<<<gs((long)k * k), TPB, 0, s>>>(V32, k, k, k, perm, Xh, Xl, k);
+    QR_CHECK_LAUNCH("gather_cols_f2_k");
+    // X must be unitary to double-float accuracy before it carries the polish rotations: two
+    // Newton-Schulz steps X <- X + X (I - X^H X) / 2 square the FP32-level error twice
+    // (1e-6 -> 1e-12 -> rounding).  I - X^H X needs the compensated products; X R has |R| << 1,
+    // so FP32 products are accurate enough for the correction term.
     for (int it = 0; it < 2; it++) {
-      QR_TRY(zgemm(s, OP_C, OP_N, k, k, k, mone, X, k, 0, X, k, 0, zero, Rm, k, 0, 1, nullptr));
-      add_identity_k<<<ceil_div(k, TPB), TPB, 0, s>>>(Rm, k, k, 1.0);
-      QR_CHECK_LAUNCH("add_identity_k");
-      QR_CUDA(cudaMemcpyAsync(V, X, sizeof(double2) * (size_t)k * k, cudaMemcpyDeviceToDevice, s));
-      QR_TRY(zgemm(s, OP_N, OP_N, k, k, k, half, V, k, 0, Rm, k, 0, one, X, k, 0, 1, nullptr));
+      QR_TRY(zgemm_df(s, DF_I_MINUS, OP_C, k, k, k, Xh, Xl, k, Xh, Xl, k, R, nullptr, k));
+      QR_TRY(zgemm_df(s, DF_F32_AXPY, OP_N, k, k, k, Xh, nullptr, k, R, nullptr, k, Yh, Yl, k, Xh, Xl, k, 0.5f));
+      std::swap(Xh, Yh);
+      std::swap(Xl, Yl);
     }
-    // B = A X, then Hestenes sweeps on (B, X) in double-float: they finish the near-degenerate
-    // pairs the FP32 sweeps leave and bring the couplings down to the double-float tolerance
-    QR_TRY(zgemm(s, OP_N, OP_N, rows, k, k, one, Asrc, rows, 0, X, k, 0, zero, B, rows, 0, 1, nullptr));
-    QR_CUDA(cudaMemcpyAsync(V, X, sizeof(double2) * (size_t)k * k, cudaMemcpyDeviceToDevice, s));
-    // double-float inner products carry ~sqrt(rows) 2^-48 relative noise: the tolerance sits 2x
-    // above that floor so converged pairs stop rotating
-    QR_TRY(jacobi_df(s, w, B, rows, rows, k, V, k, 40, 32.0 * sqrt((double)rows) * Eps<double>::v));
+    // A (B holds A or A^H in FP64) scaled by a power of two so sigma_max ~ 1, then B = A X
+    double* smax_d = sorted;  // two scratch doubles; `sorted` is rewritten below
+    col_norms_k<double2><<<ceil_div((long)k * 32, TPB), TPB, 0, s>>>(B, rows, rows, k, nrm);
+    QR_CHECK_LAUNCH("col_norms_k");
+    max_reduce_k<<<1, 256, 0, s>>>(nrm, k, smax_d);
+    QR_CHECK_LAUNCH("max_reduce_k");
+    pow2_scale_k<double2><<<gs((long)rows * k), TPB, 0, s>>>(B, rows, rows, k, smax_d, smax_d + 1, 0);
+    QR_CHECK_LAUNCH("pow2_scale_k");
+    QR_TRY(z2df(s, B, rows, rows, k, nullptr, Ah, Al, rows));
+    QR_TRY(zgemm_df(s, DF_STORE, OP_N, rows, k, k, Ah, Al, rows, Xh, Xl, k, Bh, Bl, rows));
+    // Hestenes sweeps on (B, X) in double-float finish the near-degenerate pairs the FP32 sweeps
+    // leave and bring the couplings down to the double-float tolerance (inner products carry
+    // ~sqrt(rows) 2^-48 relative noise; the tolerance sits 2x above that floor)
+    QR_TRY(jacobi_df(s, w, Bh, Bl, rows, rows, k, Xh, Xl, k, 40, 32.0 * sqrt((double)rows) * Eps<double>::v,
+                     smax_d));
+    QR_TRY(df2z(s, Bh, Bl, rows, rows, k, smax_d + 1, B, rows));
+    QR_TRY(df2z(s, Xh, Xl, k, k, k, nullptr, V, k));
   }
 
   // ---- sigma, ordering, factors

@@ -96,6 +96,62 @@ int qr_test_zgemm_split(int opA, int opB, int M, int N, int K, const double* A, 
   return QR_OK;
 }
 
+// Double-float GEMM (gemm_df.cu) through FP64 host matrices: inputs are split into (hi, lo) FP32
+// pairs on the device, the result converted back (mode 1 returns the FP32 value I - op(A) B).
+int qr_test_zgemm_df(int mode, int opA, int M, int N, int K, const double* A, long lda, const double* B, long ldb,
+                     const double* D, double* C, long ldc, int iters, double* ms_per_iter) {
+  if (M <= 0 || N <= 0 || K < 0 || iters < 1 || mode < 0 || mode > 2) return fail(QR_EINVAL, "bad gemm_df shape");
+  if (opA != OP_N && opA != OP_T && opA != OP_C) return fail(QR_EINVAL, "op(A) must be N, T or C");
+  const long ca = opA == OP_N ? K : M, rb = K;
+  if (lda < (opA == OP_N ? M : K) || ldb < rb || ldc < M) return fail(QR_EINVAL, "bad leading dimension");
+  if (mode == 2 && !D) return fail(QR_EINVAL, "mode 2 needs D");
+  Dev dA, dB, dD, aS, bS, cS, dS;
+  QR_TRY(up(dA, A, (size_t)lda * ca));
+  QR_TRY(up(dB, B, (size_t)ldb * N));
+  QR_TRY(up(aS, nullptr, (size_t)lda * ca));  // (hi, lo) float2 pairs: 16 bytes per element
+  QR_TRY(up(bS, nullptr, (size_t)ldb * N));
+  QR_TRY(up(cS, nullptr, (size_t)ldc * N));
+  const size_t na = (size_t)lda * ca, nb = (size_t)ldb * N, nc = (size_t)ldc * N;
+  float2 *Ah = (float2*)aS.p, *Al = Ah + na, *Bh = (float2*)bS.p, *Bl = Bh + nb, *Ch = (float2*)cS.p, *Cl = Ch + nc;
+  float2 *Dh = nullptr, *Dl = nullptr;
+  QR_TRY(z2df(0, (double2*)dA.p, lda, (int)lda, (int)ca, nullptr, Ah, Al, lda));
+  QR_TRY(z2df(0, (double2*)dB.p, ldb, (int)ldb, N, nullptr, Bh, Bl, ldb));
+  if (mode == 2) {
+    QR_TRY(up(dD, D, nc));
+    QR_TRY(up(dS, nullptr, nc));
+    Dh = (float2*)dS.p;
+    Dl = Dh + nc;
+    QR_TRY(z2df(0, (double2*)dD.p, ldc, (int)ldc, N, nullptr, Dh, Dl, ldc));
+  }
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0);
+  int rc = QR_OK;
+  for (int it = 0; it < iters && rc == QR_OK; it++)
+    rc = zgemm_df(0, mode, opA, M, N, K, Ah, mode == 2 ? nullptr : Al, lda, Bh, mode == 2 ? nullptr : Bl, ldb, Ch,
+                  Cl, ldc, Dh, Dl, ldc, 0.5f);
+  cudaEventRecord(e1);
+  cudaEventSynchronize(e1);
+  float t = 0;
+  cudaEventElapsedTime(&t, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  QR_TRY(rc);
+  if (ms_per_iter) *ms_per_iter = t / iters;
+  if (mode == 1) {
+    std::vector<float2> h(nc);
+    QR_CUDA(cudaMemcpy(h.data(), Ch, sizeof(float2) * nc, cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < nc; i++) { C[2 * i] = h[i].x; C[2 * i + 1] = h[i].y; }
+    return QR_OK;
+  }
+  Dev dC;
+  QR_TRY(up(dC, nullptr, nc));
+  QR_TRY(df2z(0, Ch, Cl, ldc, (int)ldc, N, nullptr, (double2*)dC.p, ldc));
+  QR_CUDA(cudaMemcpy(C, dC.p, sizeof(double2) * nc, cudaMemcpyDeviceToHost));
+  return QR_OK;
+}
+
 // Thin SVD of the m x n column-major A: U (m x k), S (k), Vh (k x n), k = min(m, n).
 int qr_test_svd(int mode, int m, int n, const double* A, double* U, double* S, double* Vh, double* ms) {
   if (m <= 0 || n <= 0) return fail(QR_EINVAL, "bad svd shape");

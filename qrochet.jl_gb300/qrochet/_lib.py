@@ -97,6 +97,7 @@ SIGNATURES = {
     "qr_svd_noalloc": [_I, _I, _P, C.c_long, _P, C.c_long, _P, _P, C.c_long, _P],
     "qr_test_zgemm": [_I, _I, _I, _I, _I, _PD, _PD, C.c_long, _PD, C.c_long, _PD, _PD, C.c_long, _PD, _I, _PD],
     "qr_test_zgemm_split": [_I, _I, _I, _I, _I, _PD, C.c_long, _PD, C.c_long, _PD, C.c_long, _I, _PD],
+    "qr_test_zgemm_df": [_I, _I, _I, _I, _I, _PD, C.c_long, _PD, C.c_long, _PD, _PD, C.c_long, _I, _PD],
     "qr_test_svd": [_I, _I, _I, _PD, _PD, _PD, _PD, _PD],
     "qr_test_qr": [_I, _I, _PD, _PD, _PD, _PD],
 }

@@ -166,3 +166,66 @@ def test_zgemm_split_large_k():
     ref = A @ B
     rel = np.linalg.norm(got - ref) / np.linalg.norm(ref)
     assert rel <= 5e-7, rel
+
+
+def zgemm_df(mode, opA, A, B, M, N, D=None):
+    K = OPS[opA](A).shape[1]
+    A = np.asfortranarray(A, dtype=np.complex128)
+    B = np.asfortranarray(B, dtype=np.complex128)
+    out = np.zeros((M, N), dtype=np.complex128, order="F")
+    Dp = None if D is None else _p(np.asfortranarray(D, dtype=np.complex128))
+    ms = C.c_double()
+    _lib.check(_lib.lib().qr_test_zgemm_df(mode, opA, M, N, K, _p(A), A.shape[0], _p(B), B.shape[0], Dp, _p(out), M,
+                                           1, C.byref(ms)))
+    return out
+
+
+# double-float products: inputs rounded to ~2^-49, compensated sums ~2^-48 of sum |a||b|
+DF_TOL = 1e-13
+
+
+@pytest.mark.parametrize("opA", [0, 1, 2])
+def test_zgemm_df_store(opA):
+    g = R.rng(400 + opA)
+    M, N, K = 90, 70, 300
+    A0 = R.complex_gaussian(g, (M, K))
+    B0 = R.complex_gaussian(g, (K, N))
+    A = {0: A0, 1: A0.T.copy(), 2: A0.conj().T.copy()}[opA]
+    got = zgemm_df(0, opA, A, B0, M, N)
+    scale = (np.abs(A0) @ np.abs(B0)).max()
+    assert np.max(np.abs(got - A0 @ B0)) <= DF_TOL * scale
+
+
+def test_zgemm_df_large_k_ragged():
+    g = R.rng(411)
+    M, N, K = 131, 67, 2053  # partial tiles in every dimension
+    A0 = R.complex_gaussian(g, (M, K))
+    B0 = R.complex_gaussian(g, (K, N))
+    got = zgemm_df(0, 0, A0, B0, M, N)
+    scale = (np.abs(A0) @ np.abs(B0)).max()
+    assert np.max(np.abs(got - A0 @ B0)) <= DF_TOL * scale
+
+
+def test_zgemm_df_identity_minus_gram():
+    """I - X^H X for a unitary X perturbed at 1e-6 (the Newton-Schulz residual): the result is
+    ~1e-6 and must be accurate to the double-float level, not the FP32 level."""
+    g = R.rng(412)
+    k = 160
+    q, _ = np.linalg.qr(R.complex_gaussian(g, (k, k)))
+    X = q + 1e-6 * R.complex_gaussian(g, (k, k))
+    got = zgemm_df(1, 2, X, X, k, k)
+    ref = np.eye(k) - X.conj().T @ X
+    assert np.max(np.abs(ref)) > 1e-7
+    assert np.max(np.abs(got - ref)) <= 1e-13 + 1e-7 * np.max(np.abs(ref))
+
+
+def test_zgemm_df_axpy_fp32_products():
+    g = R.rng(413)
+    M, N, K = 100, 80, 120
+    A = R.complex_gaussian(g, (M, K))
+    Bm = 1e-6 * R.complex_gaussian(g, (K, N))
+    D = R.complex_gaussian(g, (M, N))
+    got = zgemm_df(2, 0, A, Bm, M, N, D=D)
+    ref = D + 0.5 * A @ Bm
+    # FP32 products of FP32-rounded inputs: ~1e-7 relative to the correction term, double-float D
+    assert np.max(np.abs(got - ref)) <= 1e-6 * 0.5 * (np.abs(A) @ np.abs(Bm)).max() + DF_TOL * np.abs(D).max()
