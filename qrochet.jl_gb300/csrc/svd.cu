@@ -352,19 +352,12 @@ __device__ __forceinline__ void rot_cols_staged(cplx_t<T>* xp, cplx_t<T>* xq, in
 // B and V columns.  When a column fits (m <= NT * RPT) it stays in registers between the inner
 // products and the rotation.
 template <typename T, int NT, int RPT>
-__device__ __forceinline__ void jacobi_pair_fast(cplx_t<T>* __restrict__ B, long ldb, int m, int n,
-                                                 cplx_t<T>* __restrict__ V, long ldv, int nv, int np,
-                                                 int round, int pair, T tol, T smax,
-                                                 unsigned* __restrict__ count) {
+__device__ __forceinline__ void jacobi_pair_fast(cplx_t<T>* __restrict__ B, long ldb, int m,
+                                                 cplx_t<T>* __restrict__ V, long ldv, int nv, int p, int q,
+                                                 T tol, T smax, unsigned* __restrict__ count) {
   using C = cplx_t<T>;
   __shared__ T red[4][NT / 32];
   __shared__ RotParams<T> P;
-  const int np1 = np - 1;
-  int p, q;
-  if (pair == 0) { p = round; q = np1; }
-  else { p = (round + pair) % np1; q = (round - pair + np1) % np1; }
-  if (p >= n || q >= n) return;
-  if (p > q) { int t = p; p = q; q = t; }
   C* bp = B + (long)p * ldb;
   C* bq = B + (long)q * ldb;
   const bool fits = m <= NT * RPT;
@@ -465,31 +458,116 @@ __global__ void pow2_scale_k(C* __restrict__ B, long ldb, int rows, int k, doubl
   if (!undo && blockIdx.x == 0 && threadIdx.x == 0) scale_out[0] = ldexp(1.0, e);
 }
 
+// ---- dataflow ordering of the round-robin sweep -------------------------------------------------
+// Round r of a sweep pairs column (r + i) mod (np - 1) with (r - i) mod (np - 1), and pair 0 with
+// column np - 1 (a padding column when k is odd).  Instead of a grid barrier between rounds, each
+// column carries the number of rounds it has completed (flags[c], counted from the first sweep of
+// the call): the pair of global round R waits until both columns reached R, rotates, and publishes
+// R + 1.  CTAs take work items (round, pair) in increasing order, so the earliest unfinished item
+// always has its inputs ready and the persistent (co-resident) grid cannot deadlock.  The flags
+// pay off when a round has more pairs than the grid has CTAs (they absorb the imbalance); with at
+// most one pair per CTA the kernels keep the bounded grid barrier between rounds.  A wait gives
+// up after ~2^22 polls: it sets state[4] (reported as an error) and state[5], which makes every
+// other wait return at once.
+__device__ __forceinline__ void pair_cols(int np, int round, int pair, int& p, int& q) {
+  const int np1 = np - 1;
+  if (pair == 0) { p = round; q = np1; }
+  else { p = (round + pair) % np1; q = (round - pair + np1) % np1; }
+  if (p > q) { int t = p; p = q; q = t; }
+}
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* a) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(a) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned* a, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(a), "r"(v) : "memory");
+}
+// returns false when the sweep is aborted (this or another CTA timed out)
+__device__ __forceinline__ bool wait_cols(const unsigned* flags, int p, int q, int n, unsigned R,
+                                          unsigned* state) {
+  __shared__ int ok;
+  if (threadIdx.x == 0) {
+    int good = 1;
+    unsigned polls = 0;
+    for (;;) {
+      // both flags in one round trip
+      const unsigned fp = p < n ? ld_acquire_u32(flags + p) : 0xffffffffu;
+      const unsigned fq = q < n ? ld_acquire_u32(flags + q) : 0xffffffffu;
+      if (fp >= R && fq >= R) break;
+      if (((volatile unsigned*)state)[5]) { good = 0; break; }
+      if (++polls > (1u << 22)) {
+        atomicExch(state + 4, 1u);
+        atomicExch(state + 5, 1u);
+        good = 0;
+        break;
+      }
+      __nanosleep(64);
+    }
+    ok = good;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+__device__ __forceinline__ void post_cols(unsigned* flags, int p, int q, int n, unsigned R1) {
+  __syncthreads();  // every thread's column stores precede thread 0's release (cumulative fence)
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (p < n) st_release_u32(flags + p, R1);
+    if (q < n) st_release_u32(flags + q, R1);
+  }
+}
+// The last CTA to finish the sweep records it and decides convergence (no rotation, or in FP64
+// and double-float a largest rotation tangent below 1e-8).
+__device__ __forceinline__ void finish_sweep(unsigned* state, const unsigned* cnt, int sweep, bool tan_rule) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned prev = atomicAdd(state + 6, 1u);
+    if (prev == gridDim.x - 1) {
+      __threadfence();
+      const unsigned h = ((volatile const unsigned*)cnt)[0];
+      const float tmax = __uint_as_float(((volatile const unsigned*)cnt)[1]);
+      state[1] = sweep + 1;
+      if (h == 0 || (tan_rule && tmax < 1e-8f)) state[0] = 1;
+      state[6] = 0;
+    }
+  }
+}
+
 // Sweep `sweep` of a Jacobi whose convergence is decided on the device, so the host enqueues
 // all sweeps at once and synchronises only at the end.  state[0] = converged flag (set by the
 // sweep that finds no rotation, or, in FP64, whose largest rotation tangent is < 1e-8; later
-// sweeps then return at once), state[1] = sweeps run, state[2..4] = grid barrier,
-// state[8 + 2 s] / [9 + 2 s] = rotations / largest tangent (float bits) of sweep s.
+// sweeps then return at once), state[1] = sweeps run, state[2..3] = grid barrier, state[4] /
+// [5] = wait (flag or barrier) timeout / abort,
+// state[6] = CTAs done with the sweep, state[8 + 2 s] / [9 + 2 s] = rotations / largest tangent
+// (float bits) of sweep s; flags[c] = rounds completed by column c (dataflow ordering above).
 template <typename T, int NT, int RPT>
-__global__ void __launch_bounds__(NT) jacobi_sweep_dev_k(cplx_t<T>* __restrict__ B, long ldb, int m, int n,
+__global__ void __launch_bounds__(NT, 512 / NT) jacobi_sweep_dev_k(cplx_t<T>* __restrict__ B, long ldb, int m, int n,
                                                          cplx_t<T>* __restrict__ V, long ldv, int np, T tol,
                                                          const double* __restrict__ smax_p,
-                                                         unsigned* __restrict__ state, int sweep) {
+                                                         unsigned* __restrict__ state, int sweep,
+                                                         unsigned* __restrict__ flags) {
   if (((volatile unsigned*)state)[0]) return;
   const T smax = (T)(smax_p[0] / smax_p[1]);  // sigma_max of the pre-scaled columns (~1)
   unsigned* cnt = state + 8 + 2 * sweep;
   const int npairs = np / 2;
-  for (int round = 0; round < np - 1; round++) {
-    for (int pair = blockIdx.x; pair < npairs; pair += gridDim.x)
-      jacobi_pair_fast<T, NT, RPT>(B, ldb, m, n, V, ldv, n, np, round, pair, tol, smax, cnt);
-    if (!grid_barrier(state + 2)) return;
+  const unsigned base = (unsigned)sweep * (unsigned)(np - 1);
+  // dataflow: work items in (round, pair) order dealt round-robin to the CTAs, so the surplus
+  // pairs rotate over the CTAs from round to round; barrier mode: CTA b owns pair b of every round
+  const bool dataflow = npairs > (int)gridDim.x;
+  const long nit = dataflow ? ((long)(np - 1) * npairs - blockIdx.x + gridDim.x - 1) / gridDim.x : (long)(np - 1);
+  for (long t = 0; t < nit; t++) {
+    const long it = dataflow ? blockIdx.x + t * (long)gridDim.x : t * npairs + blockIdx.x;
+    const int round = (int)(it / npairs), pair = (int)(it % npairs);
+    int p, q;
+    pair_cols(np, round, pair, p, q);
+    if (dataflow && !wait_cols(flags, p, q, n, base + round, state)) return;
+    if (q < n) jacobi_pair_fast<T, NT, RPT>(B, ldb, m, V, ldv, n, p, q, tol, smax, cnt);
+    if (dataflow) post_cols(flags, p, q, n, base + round + 1);
+    else if (!grid_barrier(state + 2)) return;
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    const unsigned h = ((volatile unsigned*)cnt)[0];
-    const float tmax = __uint_as_float(((volatile unsigned*)cnt)[1]);
-    state[1] = sweep + 1;
-    if (h == 0 || (sizeof(T) == 8 && tmax < 1e-8f)) state[0] = 1;
-  }
+  finish_sweep(state, cnt, sweep, sizeof(T) == 8);
 }
 
 // Small problems (k <= 128 columns): the whole Jacobi iteration in one thread-block cluster of
@@ -730,16 +808,9 @@ __device__ __forceinline__ bool rotation_params_df(dfl a, dfl b, dfl gr, dfl gi,
 template <int NT, int RPT>
 __device__ __forceinline__ void jacobi_pair_df(float2* __restrict__ Bh, float2* __restrict__ Bl, long ldb, int m,
                                                int n, float2* __restrict__ Vh, float2* __restrict__ Vl, long ldv,
-                                               int np, int round, int pair, double tol, double smax,
-                                               unsigned* __restrict__ count) {
+                                               int p, int q, double tol, double smax, unsigned* __restrict__ count) {
   __shared__ float red[8][NT / 32];
   __shared__ DfParams P;
-  const int np1 = np - 1;
-  int p, q;
-  if (pair == 0) { p = round; q = np1; }
-  else { p = (round + pair) % np1; q = (round - pair + np1) % np1; }
-  if (p >= n || q >= n) return;
-  if (p > q) { int t = p; p = q; q = t; }
   float2 *bph = Bh + (long)p * ldb, *bpl = Bl + (long)p * ldb;
   float2 *bqh = Bh + (long)q * ldb, *bql = Bl + (long)q * ldb;
   const bool fits = m <= NT * RPT;
@@ -803,22 +874,28 @@ template <int NT, int RPT>
 __global__ void __launch_bounds__(NT, 2) jacobi_sweep_df_k(float2* __restrict__ Bh, float2* __restrict__ Bl, long ldb,
                                                         int m, int n, float2* __restrict__ Vh, float2* __restrict__ Vl,
                                                         long ldv, int np, double tol, const double* __restrict__ smax_p,
-                                                        unsigned* __restrict__ state, int sweep) {
+                                                        unsigned* __restrict__ state, int sweep,
+                                                        unsigned* __restrict__ flags) {
   if (((volatile unsigned*)state)[0]) return;
   const double smax = smax_p[0] / smax_p[1];
   unsigned* cnt = state + 8 + 2 * sweep;
   const int npairs = np / 2;
-  for (int round = 0; round < np - 1; round++) {
-    for (int pair = blockIdx.x; pair < npairs; pair += gridDim.x)
-      jacobi_pair_df<NT, RPT>(Bh, Bl, ldb, m, n, Vh, Vl, ldv, np, round, pair, tol, smax, cnt);
-    if (!grid_barrier(state + 2)) return;
+  const unsigned base = (unsigned)sweep * (unsigned)(np - 1);
+  // dataflow: work items in (round, pair) order dealt round-robin to the CTAs, so the surplus
+  // pairs rotate over the CTAs from round to round; barrier mode: CTA b owns pair b of every round
+  const bool dataflow = npairs > (int)gridDim.x;
+  const long nit = dataflow ? ((long)(np - 1) * npairs - blockIdx.x + gridDim.x - 1) / gridDim.x : (long)(np - 1);
+  for (long t = 0; t < nit; t++) {
+    const long it = dataflow ? blockIdx.x + t * (long)gridDim.x : t * npairs + blockIdx.x;
+    const int round = (int)(it / npairs), pair = (int)(it % npairs);
+    int p, q;
+    pair_cols(np, round, pair, p, q);
+    if (dataflow && !wait_cols(flags, p, q, n, base + round, state)) return;
+    if (q < n) jacobi_pair_df<NT, RPT>(Bh, Bl, ldb, m, n, Vh, Vl, ldv, p, q, tol, smax, cnt);
+    if (dataflow) post_cols(flags, p, q, n, base + round + 1);
+    else if (!grid_barrier(state + 2)) return;
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    const unsigned h = ((volatile unsigned*)cnt)[0];
-    const float tmax = __uint_as_float(((volatile unsigned*)cnt)[1]);
-    state[1] = sweep + 1;
-    if (h == 0 || tmax < 1e-8f) state[0] = 1;
-  }
+  finish_sweep(state, cnt, sweep, true);
 }
 
 // Xh[:, j] = src[:, perm[j]], Xl = 0 (an FP32 matrix as a double-float one, columns permuted)
@@ -925,11 +1002,14 @@ int jacobi(cudaStream_t s, SvdWork* w, cplx_t<T>* B, long ldb, int rows, int k, 
   const int kind = sizeof(T) == 8 ? PK_JACOBI64 : PK_JACOBI32;
   const double pairs = 0.5 * (double)k * (k - 1);
   const int nstate = 8 + 2 * max_sweeps;
-  QR_TRY(w->cnt.ensure(sizeof(unsigned) * nstate + 128, s));
+  // [state (nstate) | column flags (np) | pad | smax, scale (2 doubles)]
+  const int soff = nstate + np + ((nstate + np) & 1);
+  QR_TRY(w->cnt.ensure(sizeof(unsigned) * soff + 2 * sizeof(double) + 128, s));
   unsigned* state = w->cnt.as<unsigned>();
+  unsigned* flags = state + nstate;
   double* nrm = w->nrm.as<double>();
-  double* smax_d = reinterpret_cast<double*>(state + nstate + (nstate & 1));
-  QR_CUDA(cudaMemsetAsync(state, 0, sizeof(unsigned) * nstate, s));
+  double* smax_d = reinterpret_cast<double*>(state + soff);
+  QR_CUDA(cudaMemsetAsync(state, 0, sizeof(unsigned) * (nstate + np), s));
   // sigma_max scale from the largest column norm, on the device
   col_norms_k<cplx_t<T>><<<ceil_div((long)k * 32, TPB), TPB, 0, s>>>(B, ldb, rows, k, nrm);
   QR_CHECK_LAUNCH("col_norms_k");
@@ -991,7 +1071,8 @@ int jacobi(cudaStream_t s, SvdWork* w, cplx_t<T>* B, long ldb, int rows, int k, 
       T tl = tol;
       const double* sm = smax_d;
       unsigned* st = state;
-      void* args[] = {&Bp, &ldbb, &mm, &kk2, &Vp, &ldvv, &npp, &tl, &sm, &st, &sw};
+      unsigned* fl = flags;
+      void* args[] = {&Bp, &ldbb, &mm, &kk2, &Vp, &ldvv, &npp, &tl, &sm, &st, &sw, &fl};
       QR_CUDA(cudaLaunchCooperativeKernel((const void*)jacobi_sweep_dev_k<T, NT, RPT>, dim3(grid), dim3(NT), args, 0, s));
       count_launch();
     }
@@ -1007,7 +1088,7 @@ int jacobi(cudaStream_t s, SvdWork* w, cplx_t<T>* B, long ldb, int rows, int k, 
   hs.assign(nstate, 0u);
   QR_CUDA(cudaMemcpyAsync(hs.data(), state, sizeof(unsigned) * nstate, cudaMemcpyDeviceToHost, s));
   QR_CUDA(cudaStreamSynchronize(s));
-  if (hs[4]) return fail(QR_ECUDA, "Jacobi sweep: grid barrier timed out");
+  if (hs[4]) return fail(QR_ECUDA, "Jacobi sweep: a column wait timed out");
   const int ran = (int)hs[1];
   double rotated = 0;
   for (int sw = 0; sw < ran; sw++) {
@@ -1038,9 +1119,10 @@ int jacobi_df(cudaStream_t s, SvdWork* w, float2* Bh, float2* Bl, long ldb, int 
   const int np = k + (k & 1);
   const double pairs = 0.5 * (double)k * (k - 1);
   const int nstate = 8 + 2 * max_sweeps;
-  QR_TRY(w->cnt.ensure(sizeof(unsigned) * nstate + 128, s));
+  QR_TRY(w->cnt.ensure(sizeof(unsigned) * (nstate + np) + 128, s));
   unsigned* state = w->cnt.as<unsigned>();
-  QR_CUDA(cudaMemsetAsync(state, 0, sizeof(unsigned) * nstate, s));
+  unsigned* flags = state + nstate;
+  QR_CUDA(cudaMemsetAsync(state, 0, sizeof(unsigned) * (nstate + np), s));
   static int per_sm = 0, sms = 0;
   if (per_sm == 0) {
     int dev = 0;
@@ -1059,7 +1141,8 @@ int jacobi_df(cudaStream_t s, SvdWork* w, float2* Bh, float2* Bl, long ldb, int 
     double tl = tol;
     const double* sm = smax_d;
     unsigned* st = state;
-    void* args[] = {&a1, &a2, &l1, &mm, &kk, &a3, &a4, &l2, &npp, &tl, &sm, &st, &sw};
+    unsigned* fl = flags;
+    void* args[] = {&a1, &a2, &l1, &mm, &kk, &a3, &a4, &l2, &npp, &tl, &sm, &st, &sw, &fl};
     QR_CUDA(cudaLaunchCooperativeKernel((const void*)jacobi_sweep_df_k<NT, RPT>, dim3(grid), dim3(NT), args, 0, s));
     count_launch();
   }
@@ -1068,7 +1151,7 @@ int jacobi_df(cudaStream_t s, SvdWork* w, float2* Bh, float2* Bl, long ldb, int 
   hs.assign(nstate, 0u);
   QR_CUDA(cudaMemcpyAsync(hs.data(), state, sizeof(unsigned) * nstate, cudaMemcpyDeviceToHost, s));
   QR_CUDA(cudaStreamSynchronize(s));
-  if (hs[4]) return fail(QR_ECUDA, "double-float Jacobi sweep: grid barrier timed out");
+  if (hs[4]) return fail(QR_ECUDA, "double-float Jacobi sweep: a column wait timed out");
   const int ran = (int)hs[1];
   double rotated = 0;
   for (int sw = 0; sw < ran; sw++) {
