@@ -517,9 +517,11 @@ __device__ __forceinline__ void post_cols(unsigned* flags, int p, int q, int n, 
     if (q < n) st_release_u32(flags + q, R1);
   }
 }
-// The last CTA to finish the sweep records it and decides convergence (no rotation, or in FP64
-// and double-float a largest rotation tangent below 1e-8).
-__device__ __forceinline__ void finish_sweep(unsigned* state, const unsigned* cnt, int sweep, bool tan_rule) {
+// The last CTA to finish the sweep records it and decides convergence: no rotation, or a largest
+// rotation tangent below tan_stop (1e-8 in FP64 and double-float, where the next sweep could only
+// rotate at the rounding level; larger for the FP32 preconditioner, whose near-degenerate pairs
+// the double-float polish resolves anyway; 0 = off).
+__device__ __forceinline__ void finish_sweep(unsigned* state, const unsigned* cnt, int sweep, float tan_stop) {
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
@@ -529,7 +531,7 @@ __device__ __forceinline__ void finish_sweep(unsigned* state, const unsigned* cn
       const unsigned h = ((volatile const unsigned*)cnt)[0];
       const float tmax = __uint_as_float(((volatile const unsigned*)cnt)[1]);
       state[1] = sweep + 1;
-      if (h == 0 || (tan_rule && tmax < 1e-8f)) state[0] = 1;
+      if (h == 0 || tmax < tan_stop) state[0] = 1;
       state[6] = 0;
     }
   }
@@ -547,7 +549,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) jacobi_sweep_dev_k(cplx_t<T>* __
                                                          cplx_t<T>* __restrict__ V, long ldv, int np, T tol,
                                                          const double* __restrict__ smax_p,
                                                          unsigned* __restrict__ state, int sweep,
-                                                         unsigned* __restrict__ flags) {
+                                                         unsigned* __restrict__ flags, float tan_stop) {
   if (((volatile unsigned*)state)[0]) return;
   const T smax = (T)(smax_p[0] / smax_p[1]);  // sigma_max of the pre-scaled columns (~1)
   unsigned* cnt = state + 8 + 2 * sweep;
@@ -567,7 +569,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) jacobi_sweep_dev_k(cplx_t<T>* __
     if (dataflow) post_cols(flags, p, q, n, base + round + 1);
     else if (!grid_barrier(state + 2)) return;
   }
-  finish_sweep(state, cnt, sweep, sizeof(T) == 8);
+  finish_sweep(state, cnt, sweep, tan_stop);
 }
 
 // Small problems (k <= 128 columns): the whole Jacobi iteration in one thread-block cluster of
@@ -895,7 +897,7 @@ __global__ void __launch_bounds__(NT, 2) jacobi_sweep_df_k(float2* __restrict__ 
     if (dataflow) post_cols(flags, p, q, n, base + round + 1);
     else if (!grid_barrier(state + 2)) return;
   }
-  finish_sweep(state, cnt, sweep, true);
+  finish_sweep(state, cnt, sweep, 1e-8f);
 }
 
 // Xh[:, j] = src[:, perm[j]], Xl = 0 (an FP32 matrix as a double-float one, columns permuted)
@@ -995,7 +997,8 @@ inline unsigned gs(long n) {
 // whose convergence is decided on the device.  One host synchronisation per call.
 template <typename T>
 int jacobi(cudaStream_t s, SvdWork* w, cplx_t<T>* B, long ldb, int rows, int k, cplx_t<T>* V,
-           long ldv, int max_sweeps, T tol, bool must_converge = true) {
+           long ldv, int max_sweeps, T tol, bool must_converge = true, float tan_stop = -1.f) {
+  if (tan_stop < 0.f) tan_stop = sizeof(T) == 8 ? 1e-8f : 0.f;
   const int np = k + (k & 1);
   constexpr int NT = sizeof(T) == 8 ? 256 : 128;
   constexpr int RPT = sizeof(T) == 8 ? 8 : 16;
@@ -1072,7 +1075,8 @@ int jacobi(cudaStream_t s, SvdWork* w, cplx_t<T>* B, long ldb, int rows, int k, 
       const double* sm = smax_d;
       unsigned* st = state;
       unsigned* fl = flags;
-      void* args[] = {&Bp, &ldbb, &mm, &kk2, &Vp, &ldvv, &npp, &tl, &sm, &st, &sw, &fl};
+      float ts = tan_stop;
+      void* args[] = {&Bp, &ldbb, &mm, &kk2, &Vp, &ldvv, &npp, &tl, &sm, &st, &sw, &fl, &ts};
       QR_CUDA(cudaLaunchCooperativeKernel((const void*)jacobi_sweep_dev_k<T, NT, RPT>, dim3(grid), dim3(NT), args, 0, s));
       count_launch();
     }
@@ -1187,6 +1191,11 @@ static int reorthonormalize(cudaStream_t s, SvdWork* w, double2* L, long ldl, in
   return QR_OK;
 }
 
+// The FP32 preconditioner stops once a sweep's largest rotation is below this tangent: its last
+// sweeps only turn near-degenerate pairs that FP32 cannot separate and the double-float polish
+// turns again in its first sweep.
+constexpr float kPrecondTanStop = 0.15f;
+
 int zsvd_thin(cudaStream_t s, SvdWork* w, int mode, const double2* A, int m, int n, long lda,
               double2* U, long ldu, double* S, double2* Vh, long ldvh, int keep) {
   if (m <= 0 || n <= 0) return QR_OK;
@@ -1230,7 +1239,7 @@ int zsvd_thin(cudaStream_t s, SvdWork* w, int mode, const double2* A, int m, int
     // a preconditioner: 1e-5 relative orthogonality is plenty for the FP64 refinement, and sits
     // above the FP32 rounding floor (~sqrt(m) eps32) so sweeps stop once rotations are noise
     float tol32 = fmaxf(4e-6f, 2.0f * sqrtf((float)rows) * Eps<float>::v);
-    QR_TRY(jacobi<float>(s, w, B32, rows, rows, k, V32, k, 20, tol32, false));
+    QR_TRY(jacobi<float>(s, w, B32, rows, rows, k, V32, k, 20, tol32, false, kPrecondTanStop));
     // X = V32 with columns sorted by the FP32 column norms (descending), as a double-float
     // matrix (low parts zero); the Newton-Schulz steps and B = A X run in double-float on the
     // FP32 pipes and B goes straight into the double-float polish
