@@ -877,7 +877,7 @@ __global__ void __launch_bounds__(NT, 2) jacobi_sweep_df_k(float2* __restrict__ 
                                                         int m, int n, float2* __restrict__ Vh, float2* __restrict__ Vl,
                                                         long ldv, int np, double tol, const double* __restrict__ smax_p,
                                                         unsigned* __restrict__ state, int sweep,
-                                                        unsigned* __restrict__ flags) {
+                                                        unsigned* __restrict__ flags, int k0) {
   if (((volatile unsigned*)state)[0]) return;
   const double smax = smax_p[0] / smax_p[1];
   unsigned* cnt = state + 8 + 2 * sweep;
@@ -893,7 +893,7 @@ __global__ void __launch_bounds__(NT, 2) jacobi_sweep_df_k(float2* __restrict__ 
     int p, q;
     pair_cols(np, round, pair, p, q);
     if (dataflow && !wait_cols(flags, p, q, n, base + round, state)) return;
-    if (q < n) jacobi_pair_df<NT, RPT>(Bh, Bl, ldb, m, n, Vh, Vl, ldv, p, q, tol, smax, cnt);
+    if (q < n && p < k0) jacobi_pair_df<NT, RPT>(Bh, Bl, ldb, m, n, Vh, Vl, ldv, p, q, tol, smax, cnt);
     if (dataflow) post_cols(flags, p, q, n, base + round + 1);
     else if (!grid_barrier(state + 2)) return;
   }
@@ -1117,8 +1117,11 @@ int jacobi(cudaStream_t s, SvdWork* w, cplx_t<T>* B, long ldb, int rows, int k, 
 // arrive as split (hi, lo) arrays with B's columns pre-scaled by a power of two; smax_d[0] /
 // smax_d[1] is sigma_max of the scaled columns.  Sweeps run with device-side convergence and one
 // host synchronisation at the end.
+// Pairs with both columns at index >= k0 are skipped (k0 = k: none): when the caller keeps only
+// the leading singular triplets and the columns arrive sorted by an approximate sigma, the tail
+// block needs no internal orthogonality (see zsvd_thin).
 int jacobi_df(cudaStream_t s, SvdWork* w, float2* Bh, float2* Bl, long ldb, int rows, int k, float2* Vh,
-              float2* Vl, long ldv, int max_sweeps, double tol, const double* smax_d) {
+              float2* Vl, long ldv, int max_sweeps, double tol, const double* smax_d, int k0) {
   constexpr int NT = 256, RPT = 8;
   const int np = k + (k & 1);
   const double pairs = 0.5 * (double)k * (k - 1);
@@ -1146,7 +1149,8 @@ int jacobi_df(cudaStream_t s, SvdWork* w, float2* Bh, float2* Bl, long ldb, int 
     const double* sm = smax_d;
     unsigned* st = state;
     unsigned* fl = flags;
-    void* args[] = {&a1, &a2, &l1, &mm, &kk, &a3, &a4, &l2, &npp, &tl, &sm, &st, &sw, &fl};
+    int kz = k0;
+    void* args[] = {&a1, &a2, &l1, &mm, &kk, &a3, &a4, &l2, &npp, &tl, &sm, &st, &sw, &fl, &kz};
     QR_CUDA(cudaLaunchCooperativeKernel((const void*)jacobi_sweep_df_k<NT, RPT>, dim3(grid), dim3(NT), args, 0, s));
     count_launch();
   }
@@ -1283,8 +1287,13 @@ int zsvd_thin(cudaStream_t s, SvdWork* w, int mode, const double2* A, int m, int
     // Hestenes sweeps on (B, X) in double-float finish the near-degenerate pairs the FP32 sweeps
     // leave and bring the couplings down to the double-float tolerance (inner products carry
     // ~sqrt(rows) 2^-48 relative noise; the tolerance sits 2x above that floor)
+    // When only the leading `keep` triplets are used (truncation to maxdim), pairs inside the
+    // trailing block need no rotation: the cross pairs still decouple that block from the leading
+    // columns, and every tail column's norm stays below the tail's largest sigma, so the final
+    // sort separates the two sets.  The margin covers FP32 misordering at the boundary.
+    const int k0 = keep > 0 && keep < k ? std::min(k, keep + std::max(32, keep / 8)) : k;
     QR_TRY(jacobi_df(s, w, Bh, Bl, rows, rows, k, Xh, Xl, k, 40, 32.0 * sqrt((double)rows) * Eps<double>::v,
-                     smax_d));
+                     smax_d, k0));
     QR_TRY(df2z(s, Bh, Bl, rows, rows, k, smax_d + 1, B, rows));
     QR_TRY(df2z(s, Xh, Xl, k, k, k, nullptr, V, k));
   }

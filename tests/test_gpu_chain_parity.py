@@ -234,6 +234,30 @@ def test_tebd_with_truncation(precision):
         assert abs(e - e_ref) <= tol * max(1.0, abs(e_ref))
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_truncated_gate_on_large_bond(precision):
+    """A gate on a chi = 128 bond (theta 256 x 256: the mixed path's FP32-preconditioned SVD with
+    double-float GEMMs and polish) truncated to maxdim = 100, so only the leading triplets are kept:
+    bond dimension, the kept Lambda spectrum and local expectations against the oracle."""
+    n, chi, maxdim = 16, 128, 100
+    arrays = R.rand_chain_state_arrays(R.rng(61), n, chi, p=2)
+    psi, ref = Q.MPS(arrays), O.from_reference_arrays(arrays)
+    psi.set_precision(precision)
+    u = R.haar_unitary(R.rng(62), 4)
+    Q.evolve_(psi, Q.gate_from_matrix(u, [8, 9]), threshold=1e-12, maxdim=maxdim)
+    O.evolve_2site_(ref, 7, u, threshold=1e-12, maxdim=maxdim)
+    assert psi.bond_dims() == ref.bond_dims()
+    assert psi.bond_dims()[7] == maxdim
+    lam, lam_ref = psi.lambda_between(8, 9), ref.lam[7]
+    assert _close(lam, lam_ref, 1e-10 if precision == "fp64" else 1e-9)
+    tol = RTOL if precision == "fp64" else 1e-8
+    for i in (7, 8, 9, 10):
+        z = Q.gate_from_matrix(R.PAULI["Z"], [i])
+        e = Q.expect(psi, [z])
+        e_ref = O.expect(ref, [O.ODense(R.PAULI["Z"], (O.OSite(i), O.OSite(i, True)))])
+        assert abs(e - e_ref) <= tol * max(1.0, abs(e_ref)), i
+
+
 def test_config1_pipeline():
     # plain workload: n=16, d=2, chi=32 Gaussian MPS; canonize!, norm, <Z_i Z_{i+1}> for all i
     psi, ref = _pair(16, 32, seed=1)
