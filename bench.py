@@ -130,6 +130,14 @@ class DevTimer:
         return self.e0.elapsed_time(self.e1) * 1e-3
 
 
+# DRAM bytes (read + write) per launch from one ncu capture of each kernel on a 1024 x 1024 mixed
+# SVD (profiles/jacobi_sweep_fp32_1024.md, jacobi_sweep_df_1024.md, zgemm_df_1024.md).  The
+# sweeps' traffic is the first touch of B and V and the GEMM's the first touch of its operands,
+# so it scales with the operand size: (k / 1024)^2 at k columns.
+NCU_TRAFFIC_1024 = {"jacobi_fp32": 16.821248e6 + 2.321920e6, "jacobi_df": 33.656064e6 + 7.758592e6,
+                    "zgemm_df": 16.850432e6}
+
+
 def workload(chi):
     from qrochet import random as R
 
@@ -460,7 +468,10 @@ def run_ours(args, chi):
     achieved = st["flops"] / (st["ms"] * 1e-3) / 1e12 if st["ms"] > 0 else 0.0
     shares = {k: round(v["ms"] / max(1e-9, sum(x["ms"] for x in stats.values())), 4) for k, v in stats.items()}
     roofline = {"bound": bound, "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak if peak else None, "traffic": None,
+                "frac": achieved / peak if peak else None,
+                "traffic": (NCU_TRAFFIC_1024[dom] * (2 * chi / 1024) ** 2 if dom in NCU_TRAFFIC_1024 else None),
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch at k = 1024, "
+                                  "scaled by (k / 1024)^2 to k = 2 chi",
                 "peak_source": ("measured cuBLAS bf16 (MEASURED_PEAKS.json)" if pk_kind == "bf16" else
                                 f"measured in-process ({pk_kind} loop kernel, best of 3)"),
                 "launches": st["launches"], "avg_launch_ms": st["ms"] / max(1, st["launches"]),
@@ -493,7 +504,7 @@ def run_ours(args, chi):
         line = {"metric": METRIC, "value": value, "unit": "gate-steps/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1e3 * dt_max / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None,
-                "dtype": "complex64 Jacobi preconditioner + double-float (FP32-pair) Jacobi polish + complex128 (FP64 DMMA) GEMMs; FP64 theta",
+                "dtype": "complex64 Jacobi preconditioner + double-float (FP32-pair) Newton-Schulz, B = A X and Jacobi polish; complex128 theta (FP64 DMMA)",
                 "data": "synthetic",
                 "config": {"workload": f"tebd_gate_step_chi{chi}", "chi": chi, "theta": f"{2 * chi}x{2 * chi}",
                            "maxdim": maxdim, "threshold": CUTOFF, "n_sites": N_SITES, "precision": "mixed",

@@ -52,8 +52,10 @@ typedef struct qr_mpo qr_mpo;     /* one open-boundary MPO resident in device me
 
 /* Precision of a chain's arithmetic (qr_chain_set_precision), a bit mask. */
 #define QR_FP64 0           /* plain: all ComplexF64 */
-#define QR_MIXED 1          /* SVD: FP32 Jacobi preconditioner + FP64 Newton-Schulz and Jacobi polish
-                               (singular values/vectors and the truncation cutoff stay FP64) */
+#define QR_MIXED 1          /* SVD with more than 128 columns: FP32 Jacobi preconditioner, then
+                               Newton-Schulz, B = A X and Jacobi polish in double-float (FP32 pairs,
+                               ~2^-48) on the FP32 pipes; theta, singular values and vectors and the
+                               truncation cutoff stay FP64.  Smaller SVDs run the FP64 Jacobi. */
 #define QR_SPLIT_CONTRACT 2 /* environment contractions (expect, overlap, norm, MPO expectation) on
                                the BF16 tensor cores with 3-way BF16 splits, FP32 accumulation */
 
