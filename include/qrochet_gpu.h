@@ -179,7 +179,8 @@ int qr_test_zgemm(int opA, int opB, int M, int N, int K, const double* alpha, co
 int qr_test_zgemm_split(int opA, int opB, int M, int N, int K, const double* A, long lda, const double* B,
                         long ldb, double* C, long ldc, int iters, double* ms_per_iter);
 /* Double-float GEMM on the FP32 pipes.  mode 0: C = op(A) B; 1: C = I - op(A) B; 2: C = D + 0.5
-   op(A) B with FP32 products (A, B rounded to FP32).  op(A) in {0 N, 1 T, 2 C}; D used by mode 2. */
+   op(A) B with FP32 products (A, B rounded to FP32); 3: C = I - A^H A from the upper tiles (op C,
+   B ignored).  op(A) in {0 N, 1 T, 2 C}; D used by mode 2. */
 int qr_test_zgemm_df(int mode, int opA, int M, int N, int K, const double* A, long lda, const double* B, long ldb,
                      const double* D, double* C, long ldc, int iters, double* ms_per_iter);
 int qr_test_svd(int mode, int m, int n, const double* A, double* U, double* S, double* Vh, double* ms);

@@ -12,6 +12,9 @@
 //   DF_I_MINUS C = I - op(A) B                   (FP32 complex result in Ch; used for I - X^H X)
 //   F32_AXPY   C = D + alpha op(A_hi) B_hi       (FP32 products and accumulation, double-float
 //                                                 addition to D; used for X + X R / 2, |R| << 1)
+//   DF_GRAM    C = I - A^H A                     (as DF_I_MINUS for the Hermitian Gram matrix:
+//                                                 only tiles on or above the diagonal are
+//                                                 computed, each off-diagonal tile is stored twice)
 // Tiling: a CTA of 256 threads owns a 64 x 64 block of C, each thread a 4 x 4 sub-block (rows
 // tx + 16 i, columns ty + 16 j); K advances in steps of 16 through double-buffered shared
 // memory filled by cp.async (8-byte copies, zero-filled outside the matrix).
@@ -81,7 +84,15 @@ __global__ void __launch_bounds__(DNT, 2)
   extern __shared__ __align__(16) unsigned char smraw[];
   DfSmem& sm = *reinterpret_cast<DfSmem*>(smraw);
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  const int m0 = blockIdx.x * DBM, n0 = blockIdx.y * DBN;
+  int bx = blockIdx.x, by = blockIdx.y;
+  if (MODE == DF_GRAM) {  // linear index over the tiles with bx <= by
+    const int t = blockIdx.x;
+    by = (int)((sqrtf(8.f * t + 1.f) - 1.f) * 0.5f);
+    while (by * (by + 1) / 2 > t) by--;
+    while ((by + 1) * (by + 2) / 2 <= t) by++;
+    bx = t - by * (by + 1) / 2;
+  }
+  const int m0 = bx * DBM, n0 = by * DBN;
   DotAcc re[4][4], im[4][4];
 #pragma unroll
   for (int i = 0; i < 4; i++)
@@ -160,10 +171,11 @@ __global__ void __launch_bounds__(DNT, 2)
         const dfl r = dot_final(re[i][j]), m = dot_final(im[i][j]);
         Ch[o] = make_float2(r.h, m.h);
         Cl[o] = make_float2(r.l, m.l);
-      } else if (MODE == DF_I_MINUS) {
+      } else if (MODE == DF_I_MINUS || MODE == DF_GRAM) {
         const dfl r = df_add({row == col ? 1.f : 0.f, 0.f}, df_neg(dot_final(re[i][j])));
         const dfl m = df_neg(dot_final(im[i][j]));
         Ch[o] = make_float2(r.h + r.l, m.h + m.l);
+        if (MODE == DF_GRAM && bx != by) Ch[(long)col + (long)row * ldc] = make_float2(r.h + r.l, -(m.h + m.l));
       } else {
         const long od = (long)row + (long)col * ldd;
         const float2 dh = Dh[od], dl = Dl[od];
@@ -187,6 +199,10 @@ int launch_df(cudaStream_t s, int M, int N, int K, const float2* Ah, const float
     attr = true;
   }
   dim3 grid((M + DBM - 1) / DBM, (N + DBN - 1) / DBN);
+  if (MODE == DF_GRAM) {
+    const int tiles = (M + DBM - 1) / DBM;
+    grid = dim3(tiles * (tiles + 1) / 2, 1);
+  }
   zgemm_df_k<OPA, MODE><<<grid, DNT, bytes, s>>>(M, N, K, Ah, Al, lda, Bh, Bl, ldb, Ch, Cl, ldc, Dh, Dl, ldd,
                                                  alpha);
   QR_CHECK_LAUNCH("zgemm_df_k");
@@ -233,7 +249,9 @@ int zgemm_df(cudaStream_t s, int mode, int opA, int M, int N, int K, const float
   if (opA != OP_N && opA != OP_C && opA != OP_T) return fail(QR_EINVAL, "zgemm_df: op(A) must be N, T or C");
   if (mode == DF_F32_AXPY && (!Dh || !Dl)) return fail(QR_EINVAL, "zgemm_df: AXPY mode needs D");
   if (mode != DF_F32_AXPY && !Al) return fail(QR_EINVAL, "zgemm_df: double-float mode needs low parts");
-  int pr = prof_begin(s, PK_ZGEMM_DF, 8.0 * M * N * K,
+  if (mode == DF_GRAM && (opA != OP_C || M != N || Ah != Bh || Al != Bl))
+    return fail(QR_EINVAL, "zgemm_df: the Gram mode computes I - A^H A (op C, B = A)");
+  int pr = prof_begin(s, PK_ZGEMM_DF, (mode == DF_GRAM ? 4.0 : 8.0) * M * N * K,
                       (mode == DF_F32_AXPY ? 8.0 : 16.0) * ((double)M * K + (double)K * N) + 16.0 * M * N);
   int rc = QR_OK;
 #define QR_DF_CASE(OPV, MV)                                                                                   \
@@ -248,6 +266,7 @@ int zgemm_df(cudaStream_t s, int mode, int opA, int M, int N, int K, const float
   QR_DF_CASE(OP_N, DF_F32_AXPY)
   QR_DF_CASE(OP_C, DF_F32_AXPY)
   QR_DF_CASE(OP_T, DF_F32_AXPY)
+  QR_DF_CASE(OP_C, DF_GRAM)
 #undef QR_DF_CASE
   prof_end(s, pr);
   return rc;

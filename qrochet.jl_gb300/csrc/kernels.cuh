@@ -16,9 +16,10 @@ int zgemm_split(cudaStream_t s, int opA, int opB, int M, int N, int K, const dou
                 const double2* B, long ldb, long sB, double2* C, long ldc, long sC, int batch);
 
 // ---- gemm_df.cu: complex GEMM in double-float (hi, lo FP32 pairs) on the FP32 pipes
-enum { DF_STORE = 0, DF_I_MINUS = 1, DF_F32_AXPY = 2 };
+enum { DF_STORE = 0, DF_I_MINUS = 1, DF_F32_AXPY = 2, DF_GRAM = 3 };
 // DF_STORE: (Ch, Cl) = op(A) B; DF_I_MINUS: Ch = I - op(A) B (FP32); DF_F32_AXPY: (Ch, Cl) = D +
-// alpha op(A_hi) B_hi with FP32 products.  op(A) in {N, T, C}; B is not transformed.
+// alpha op(A_hi) B_hi with FP32 products; DF_GRAM: Ch = I - A^H A from the tiles on or above the
+// diagonal (op C, B = A).  op(A) in {N, T, C}; B is not transformed.
 int zgemm_df(cudaStream_t s, int mode, int opA, int M, int N, int K, const float2* Ah, const float2* Al, long lda,
              const float2* Bh, const float2* Bl, long ldb, float2* Ch, float2* Cl, long ldc,
              const float2* Dh = nullptr, const float2* Dl = nullptr, long ldd = 0, float alpha = 1.f);

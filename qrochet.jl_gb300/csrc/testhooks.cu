@@ -100,7 +100,7 @@ int qr_test_zgemm_split(int opA, int opB, int M, int N, int K, const double* A, 
 // pairs on the device, the result converted back (mode 1 returns the FP32 value I - op(A) B).
 int qr_test_zgemm_df(int mode, int opA, int M, int N, int K, const double* A, long lda, const double* B, long ldb,
                      const double* D, double* C, long ldc, int iters, double* ms_per_iter) {
-  if (M <= 0 || N <= 0 || K < 0 || iters < 1 || mode < 0 || mode > 2) return fail(QR_EINVAL, "bad gemm_df shape");
+  if (M <= 0 || N <= 0 || K < 0 || iters < 1 || mode < 0 || mode > 3) return fail(QR_EINVAL, "bad gemm_df shape");
   if (opA != OP_N && opA != OP_T && opA != OP_C) return fail(QR_EINVAL, "op(A) must be N, T or C");
   const long ca = opA == OP_N ? K : M, rb = K;
   if (lda < (opA == OP_N ? M : K) || ldb < rb || ldc < M) return fail(QR_EINVAL, "bad leading dimension");
@@ -129,8 +129,9 @@ int qr_test_zgemm_df(int mode, int opA, int M, int N, int K, const double* A, lo
   cudaEventRecord(e0);
   int rc = QR_OK;
   for (int it = 0; it < iters && rc == QR_OK; it++)
-    rc = zgemm_df(0, mode, opA, M, N, K, Ah, mode == 2 ? nullptr : Al, lda, Bh, mode == 2 ? nullptr : Bl, ldb, Ch,
-                  Cl, ldc, Dh, Dl, ldc, 0.5f);
+    rc = mode == 3 ? zgemm_df(0, mode, opA, M, N, K, Ah, Al, lda, Ah, Al, lda, Ch, Cl, ldc)
+                   : zgemm_df(0, mode, opA, M, N, K, Ah, mode == 2 ? nullptr : Al, lda, Bh, mode == 2 ? nullptr : Bl, ldb,
+                              Ch, Cl, ldc, Dh, Dl, ldc, 0.5f);
   cudaEventRecord(e1);
   cudaEventSynchronize(e1);
   float t = 0;
@@ -139,7 +140,7 @@ int qr_test_zgemm_df(int mode, int opA, int M, int N, int K, const double* A, lo
   cudaEventDestroy(e1);
   QR_TRY(rc);
   if (ms_per_iter) *ms_per_iter = t / iters;
-  if (mode == 1) {
+  if (mode == 1 || mode == 3) {
     std::vector<float2> h(nc);
     QR_CUDA(cudaMemcpy(h.data(), Ch, sizeof(float2) * nc, cudaMemcpyDeviceToHost));
     for (size_t i = 0; i < nc; i++) { C[2 * i] = h[i].x; C[2 * i + 1] = h[i].y; }

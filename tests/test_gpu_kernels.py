@@ -229,3 +229,19 @@ def test_zgemm_df_axpy_fp32_products():
     ref = D + 0.5 * A @ Bm
     # FP32 products of FP32-rounded inputs: ~1e-7 relative to the correction term, double-float D
     assert np.max(np.abs(got - ref)) <= 1e-6 * 0.5 * (np.abs(A) @ np.abs(Bm)).max() + DF_TOL * np.abs(D).max()
+
+
+@pytest.mark.parametrize("k", [160, 200])
+def test_zgemm_df_gram_half(k):
+    """I - X^H X from the tiles on or above the diagonal (mirrored): equal to the full product."""
+    g = R.rng(414 + k)
+    q, _ = np.linalg.qr(R.complex_gaussian(g, (k, k)))
+    X = q + 1e-6 * R.complex_gaussian(g, (k, k))
+    half = zgemm_df(3, 2, X, X, k, k)
+    full = zgemm_df(1, 2, X, X, k, k)
+    ref = np.eye(k) - X.conj().T @ X
+    assert np.max(np.abs(half - ref)) <= 1e-13 + 1e-7 * np.max(np.abs(ref))
+    # R is stored in FP32: mirrored and directly computed entries differ by ~1 ulp of |R|
+    ulp = 2.0 ** -23 * np.max(np.abs(ref))
+    assert np.max(np.abs(half - full)) <= 2 * ulp
+    assert np.max(np.abs(half - half.conj().T)) <= 2 * ulp
