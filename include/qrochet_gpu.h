@@ -98,6 +98,12 @@ int qr_chain_set_lambda(qr_chain* h, int bond, const double* lam, int len);
 int qr_chain_ntensors(const qr_chain* h, int* out);
 int qr_chain_nsites(const qr_chain* h, int* out);
 int qr_chain_set_precision(qr_chain* h, int mode);
+/* Checkpoint / export (SURVEY next row: round trip with Julia).  The file holds the site arrays
+   in the reference's (:o, :l, :r) column-major layout (open ends without l / r), the bond
+   dimensions, the Lambda vectors and the precision; little-endian, layout documented in
+   INTEGRATION.md.  No reference counterpart beyond MPS(arrays) on the Julia side. */
+int qr_chain_save(const qr_chain* h, const char* path);
+int qr_chain_load(const char* path, qr_chain** out);
 int qr_chain_get_precision(const qr_chain* h, int* mode);
 /* the cudaStream_t this chain's work is ordered on (for caller-side CUDA events) */
 int qr_chain_stream(const qr_chain* h, void** stream);
@@ -136,6 +142,14 @@ int qr_mpo_create(int n, int d, const int* bond_dims /* n-1 */, qr_mpo** out);
 int qr_mpo_free(qr_mpo* w);
 int qr_mpo_upload_site(qr_mpo* w, int site, const double* host, const char* order);
 int qr_mpo_expect(const qr_chain* h, const qr_mpo* w, double* out);
+int qr_mpo_download_site(const qr_mpo* w, int site, double* host, const char* order);
+/* rand(Chain, Open, State; n, p = d, chi, eltype) and rand(Chain, Open, Operator; ...)
+   (src/Ansatz/Chain.jl:223-297) generated on the device: the reference's bond-dimension pattern,
+   uniform [0,1) entries (complex when complex_entries) with Gram-Schmidt orthonormalised rows,
+   the first site normalised.  Entries come from a counter-based generator (Philox-4x32-10) keyed
+   by seed, not from Julia's RNG. */
+int qr_chain_random(int n, int d, int chi, uint64_t seed, int complex_entries, qr_chain** out);
+int qr_mpo_random(int n, int d, int chi, uint64_t seed, int complex_entries, qr_mpo** out);
 
 /* ---- request server: continuous batching of simulate-and-measure requests (no reference
    counterpart; the reference has no serving layer).  A request is a circuit of two-site gates on

@@ -9,10 +9,13 @@
 // in their own device buffers, one per bond that holds one (the reference keeps them as
 // separate hyperindex tensors on the bond, src/Ansatz/Chain.jl:338).
 #include <vector>
+#include <cstdio>
 #include <string>
 #include <complex>
 #include <cstring>
 #include <cmath>
+#include <cstdlib>
+#include <algorithm>
 #include <mutex>
 #include "kernels.cuh"
 
@@ -618,6 +621,226 @@ int qr_chain_download_site(const qr_chain* hc, int site, double* host, const cha
   return QR_OK;
 }
 
+// ---- rand(Chain, Open, State / Operator) on the device ---------------------------------------
+// Bond dimensions follow the reference's sampler (src/Ansatz/Chain.jl:223-297): site i (1-based)
+// draws a (chi_l x chi_r p) random matrix with chi_l = min(chi, p^(m-1)), chi_r = min(chi, p^m),
+// m = (n + 1 - |2i - n - 1|) / 2, the two swapped after the middle and equal at the middle site of
+// an odd chain; the State's first site uses (chi_r, 1) (its rows become the right bond).  Rows are
+// Gram-Schmidt orthonormalised (random.cu), the first site is divided by sqrt(p) for the State and
+// by sqrt(min(chi, p^2)) for the Operator.
+namespace {
+long ipow_cap(long p, int e, long cap) {
+  long v = 1;
+  for (int k = 0; k < e && v < cap; k++) v *= p;
+  return v < cap ? v : cap;
+}
+void sampler_dims(int n, long p, long chi, int i, long& l, long& r) {
+  const bool after_mid = i > n / 2;
+  const int m = (n + 1 - std::abs(2 * i - n - 1)) / 2;
+  l = ipow_cap(p, m - 1, chi);
+  r = ipow_cap(p, m, chi);
+  if ((n % 2 == 1) && i == n / 2 + 1) r = l;
+  else if (after_mid) std::swap(l, r);
+}
+}  // namespace
+
+int qr_chain_random(int n, int d, int chi, uint64_t seed, int complex_entries, qr_chain** out) {
+  if (!out) return fail(QR_EINVAL, "null output");
+  *out = nullptr;
+  if (n < 2 || d < 2 || chi < d) return fail(QR_EINVAL, "rand(Chain, Open, State) needs n >= 2, p >= 2 and chi >= p");
+  std::vector<long> L(n), Rr(n);
+  for (int i = 1; i <= n; i++) sampler_dims(n, d, chi, i, L[i - 1], Rr[i - 1]);
+  // site 1 samples (chi_r, 1) and its rows become the right bond; the last site has chi_r = 1
+  std::vector<int> bd(n - 1);
+  bd[0] = (int)Rr[0];
+  for (int b = 1; b < n - 1; b++) bd[b] = (int)Rr[b];
+  for (int b = 0; b < n - 1; b++)
+    if (bd[b] != (int)L[b + 1]) return fail(QR_EDIM, "sampler bond dimensions do not chain");
+  qr_chain* h = nullptr;
+  QR_TRY(qr_chain_create(n, d, bd.data(), &h));
+  int rc = QR_OK;
+  double2* E = nullptr;
+  for (int i = 0; i < n && !rc; i++) {
+    // rows x N random isometry; device site (cl, d, cr), l fastest
+    const long rows = i == 0 ? Rr[0] : L[i];
+    const long rdim = (i == 0 || i == n - 1) ? 1 : Rr[i];
+    const long N = rdim * d;
+    const double scale = i == 0 ? 1.0 / std::sqrt((double)d) : 1.0;
+    rc = cuda_ok(cudaMallocAsync(&E, sizeof(double2) * rows * N, h->stream), "cudaMallocAsync");
+    if (!rc) rc = rand_rows_isometry(h->stream, (int)rows, (int)N, seed, (uint32_t)i, complex_entries, scale, E);
+    if (!rc) {
+      // E[row, r + rdim * o] -> site[l, o, r]; on site 1 the row index is the right bond
+      Perm p;
+      p.nd = 3;
+      p.dims[0] = h->cl(i);
+      p.dims[1] = d;
+      p.dims[2] = h->cr(i);
+      if (i == 0) {
+        p.src_stride[0] = 0;
+        p.src_stride[1] = rows;
+        p.src_stride[2] = 1;
+      } else {
+        p.src_stride[0] = 1;
+        p.src_stride[1] = rows * rdim;
+        p.src_stride[2] = rows;
+      }
+      rc = zpermute(h->stream, E, h->site[i], p);
+    }
+    if (E) cudaFreeAsync(E, h->stream);
+    E = nullptr;
+  }
+  if (!rc) rc = cuda_ok(cudaStreamSynchronize(h->stream), "cudaStreamSynchronize");
+  if (rc) {
+    qr_chain_free(h);
+    return rc;
+  }
+  *out = h;
+  return QR_OK;
+}
+
+int qr_mpo_random(int n, int d, int chi, uint64_t seed, int complex_entries, qr_mpo** out) {
+  if (!out) return fail(QR_EINVAL, "null output");
+  *out = nullptr;
+  if (n < 2 || d < 2 || chi < 1) return fail(QR_EINVAL, "rand(Chain, Open, Operator) needs n >= 2, p >= 2 and chi >= 1");
+  const long p2 = (long)d * d;
+  std::vector<long> L(n), Rr(n);
+  for (int i = 1; i <= n; i++) sampler_dims(n, p2, chi, i, L[i - 1], Rr[i - 1]);
+  std::vector<int> bd(n - 1);
+  for (int b = 0; b < n - 1; b++) bd[b] = (int)Rr[b];
+  for (int b = 0; b < n - 1; b++)
+    if (bd[b] != (int)L[b + 1]) return fail(QR_EDIM, "sampler bond dimensions do not chain");
+  qr_mpo* w = nullptr;
+  QR_TRY(qr_mpo_create(n, d, bd.data(), &w));
+  int rc = QR_OK;
+  double2* E = nullptr;
+  for (int i = 0; i < n && !rc; i++) {
+    // shapes (chi_r, ip, op) at site 1, (chi_l, chi_r, ip, op) inside, (chi_l, ip, op) at site n;
+    // the rows are the first dimension, columns the rest (column-major)
+    const long rows = i == 0 ? Rr[0] : L[i];
+    const long rdim = (i == 0 || i == n - 1) ? 1 : Rr[i];
+    const long N = rdim * p2;
+    const double scale = i == 0 ? 1.0 / std::sqrt((double)std::min<long>(chi, p2)) : 1.0;
+    rc = cuda_ok(cudaMalloc(&E, sizeof(double2) * rows * N), "cudaMalloc");
+    if (!rc) rc = rand_rows_isometry(0, (int)rows, (int)N, seed, (uint32_t)(0x4000u + i), complex_entries, scale, E);
+    if (!rc) {
+      // E[row, r + rdim (o + d i)] -> W[wl, o, i, wr] (the permuted sampler array read as
+      // (o, i, l, r)); on site 1 the row index is the right bond
+      Perm p;
+      p.nd = 4;
+      p.dims[0] = w->wl(i);
+      p.dims[1] = d;
+      p.dims[2] = d;
+      p.dims[3] = w->wr(i);
+      if (i == 0) {
+        p.src_stride[0] = 0;
+        p.src_stride[1] = rows;
+        p.src_stride[2] = rows * d;
+        p.src_stride[3] = 1;
+      } else {
+        p.src_stride[0] = 1;
+        p.src_stride[1] = rows * rdim;
+        p.src_stride[2] = rows * rdim * d;
+        p.src_stride[3] = rows;
+      }
+      rc = zpermute(0, E, w->site[i], p);
+    }
+    if (E) cudaFree(E);
+    E = nullptr;
+  }
+  if (!rc) rc = cuda_ok(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
+  if (rc) {
+    qr_mpo_free(w);
+    return rc;
+  }
+  *out = w;
+  return QR_OK;
+}
+
+// ---- checkpoint / export ---------------------------------------------------------------------
+// File layout (little-endian), written so a Julia reader can rebuild MPS(arrays) directly:
+//   "QRCHAIN1" | int32 n, d, precision, 0 | int32 bond_dims[n-1] | uint8 has_lambda[n-1]
+//   | site 0 .. n-1: ComplexF64 data in the reference's (o, l, r) column-major order, the open ends
+//     without l (site 1) and r (site n) | for every bond with has_lambda: Float64 Lambda[bond_dim]
+namespace {
+const char kChainMagic[8] = {'Q', 'R', 'C', 'H', 'A', 'I', 'N', '1'};
+struct FileCloser {
+  FILE* f;
+  ~FileCloser() {
+    if (f) fclose(f);
+  }
+};
+}  // namespace
+
+int qr_chain_save(const qr_chain* h, const char* path) {
+  if (!h || !path) return fail(QR_EINVAL, "null argument");
+  FileCloser fc{fopen(path, "wb")};
+  if (!fc.f) return fail(QR_EINVAL, std::string("cannot open for writing: ") + path);
+  const int32_t hdr[4] = {h->n, h->d, h->precision, 0};
+  bool ok = fwrite(kChainMagic, 1, 8, fc.f) == 8 && fwrite(hdr, sizeof(int32_t), 4, fc.f) == 4;
+  std::vector<int32_t> bd(h->bd.begin(), h->bd.end());
+  std::vector<uint8_t> fl(h->n - 1);
+  for (int b = 0; b < h->n - 1; b++) fl[b] = h->lam[b] != nullptr;
+  ok = ok && fwrite(bd.data(), sizeof(int32_t), bd.size(), fc.f) == bd.size();
+  ok = ok && fwrite(fl.data(), 1, fl.size(), fc.f) == fl.size();
+  std::vector<double> buf;
+  for (int i = 0; i < h->n && ok; i++) {
+    buf.resize(2 * h->elems(i));
+    QR_TRY(qr_chain_download_site(h, i, buf.data(), "olr"));
+    ok = fwrite(buf.data(), sizeof(double), buf.size(), fc.f) == buf.size();
+  }
+  for (int b = 0; b < h->n - 1 && ok; b++) {
+    if (!fl[b]) continue;
+    buf.resize(h->bd[b]);
+    int len = 0;
+    QR_TRY(qr_chain_get_lambda(h, b, buf.data(), &len));
+    ok = fwrite(buf.data(), sizeof(double), (size_t)len, fc.f) == (size_t)len;
+  }
+  if (!ok) return fail(QR_EINVAL, std::string("write failed: ") + path);
+  return QR_OK;
+}
+
+int qr_chain_load(const char* path, qr_chain** out) {
+  if (!path || !out) return fail(QR_EINVAL, "null argument");
+  *out = nullptr;
+  FileCloser fc{fopen(path, "rb")};
+  if (!fc.f) return fail(QR_EINVAL, std::string("cannot open: ") + path);
+  char magic[8];
+  int32_t hdr[4];
+  if (fread(magic, 1, 8, fc.f) != 8 || memcmp(magic, kChainMagic, 8) != 0 ||
+      fread(hdr, sizeof(int32_t), 4, fc.f) != 4)
+    return fail(QR_EINVAL, "not a chain checkpoint");
+  const int n = hdr[0], d = hdr[1], prec = hdr[2];
+  if (n < 2 || n > (1 << 20) || d < 1 || d > 64) return fail(QR_EINVAL, "corrupt chain checkpoint header");
+  std::vector<int32_t> bd(n - 1);
+  std::vector<uint8_t> fl(n - 1);
+  if (fread(bd.data(), sizeof(int32_t), bd.size(), fc.f) != bd.size() || fread(fl.data(), 1, fl.size(), fc.f) != fl.size())
+    return fail(QR_EINVAL, "truncated chain checkpoint");
+  for (int32_t b : bd)
+    if (b < 1) return fail(QR_EINVAL, "corrupt chain checkpoint bond dimensions");
+  std::vector<int> bdi(bd.begin(), bd.end());
+  qr_chain* h = nullptr;
+  QR_TRY(qr_chain_create(n, d, bdi.data(), &h));
+  int rc = qr_chain_set_precision(h, prec);
+  std::vector<double> buf;
+  for (int i = 0; i < n && !rc; i++) {
+    buf.resize(2 * h->elems(i));
+    if (fread(buf.data(), sizeof(double), buf.size(), fc.f) != buf.size()) rc = fail(QR_EINVAL, "truncated chain checkpoint");
+    else rc = qr_chain_upload_site(h, i, buf.data(), "olr");
+  }
+  for (int b = 0; b < n - 1 && !rc; b++) {
+    if (!fl[b]) continue;
+    buf.resize(bd[b]);
+    if (fread(buf.data(), sizeof(double), buf.size(), fc.f) != buf.size()) rc = fail(QR_EINVAL, "truncated chain checkpoint");
+    else rc = qr_chain_set_lambda(h, b, buf.data(), bd[b]);
+  }
+  if (rc) {
+    qr_chain_free(h);
+    return rc;
+  }
+  *out = h;
+  return QR_OK;
+}
+
 int qr_chain_site_dims(const qr_chain* h, int site, int* chi_l, int* d, int* chi_r) {
   QR_TRY(check_site(h, site));
   if (chi_l) *chi_l = h->cl(site);
@@ -951,6 +1174,33 @@ int qr_mpo_upload_site(qr_mpo* w, int site, const double* host, const char* orde
   cudaError_t e = cudaMemcpy(tmp, host, sizeof(double2) * ne, cudaMemcpyHostToDevice);
   int rc = (e == cudaSuccess) ? zpermute(0, tmp, w->site[site], p) : cuda_fail(e, "cudaMemcpy");
   cudaDeviceSynchronize();
+  cudaFree(tmp);
+  return rc;
+}
+
+int qr_mpo_download_site(const qr_mpo* w, int site, double* host, const char* order) {
+  if (!w || site < 0 || site >= w->n || !host) return fail(QR_EINVAL, "bad MPO site");
+  if (!is_perm(order ? order : "", "oilr")) return fail(QR_EINVAL, "order must be a permutation of (o, i, l, r)");
+  std::string ho = filtered(order, site == 0, site == w->n - 1);
+  // host order gathers from the internal (l, o, i, r) layout
+  long dims_by_letter[4] = {w->wl(site), w->d, w->d, w->wr(site)};  // l, o, i, r
+  const std::string iord = "loir";
+  long istride[4] = {1, dims_by_letter[0], dims_by_letter[0] * w->d, dims_by_letter[0] * w->d * w->d};
+  Perm p;
+  p.nd = (int)ho.size();
+  for (int k = 0; k < p.nd; k++) {
+    size_t q = iord.find(ho[k]);
+    p.dims[k] = dims_by_letter[q];
+    p.src_stride[k] = istride[q];
+  }
+  const size_t ne = (size_t)dims_by_letter[0] * w->d * w->d * dims_by_letter[3];
+  double2* tmp = nullptr;
+  QR_CUDA(cudaMalloc(&tmp, sizeof(double2) * ne));
+  int rc = zpermute(0, w->site[site], tmp, p);
+  if (!rc) {
+    cudaError_t e = cudaMemcpy(host, tmp, sizeof(double2) * ne, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) rc = cuda_fail(e, "cudaMemcpy");
+  }
   cudaFree(tmp);
   return rc;
 }

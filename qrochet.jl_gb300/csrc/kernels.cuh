@@ -30,6 +30,11 @@ int z2df(cudaStream_t s, const double2* src, long lds, int rows, int cols, const
 int df2z(cudaStream_t s, const float2* hi, const float2* lo, long lds, int rows, int cols, const double* scale,
          double2* dst, long ldd);
 
+// ---- random.cu: E (rows x N, ld rows) = scale * the Gram-Schmidt orthonormalised rows of a
+// uniform [0,1) random rows x N matrix (complex entries when cplx), from stream `stream` of `seed`
+int rand_rows_isometry(cudaStream_t s, int rows, int N, uint64_t seed, uint32_t stream, int cplx, double scale,
+                       double2* E);
+
 // ---- misc.cu -----------------------------------------------------------------------------------
 int zscale_matrix(cudaStream_t s, int M, int N, double2 alpha, double2* C, long ldc, long sC,
                   int batch);

@@ -9,9 +9,11 @@ from .chain import (MPO, MPS, Chain, Open, Periodic, canonicality_error, canoniz
                     canonize_site, canonize_site_, contract_between, contract_between_, device_count,
                     evolve_, expect, isleftcanonical, isrightcanonical, mixed_canonize, mixed_canonize_,
                     mpo_expect, norm, normalize_, overlap, truncate, truncate_, zeros_chain,
-                    PinnedArray, probe_peak, prof_enable, prof_read, set_device, PROF_KINDS)
+                    PinnedArray, probe_peak, prof_enable, prof_read, set_device, PROF_KINDS, rand,
+                    sampler_bond_dims)
 from .dense import Dense, Operator, State, gate_from_matrix, validate_gate
 from .site import Site, nextindex, site
+from . import checkpoint
 
 __all__ = [
     "ArgumentError", "DimensionMismatch", "GPUError", "MissingSchmidtCoefficientsException",
@@ -21,5 +23,5 @@ __all__ = [
     "mixed_canonize_", "mpo_expect", "norm", "normalize_", "overlap", "truncate", "truncate_",
     "zeros_chain", "Dense", "Operator", "State", "gate_from_matrix", "validate_gate", "Site",
     "nextindex", "site", "PinnedArray", "probe_peak", "prof_enable", "prof_read", "set_device",
-    "PROF_KINDS",
+    "PROF_KINDS", "checkpoint", "rand", "sampler_bond_dims",
 ]

@@ -69,6 +69,11 @@ SIGNATURES = {
     "qr_chain_ntensors": [_P, _PI],
     "qr_chain_nsites": [_P, _PI],
     "qr_chain_set_precision": [_P, _I],
+    "qr_chain_save": [_P, _S],
+    "qr_chain_random": [_I, _I, _I, C.c_uint64, _I, C.POINTER(_P)],
+    "qr_mpo_random": [_I, _I, _I, C.c_uint64, _I, C.POINTER(_P)],
+    "qr_mpo_download_site": [_P, _I, _PD, _S],
+    "qr_chain_load": [_S, C.POINTER(_P)],
     "qr_chain_get_precision": [_P, _PI],
     "qr_chain_stream": [_P, C.POINTER(_P)],
     "qr_chain_sync": [_P],

@@ -108,6 +108,22 @@ class Chain:
         check(lib().qr_chain_copy(self._h, C.byref(h)))
         return Chain(h, self.n, self.d, list(self._phys), list(self._bonds))
 
+    def save(self, path):
+        """Checkpoint: the sites in the reference's ``(:o, :l, :r)`` layout, bond dimensions,
+        Lambda vectors and precision (``qr_chain_save``; layout in ``qrochet.checkpoint``)."""
+        check(lib().qr_chain_save(self._h, str(path).encode()))
+
+    @classmethod
+    def load(cls, path):
+        """Restore a checkpoint written by ``save`` (or by any writer of the same layout)."""
+        h = C.c_void_p()
+        check(lib().qr_chain_load(str(path).encode(), C.byref(h)))
+        n = C.c_int()
+        check(lib().qr_chain_nsites(h, C.byref(n)))
+        a, d, b = C.c_int(), C.c_int(), C.c_int()
+        check(lib().qr_chain_site_dims(h, 0, C.byref(a), C.byref(d), C.byref(b)))
+        return cls(h, n.value, d.value)
+
     __copy__ = copy
     __deepcopy__ = lambda self, memo: self.copy()  # noqa: E731
 
@@ -285,9 +301,36 @@ class MPO:
         check(lib().qr_mpo_create(n, d, (C.c_int * (n - 1))(*bond), C.byref(h)))
         self._h = h
         self.n, self.d = n, d
+        self._bonds = list(bond)
         for i, a in enumerate(arrays):
             buf = np.asfortranarray(a, dtype=np.complex128)
             check(lib().qr_mpo_upload_site(h, i, dptr(buf), "".join(order).encode()))
+
+    @classmethod
+    def _from_handle(cls, h, n, d):
+        w = cls.__new__(cls)
+        w._h, w.n, w.d = h, n, d
+        return w
+
+    def site_array(self, i, order=("o", "i", "l", "r")):
+        """Site ``i`` (0-based) in the reference layout (ends without ``:l`` / ``:r``)."""
+        order = _norm_order(order, "oilr")
+        shp = self._shape(i)
+        sub = [x for x in order if not ((i == 0 and x == "l") or (i == self.n - 1 and x == "r"))]
+        out = np.empty(tuple(shp[x] for x in sub), dtype=np.complex128, order="F")
+        check(lib().qr_mpo_download_site(self._h, i, dptr(out), "".join(order).encode()))
+        return out
+
+    def arrays(self, order=("o", "i", "l", "r")):
+        return [self.site_array(i, order) for i in range(self.n)]
+
+    def _shape(self, i):
+        if not hasattr(self, "_bonds"):
+            # bond sizes from the sites' element counts would need the C ABI; the sampler and the
+            # array constructor record them
+            raise ArgumentError("MPO bond sizes unknown")
+        b = self._bonds
+        return {"o": self.d, "i": self.d, "l": 1 if i == 0 else b[i - 1], "r": 1 if i == self.n - 1 else b[i]}
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -297,6 +340,45 @@ class MPO:
             except Exception:
                 pass
             self._h = None
+
+
+def sampler_bond_dims(n, chi, p=2, socket=State):
+    """Bond dimensions of ``rand(Chain, Open, socket; n, p, χ)`` (Chain.jl:223-297)."""
+    q = p if socket is State else p * p
+    L_, R_ = [], []
+    for i in range(1, n + 1):
+        after_mid = i > n // 2
+        m = (n + 1 - abs(2 * i - n - 1)) // 2
+        l, r = min(chi, q ** (m - 1)), min(chi, q ** m)
+        if n % 2 == 1 and i == n // 2 + 1:
+            r = l
+        elif after_mid:
+            l, r = r, l
+        L_.append(l)
+        R_.append(r)
+    return R_[: n - 1]
+
+
+def rand(A, B, S, *, n, chi, p=2, eltype=np.float64, seed=0):
+    """``rand(Chain, Open, State; n, p, χ, eltype)`` / ``rand(Chain, Open, Operator; ...)``
+    (Chain.jl:223-297), generated on the device: the reference's bond pattern, uniform [0,1)
+    entries with Gram-Schmidt orthonormalised rows, the first site normalised.  The stream of
+    random numbers is the library's own (Philox-4x32-10 keyed by ``seed``), not Julia's."""
+    if A is not Chain:
+        raise ArgumentError("rand(A, B, S) builds a Chain")
+    if B is not Open:
+        raise ArgumentError("only Open chains have a sampler (as in the reference)")
+    cplx = int(np.issubdtype(np.dtype(eltype), np.complexfloating))
+    h = C.c_void_p()
+    if S is State:
+        check(lib().qr_chain_random(int(n), int(p), int(chi), int(seed) & (2 ** 64 - 1), cplx, C.byref(h)))
+        return Chain(h, int(n), int(p))
+    if S is Operator:
+        check(lib().qr_mpo_random(int(n), int(p), int(chi), int(seed) & (2 ** 64 - 1), cplx, C.byref(h)))
+        w = MPO._from_handle(h, int(n), int(p))
+        w._bonds = sampler_bond_dims(int(n), int(chi), int(p), Operator)
+        return w
+    raise ArgumentError("socket must be State or Operator")
 
 
 # ---- canonical forms --------------------------------------------------------------------------------

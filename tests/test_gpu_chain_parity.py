@@ -258,6 +258,73 @@ def test_truncated_gate_on_large_bond(precision):
         assert abs(e - e_ref) <= tol * max(1.0, abs(e_ref)), i
 
 
+def test_checkpoint_roundtrip(tmp_path):
+    """qr_chain_save / qr_chain_load: the file holds the reference-layout arrays and Lambdas
+    (read back independently on the host) and restores the same chain."""
+    from qrochet import checkpoint
+
+    psi, ref = _pair(6, 4, seed=21, uniform=False)
+    Q.canonize_(psi)
+    O.canonize_(ref)
+    psi.set_precision("mixed")
+    path = tmp_path / "psi.qrchain"
+    psi.save(path)
+    arrays, lams, prec = checkpoint.read(path)
+    assert prec == 1
+    for a, b in zip(psi.arrays(), arrays):
+        assert np.array_equal(np.asarray(a), b)
+    assert [x is not None for x in lams] == psi.lambda_flags()
+    back = Q.Chain.load(path)
+    _check_same(back, ref)
+    assert back.bond_dims() == psi.bond_dims()
+    # a file from the host writer (e.g. exported from Julia) loads as well
+    host = tmp_path / "host.qrchain"
+    raw = R.gaussian_mps_arrays(5, 3, seed=22, uniform=True)
+    checkpoint.write(host, raw)
+    c2 = Q.Chain.load(host)
+    assert _close(_sv(c2), O.to_statevector(O.from_reference_arrays(raw)))
+    with pytest.raises(Q.ArgumentError):
+        Q.Chain.load(tmp_path / "missing.qrchain")
+
+
+@pytest.mark.parametrize("eltype", [np.float64, np.complex128])
+def test_rand_state_on_device(eltype):
+    """rand(Chain, Open, State; n, p, χ) on the device (Chain_test.jl:209-221): norm 1, bonds at
+    most χ and equal to the sampler's pattern, sites 2..n right-canonical, seed-deterministic."""
+    n, chi = 8, 10
+    psi = Q.rand(Q.Chain, Q.Open, Q.State, n=n, chi=chi, p=2, eltype=eltype, seed=5)
+    assert psi.bond_dims() == Q.sampler_bond_dims(n, chi, 2)
+    assert max(psi.bond_dims()) <= chi
+    assert abs(Q.norm(psi) - 1.0) <= 1e-12
+    for i in range(2, n + 1):
+        assert Q.isrightcanonical(psi, i)
+    arrays = psi.arrays()
+    if eltype is np.float64:
+        assert all(np.max(np.abs(np.imag(a))) == 0 for a in arrays)
+    else:
+        assert any(np.max(np.abs(np.imag(a))) > 0.01 for a in arrays)
+    again = Q.rand(Q.Chain, Q.Open, Q.State, n=n, chi=chi, p=2, eltype=eltype, seed=5)
+    other = Q.rand(Q.Chain, Q.Open, Q.State, n=n, chi=chi, p=2, eltype=eltype, seed=6)
+    assert all(np.array_equal(a, b) for a, b in zip(arrays, again.arrays()))
+    assert not all(np.allclose(a, b) for a, b in zip(arrays, other.arrays()))
+    # the oracle agrees on the state's norm from the same arrays
+    assert abs(O.norm(O.from_reference_arrays(arrays)) - 1.0) <= 1e-12
+
+
+def test_rand_operator_on_device():
+    """rand(Chain, Open, Operator; n, p, χ) on the device (Chain_test.jl:223-235): Frobenius norm 1
+    and bonds at most χ, checked on the downloaded arrays with the oracle."""
+    n, chi = 6, 10
+    w = Q.rand(Q.Chain, Q.Open, Q.Operator, n=n, chi=chi, p=2, seed=9)
+    assert max(w._bonds) <= chi
+    arrays = w.arrays()
+    ws = [arrays[0][None, :, :, :]]
+    ws += [np.transpose(a, (2, 0, 1, 3)) for a in arrays[1:-1]]
+    ws += [np.transpose(arrays[-1], (2, 0, 1))[..., None]]
+    dense = O.mpo_to_dense(ws)
+    assert abs(np.linalg.norm(dense) - 1.0) <= 1e-12
+
+
 def test_config1_pipeline():
     # plain workload: n=16, d=2, chi=32 Gaussian MPS; canonize!, norm, <Z_i Z_{i+1}> for all i
     psi, ref = _pair(16, 32, seed=1)
