@@ -87,11 +87,17 @@ int qr_host_free(void* ptr);
 /* ---- chain lifecycle (Chain.jl:64-100, :11) --------------------------------------------- */
 int qr_chain_create(int n, int d, const int* bond_dims /* n-1 */, qr_chain** out);
 int qr_chain_free(qr_chain* h);
+/* pMPS(arrays) / Chain(State(), Periodic(), arrays) (src/Ansatz/Chain.jl:19,36-62): n bonds, the
+   last between site n and site 1; every site is (o, l, r) (no open ends).  Canonical forms stay
+   Open-only as in the reference (QR_EINVAL); overlap, norm, expect, evolve! (1 site, and 2 sites
+   on an inner bond), truncate! and the canonicality checks work on periodic chains. */
+int qr_chain_create_periodic(int n, int d, const int* bond_dims /* n */, qr_chain** out);
+int qr_chain_boundary(const qr_chain* h, int* periodic);
 int qr_chain_copy(const qr_chain* src, qr_chain** out);
 int qr_chain_upload_site(qr_chain* h, int site, const double* host, const char* order);
 int qr_chain_download_site(const qr_chain* h, int site, double* host, const char* order);
 int qr_chain_site_dims(const qr_chain* h, int site, int* chi_l, int* d, int* chi_r);
-int qr_chain_bond_dims(const qr_chain* h, int* out /* n-1 */);
+int qr_chain_bond_dims(const qr_chain* h, int* out /* n-1, or n for a periodic chain */);
 int qr_chain_has_lambda(const qr_chain* h, int bond, int* flag);
 int qr_chain_get_lambda(const qr_chain* h, int bond, double* out, int* len);
 int qr_chain_set_lambda(qr_chain* h, int bond, const double* lam, int len);

@@ -4,7 +4,8 @@ This module is the checker, never the product: only ``tests/``, ``__graft_entry_
 and the ``cpu_baseline`` / ``--impl reference`` legs of ``bench.py`` may import it.
 
 It restates, in NumPy on LAPACK, the semantics of Qrochet.jl's ``src/Ansatz/Chain.jl`` (v0.1.2)
-for open-boundary chains.  Qrochet itself is Julia, and its arithmetic lives in the un-vendored
+for open-boundary chains, and for periodic ones the operations the reference does not restrict to
+``::Open`` (construction, evolve!, truncate!, overlap, expect).  Qrochet itself is Julia, and its arithmetic lives in the un-vendored
 packages Tenet.jl (compat 0.6) and Muscle.jl (compat 0.2) on top of Julia ``LinearAlgebra``:
 ``qr`` = LAPACK geqrf + ungqr (thin Q) and ``svd`` = LAPACK gesdd (thin, descending singular
 values).  NumPy's ``linalg.qr(mode="reduced")`` and ``linalg.svd(full_matrices=False)`` call the
@@ -50,10 +51,13 @@ class MissingSchmidtCoefficientsException(RuntimeError):
 # ---------------------------------------------------------------------------------------------
 @dataclass
 class OChain:
-    """Open-boundary MPS: ``sites[i]`` shaped (chi_l, d, chi_r), ``lam[i]`` on bond (i, i+1)."""
+    """MPS: ``sites[i]`` shaped (chi_l, d, chi_r), ``lam[i]`` on bond (i, i+1).  Open boundary by
+    default (end bonds of size 1); ``periodic=True`` closes site n's right bond onto site 1's
+    left bond (``Chain(State(), Periodic(), arrays)``, ``Chain.jl:36-62``)."""
 
     sites: list
     lam: list = field(default=None)
+    periodic: bool = False
 
     def __post_init__(self):
         n = len(self.sites)
@@ -64,15 +68,18 @@ class OChain:
             assert a.ndim == 3, "site tensors are (chi_l, d, chi_r)"
             if i > 0:
                 assert self.sites[i - 1].shape[2] == a.shape[0], f"bond {i - 1} mismatch"
-        assert self.sites[0].shape[0] == 1 and self.sites[-1].shape[2] == 1
+        if self.periodic:
+            assert self.sites[-1].shape[2] == self.sites[0].shape[0], "closing bond mismatch"
+        else:
+            assert self.sites[0].shape[0] == 1 and self.sites[-1].shape[2] == 1
 
     @property
     def n(self):
         return len(self.sites)
 
     def bond_dims(self):
-        """Sizes of the n-1 virtual bonds."""
-        return [a.shape[2] for a in self.sites[:-1]]
+        """Sizes of the n-1 virtual bonds (n for a periodic chain: the last closes the ring)."""
+        return [a.shape[2] for a in (self.sites if self.periodic else self.sites[:-1])]
 
     def lambda_flags(self):
         """Which bonds hold a Lambda hyperindex tensor."""
@@ -84,6 +91,20 @@ class OChain:
 
     def copy(self):
         return _copy.deepcopy(self)
+
+
+def from_reference_arrays_periodic(arrays, order=("o", "l", "r")):
+    """``pMPS(arrays)`` / ``Chain(State(), Periodic(), arrays; order)`` (``Chain.jl:36-62``):
+    every array is 3-d."""
+    order = tuple(order)
+    if set(order) != {"o", "l", "r"} or len(order) != 3:
+        raise ArgumentError("order must be a permutation of (o, l, r)")
+    sites = []
+    for a in arrays:
+        a = np.asarray(a, dtype=np.complex128)
+        assert a.ndim == 3, "All arrays must have 3 dimensions"
+        sites.append(np.ascontiguousarray(np.transpose(a, (order.index("l"), order.index("o"), order.index("r")))))
+    return OChain(sites, periodic=True)
 
 
 def from_reference_arrays(arrays, order=("o", "l", "r")):
@@ -124,6 +145,12 @@ def _pinv_diag(lam, atol):
     mask = np.abs(lam) > atol
     out[mask] = 1.0 / lam[mask]
     return out
+
+
+def _require_open(ch):
+    """Canonical forms dispatch on ``::Open`` only (``Chain.jl:339,469,509``)."""
+    if ch.periodic:
+        raise ArgumentError("canonical forms are defined for Open chains only")
 
 
 def _thin_qr(m):
@@ -176,6 +203,7 @@ def canonize_site_(ch: OChain, site: int, direction: str, method: str = "qr"):
     together with any Lambda already on that bond, S becomes that bond's Lambda.
     ``:left`` mirrors it with A[(o,r) x l] and site-1.
     """
+    _require_open(ch)
     n = ch.n
     if direction == "left":
         if site == 0:
@@ -266,6 +294,7 @@ def isrightcanonical(ch: OChain, site: int, atol=1e-12):
 # canonize! (Vidal form) -- Chain.jl:469-497
 # ---------------------------------------------------------------------------------------------
 def canonize_(ch: OChain):
+    _require_open(ch)
     n = ch.n
     for i in range(n - 1, 0, -1):  # right-to-left QR sweep
         canonize_site_(ch, i, "left", "qr")
@@ -287,6 +316,7 @@ def canonize_(ch: OChain):
 # mixed_canonize! / normalize! -- Chain.jl:509-536
 # ---------------------------------------------------------------------------------------------
 def mixed_canonize_(ch: OChain, center: int):
+    _require_open(ch)
     n = ch.n
     for i in range(0, center):
         canonize_site_(ch, i, "right", "qr")
@@ -297,6 +327,7 @@ def mixed_canonize_(ch: OChain, center: int):
 
 
 def normalize_(ch: OChain, root: int):
+    _require_open(ch)
     mixed_canonize_(ch, root)
     lm = ch.lam[root - 1]
     ch.lam[root - 1] = lm / np.linalg.norm(lm)
@@ -437,6 +468,8 @@ def overlap(a: OChain, b: OChain):
     """``overlap(a, b)`` = contract(a with b'), i.e. <b|a> (b conjugated)."""
     if a.n != b.n:
         raise ArgumentError("Ansatzes must have the same sites")
+    if a.periodic or b.periodic:  # ring: contract the state vectors (oracle sizes are small)
+        return np.vdot(to_statevector(b), to_statevector(a))
     sa, sb = _with_lambdas(a), _with_lambdas(b)
     env = np.ones((1, 1), dtype=np.complex128)  # env[ket, bra]
     for x, y in zip(sa, sb):
@@ -469,8 +502,14 @@ def mpo_expect(psi: OChain, w_sites):
 
 
 def to_statevector(ch: OChain):
-    """Full contraction to a dense vector indexed (o_1, ..., o_n), o_1 slowest."""
+    """Full contraction to a dense vector indexed (o_1, ..., o_n), o_1 slowest; a periodic
+    chain is traced over its closing bond."""
     s = _with_lambdas(ch)
+    if ch.periodic:
+        v = s[0]  # (a0, d, chi_r): the closing index a0 rides along
+        for a in s[1:]:
+            v = np.einsum("kxb,bor->kxor", v, a).reshape(v.shape[0], -1, a.shape[2])
+        return np.einsum("kxk->x", v)
     v = s[0][0]  # (d, chi_r)
     for a in s[1:]:
         v = np.einsum("xb,bor->xor", v, a).reshape(-1, a.shape[2])

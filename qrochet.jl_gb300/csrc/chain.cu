@@ -59,6 +59,7 @@ using namespace qr;
 
 struct qr_chain {
   int n = 0, d = 0, precision = QR_FP64;
+  bool periodic = false;          // Periodic boundary: bd[n-1] is the bond between site n and site 1
   cudaStream_t stream = nullptr;
   std::vector<int> bd;            // n-1 bond sizes
   std::vector<double2*> site;     // n site tensors
@@ -70,8 +71,8 @@ struct qr_chain {
   double2* ws = nullptr;          // theta / factorisation workspace
   size_t ws_cap = 0;
   double* scal = nullptr;         // small device scalars
-  int cl(int i) const { return i == 0 ? 1 : bd[i - 1]; }
-  int cr(int i) const { return i == n - 1 ? 1 : bd[i]; }
+  int cl(int i) const { return i == 0 ? (periodic ? bd[n - 1] : 1) : bd[i - 1]; }
+  int cr(int i) const { return i == n - 1 ? (periodic ? bd[n - 1] : 1) : bd[i]; }
   size_t elems(int i) const { return (size_t)cl(i) * d * cr(i); }
 };
 
@@ -192,7 +193,13 @@ int check_site(const qr_chain* h, int i) {
 }
 
 // ---- canonize_site! (Chain.jl:339-376) ---------------------------------------------------------
+// Canonical forms exist for Open chains only (src/Ansatz/Chain.jl:339,469,509 dispatch on ::Open).
+int require_open(const qr_chain* h) {
+  return h->periodic ? fail(QR_EINVAL, "canonical forms are defined for Open chains only") : QR_OK;
+}
+
 int canonize_site_impl(qr_chain* h, int i, int dir, int method) {
+  QR_TRY(require_open(h));
   QR_TRY(check_site(h, i));
   if (dir == QR_DIR_LEFT) {
     if (i == 0) return fail(QR_EINVAL, "Cannot right-canonize left-most tensor");
@@ -321,6 +328,7 @@ int truncate_impl(qr_chain* h, int s1, int s2, double threshold, int maxdim) {
 }
 
 int mixed_canonize_impl(qr_chain* h, int center) {
+  QR_TRY(require_open(h));
   QR_TRY(check_site(h, center));
   for (int i = 0; i < center; i++) QR_TRY(canonize_site_impl(h, i, QR_DIR_RIGHT, QR_METHOD_QR));
   for (int i = h->n - 1; i > center; i--) QR_TRY(canonize_site_impl(h, i, QR_DIR_LEFT, QR_METHOD_QR));
@@ -328,6 +336,7 @@ int mixed_canonize_impl(qr_chain* h, int center) {
 }
 
 int normalize_impl(qr_chain* h, int root) {
+  QR_TRY(require_open(h));
   QR_TRY(mixed_canonize_impl(h, root));
   return dnormalize(h->stream, h->lam[root - 1], h->lamlen[root - 1]);
 }
@@ -422,7 +431,111 @@ struct EnvOps {
 // In QR_MIXED the two contractions of every site step run on the BF16 tensor cores
 // (zgemm_split, ~FP32 accuracy); the operator mixing, Lambda scaling and the stored environments
 // stay FP64.
+// <b|a> of two periodic chains: the closing bond pair (a0, b0) rides along as a spectator index
+// s = a0 + chi0a b0 in the environment E[a, s, b] (the slot an MPO index takes in env_sweep), the
+// sweep starts from E = delta(a, a0) delta(b, b0) and ends with the trace over a_n = a0, b_n = b0.
+// Per site: X[(s, b), (o, a')] = E^T A, the permute Y[(b, o), s, a'] = X, then the batched
+// E'[a', s, b'] = sum_{(b,o)} Y conj(B).  Cost and memory grow with chi0a chi0b.
+__global__ void ring_init_k(double2* E, int ca, int cb) {
+  const long total = (long)ca * ca * cb * cb;  // E[a, s, b], s = a0 + ca b0
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+    const long a = t % ca, r = t / ca, sidx = r % ((long)ca * cb), b = r / ((long)ca * cb);
+    const long a0 = sidx % ca, b0 = sidx / ca;
+    E[t] = make_double2(a == a0 && b == b0 ? 1.0 : 0.0, 0.0);
+  }
+}
+__global__ void ring_trace_k(const double2* E, int ca, int cb, double2* out) {
+  // out[s] = E[a0, s, b0] for s = a0 + ca b0 (summed on the host in FP64)
+  const long S = (long)ca * cb;
+  for (long sidx = blockIdx.x * (long)blockDim.x + threadIdx.x; sidx < S; sidx += (long)gridDim.x * blockDim.x) {
+    const long a0 = sidx % ca, b0 = sidx / ca;
+    out[sidx] = E[a0 + ca * (sidx + S * b0)];
+  }
+}
+
+int env_sweep_ring(const qr_chain* a, const qr_chain* b, cudaStream_t s, double out[2]) {
+  const int n = a->n, d = a->d;
+  const int c0a = a->cl(0), c0b = b->cl(0);
+  const long S = (long)c0a * c0b;
+  const bool split = (a->precision & QR_SPLIT_CONTRACT) != 0;
+  size_t maxE = 1, maxX = 1;
+  for (int i = 0; i < n; i++) {
+    maxE = std::max(maxE, (size_t)std::max(a->cl(i), a->cr(i)) * S * std::max(b->cl(i), b->cr(i)));
+    maxX = std::max(maxX, (size_t)S * b->cl(i) * d * a->cr(i));
+  }
+  double2 *E0 = nullptr, *E1 = nullptr, *X = nullptr, *Y = nullptr, *tr = nullptr;
+  QR_TRY(dalloc((void**)&E0, sizeof(double2) * maxE, s));
+  QR_TRY(dalloc((void**)&E1, sizeof(double2) * maxE, s));
+  QR_TRY(dalloc((void**)&X, sizeof(double2) * maxX, s));
+  QR_TRY(dalloc((void**)&Y, sizeof(double2) * maxX, s));
+  QR_TRY(dalloc((void**)&tr, sizeof(double2) * S, s));
+  const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
+  {
+    long tot = (long)c0a * S * c0b;
+    unsigned g = (unsigned)std::min<long>((tot + 255) / 256, 4864);
+    ring_init_k<<<g, 256, 0, s>>>(E0, c0a, c0b);
+    count_launch();
+  }
+  int rc = QR_OK;
+  for (int i = 0; i < n && rc == QR_OK; i++) {
+    const int ca = a->cl(i), ca2 = a->cr(i), cb = b->cl(i), cb2 = b->cr(i);
+    if (i > 0 && (a->lam[i - 1] || b->lam[i - 1])) {
+      long tot = (long)ca * S * cb;
+      unsigned g = (unsigned)std::min<long>((tot + 255) / 256, 4864);
+      scale_env_k<<<g, 256, 0, s>>>(E0, ca, (int)S, cb, a->lam[i - 1], b->lam[i - 1]);
+      count_launch();
+    }
+    // X[(s, b), (o, a')] = E^T A
+    rc = split ? zgemm_split(s, OP_T, OP_N, (int)(S * cb), d * ca2, ca, E0, ca, 0, a->site[i], ca, 0, X, S * cb, 0, 1)
+               : zgemm(s, OP_T, OP_N, (int)(S * cb), d * ca2, ca, one, E0, ca, 0, a->site[i], ca, 0, zero, X, S * cb,
+                       0, 1, nullptr);
+    if (rc) break;
+    // Y[(b, o), s, a'] = X[(s, b), (o, a')]
+    Perm p;
+    p.nd = 4;
+    p.dims[0] = cb;
+    p.dims[1] = d;
+    p.dims[2] = S;
+    p.dims[3] = ca2;
+    p.src_stride[0] = S;
+    p.src_stride[1] = S * cb;
+    p.src_stride[2] = 1;
+    p.src_stride[3] = S * cb * d;
+    rc = zpermute(s, X, Y, p);
+    if (rc) break;
+    // E'[a', s, b'] = sum_{(b,o)} Y[(b,o), s, a'] conj(B[(b,o), b'])
+    rc = split ? zgemm_split(s, OP_T, OP_R, ca2, cb2, cb * d, Y, (long)cb * d * S, (long)cb * d, b->site[i],
+                             (long)cb * d, 0, E1, (long)ca2 * S, ca2, (int)S)
+               : zgemm(s, OP_T, OP_R, ca2, cb2, cb * d, one, Y, (long)cb * d * S, (long)cb * d, b->site[i],
+                       (long)cb * d, 0, zero, E1, (long)ca2 * S, ca2, (int)S, nullptr);
+    std::swap(E0, E1);
+  }
+  if (rc == QR_OK) {
+    unsigned g = (unsigned)std::min<long>((S + 255) / 256, 4864);
+    ring_trace_k<<<g, 256, 0, s>>>(E0, c0a, c0b, tr);
+    count_launch();
+    std::vector<double2> h(S);
+    rc = cuda_ok(cudaMemcpyAsync(h.data(), tr, sizeof(double2) * S, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
+    if (!rc) rc = cuda_ok(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    double re = 0, im = 0;
+    for (const double2& v : h) { re += v.x; im += v.y; }
+    out[0] = re;
+    out[1] = im;
+  }
+  cudaFreeAsync(E0, s);
+  cudaFreeAsync(E1, s);
+  cudaFreeAsync(X, s);
+  cudaFreeAsync(Y, s);
+  cudaFreeAsync(tr, s);
+  return rc;
+}
+
 int env_sweep(const qr_chain* a, const qr_chain* b, const EnvOps* ops, cudaStream_t s, double out[2]) {
+  if (a->periodic || b->periodic) {
+    if (!(a->periodic && b->periodic)) return fail(QR_EINVAL, "both chains must have the same boundary");
+    if (ops) return fail(QR_EINVAL, "operator expectation values of periodic chains are not implemented");
+    return env_sweep_ring(a, b, s, out);
+  }
   const int n = a->n, d = a->d;
   const bool split = (a->precision & QR_SPLIT_CONTRACT) != 0;
   // largest buffers
@@ -521,12 +634,29 @@ int qr_launch_count(uint64_t* count) {
   return QR_OK;
 }
 
+static int chain_create(int n, int d, const int* bond_dims, bool periodic, qr_chain** out);
+
 int qr_chain_create(int n, int d, const int* bond_dims, qr_chain** out) {
+  return chain_create(n, d, bond_dims, false, out);
+}
+
+int qr_chain_create_periodic(int n, int d, const int* bond_dims, qr_chain** out) {
+  return chain_create(n, d, bond_dims, true, out);
+}
+
+int qr_chain_boundary(const qr_chain* h, int* periodic) {
+  if (!h || !periodic) return fail(QR_EINVAL, "null argument");
+  *periodic = h->periodic ? 1 : 0;
+  return QR_OK;
+}
+
+static int chain_create(int n, int d, const int* bond_dims, bool periodic, qr_chain** out) {
   if (!out) return fail(QR_EINVAL, "null output");
   *out = nullptr;
   if (n < 2) return fail(QR_EINVAL, "a Chain needs at least 2 sites");
   if (d < 2 || d > 4) return fail(QR_EINVAL, "physical dimension must be 2..4");
-  for (int b = 0; b < n - 1; b++)
+  const int nb = periodic ? n : n - 1;
+  for (int b = 0; b < nb; b++)
     if (!bond_dims || bond_dims[b] < 1) return fail(QR_EINVAL, "bond dimensions must be >= 1");
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(QR_ENODEV, "no CUDA device");
@@ -534,7 +664,8 @@ int qr_chain_create(int n, int d, const int* bond_dims, qr_chain** out) {
   qr_chain* h = new qr_chain();
   h->n = n;
   h->d = d;
-  h->bd.assign(bond_dims, bond_dims + n - 1);
+  h->periodic = periodic;
+  h->bd.assign(bond_dims, bond_dims + nb);
   h->site.assign(n, nullptr);
   h->lam.assign(n - 1, nullptr);
   h->lamlen.assign(n - 1, 0);
@@ -571,7 +702,7 @@ int qr_chain_free(qr_chain* h) {
 int qr_chain_copy(const qr_chain* src, qr_chain** out) {
   if (!src || !out) return fail(QR_EINVAL, "null chain");
   QR_CUDA(cudaStreamSynchronize(src->stream));
-  QR_TRY(qr_chain_create(src->n, src->d, src->bd.data(), out));
+  QR_TRY(chain_create(src->n, src->d, src->bd.data(), src->periodic, out));
   qr_chain* h = *out;
   h->precision = src->precision;
   for (int i = 0; i < src->n; i++)
@@ -585,7 +716,7 @@ int qr_chain_upload_site(qr_chain* h, int site, const double* host, const char* 
   QR_TRY(check_site(h, site));
   if (!host) return fail(QR_EINVAL, "null host array");
   if (!is_perm(order ? order : "", "olr")) return fail(QR_EINVAL, "order must be a permutation of (o, l, r)");
-  std::string ho = filtered(order, site == 0, site == h->n - 1);
+  std::string ho = filtered(order, site == 0 && !h->periodic, site == h->n - 1 && !h->periodic);
   long idims[3] = {h->cl(site), h->d, h->cr(site)};
   Perm p = make_perm(ho, "lor", idims);
   size_t ne = h->elems(site);
@@ -601,7 +732,7 @@ int qr_chain_download_site(const qr_chain* hc, int site, double* host, const cha
   QR_TRY(check_site(h, site));
   if (!host) return fail(QR_EINVAL, "null host array");
   if (!is_perm(order ? order : "", "olr")) return fail(QR_EINVAL, "order must be a permutation of (o, l, r)");
-  std::string ho = filtered(order, site == 0, site == h->n - 1);
+  std::string ho = filtered(order, site == 0 && !h->periodic, site == h->n - 1 && !h->periodic);
   // dst (host order) gathers from the internal (l,o,r) layout: build the inverse map
   long dims_by_letter[3] = {h->cl(site), h->d, h->cr(site)};  // l, o, r
   const std::string iord = "lor";
@@ -757,8 +888,9 @@ int qr_mpo_random(int n, int d, int chi, uint64_t seed, int complex_entries, qr_
 }
 
 // ---- checkpoint / export ---------------------------------------------------------------------
-// File layout (little-endian), written so a Julia reader can rebuild MPS(arrays) directly:
-//   "QRCHAIN1" | int32 n, d, precision, 0 | int32 bond_dims[n-1] | uint8 has_lambda[n-1]
+// File layout (little-endian), written so a Julia reader can rebuild MPS(arrays) / pMPS(arrays):
+//   "QRCHAIN1" | int32 n, d, precision, periodic | int32 bond_dims[n-1, or n when periodic: the
+//   last is the bond between site n and site 1] | uint8 has_lambda[n-1]
 //   | site 0 .. n-1: ComplexF64 data in the reference's (o, l, r) column-major order, the open ends
 //     without l (site 1) and r (site n) | for every bond with has_lambda: Float64 Lambda[bond_dim]
 namespace {
@@ -775,9 +907,9 @@ int qr_chain_save(const qr_chain* h, const char* path) {
   if (!h || !path) return fail(QR_EINVAL, "null argument");
   FileCloser fc{fopen(path, "wb")};
   if (!fc.f) return fail(QR_EINVAL, std::string("cannot open for writing: ") + path);
-  const int32_t hdr[4] = {h->n, h->d, h->precision, 0};
+  const int32_t hdr[4] = {h->n, h->d, h->precision, h->periodic ? 1 : 0};
   bool ok = fwrite(kChainMagic, 1, 8, fc.f) == 8 && fwrite(hdr, sizeof(int32_t), 4, fc.f) == 4;
-  std::vector<int32_t> bd(h->bd.begin(), h->bd.end());
+  std::vector<int32_t> bd(h->bd.begin(), h->bd.end());  // n - 1 bonds, n for a periodic chain
   std::vector<uint8_t> fl(h->n - 1);
   for (int b = 0; b < h->n - 1; b++) fl[b] = h->lam[b] != nullptr;
   ok = ok && fwrite(bd.data(), sizeof(int32_t), bd.size(), fc.f) == bd.size();
@@ -809,9 +941,10 @@ int qr_chain_load(const char* path, qr_chain** out) {
   if (fread(magic, 1, 8, fc.f) != 8 || memcmp(magic, kChainMagic, 8) != 0 ||
       fread(hdr, sizeof(int32_t), 4, fc.f) != 4)
     return fail(QR_EINVAL, "not a chain checkpoint");
-  const int n = hdr[0], d = hdr[1], prec = hdr[2];
-  if (n < 2 || n > (1 << 20) || d < 1 || d > 64) return fail(QR_EINVAL, "corrupt chain checkpoint header");
-  std::vector<int32_t> bd(n - 1);
+  const int n = hdr[0], d = hdr[1], prec = hdr[2], periodic = hdr[3];
+  if (n < 2 || n > (1 << 20) || d < 1 || d > 64 || (periodic != 0 && periodic != 1))
+    return fail(QR_EINVAL, "corrupt chain checkpoint header");
+  std::vector<int32_t> bd(periodic ? n : n - 1);
   std::vector<uint8_t> fl(n - 1);
   if (fread(bd.data(), sizeof(int32_t), bd.size(), fc.f) != bd.size() || fread(fl.data(), 1, fl.size(), fc.f) != fl.size())
     return fail(QR_EINVAL, "truncated chain checkpoint");
@@ -819,7 +952,7 @@ int qr_chain_load(const char* path, qr_chain** out) {
     if (b < 1) return fail(QR_EINVAL, "corrupt chain checkpoint bond dimensions");
   std::vector<int> bdi(bd.begin(), bd.end());
   qr_chain* h = nullptr;
-  QR_TRY(qr_chain_create(n, d, bdi.data(), &h));
+  QR_TRY(chain_create(n, d, bdi.data(), periodic != 0, &h));
   int rc = qr_chain_set_precision(h, prec);
   std::vector<double> buf;
   for (int i = 0; i < n && !rc; i++) {
@@ -851,7 +984,7 @@ int qr_chain_site_dims(const qr_chain* h, int site, int* chi_l, int* d, int* chi
 
 int qr_chain_bond_dims(const qr_chain* h, int* out) {
   if (!h || !out) return fail(QR_EINVAL, "null argument");
-  for (int b = 0; b < h->n - 1; b++) out[b] = h->bd[b];
+  for (int b = 0; b < (int)h->bd.size(); b++) out[b] = h->bd[b];
   return QR_OK;
 }
 
@@ -1056,6 +1189,25 @@ int qr_expect(const qr_chain* h, int nobs, const int* first, const int* nlanes, 
   if (!h || !out) return fail(QR_EINVAL, "null argument");
   if (nobs < 0 || (nobs > 0 && (!first || !nlanes || !mats))) return fail(QR_EINVAL, "bad observable list");
   const int n = h->n, d = h->d;
+  if (h->periodic) {
+    // the reference's own algorithm (Chain.jl:724-735): evolve! a copy by every observable (no
+    // truncation), then contract it with the adjoint of the original (the ring sweep)
+    qr_chain* c = nullptr;
+    QR_TRY(qr_chain_copy(h, &c));
+    int rc = QR_OK;
+    size_t off = 0;
+    for (int j = 0; j < nobs && !rc; j++) {
+      const int s0 = first[j], nl = nlanes[j];
+      if (nl != 1 && nl != 2) rc = fail(QR_EINVAL, "Invalid number of lanes, maximum is 2");
+      else if (s0 < 0 || s0 + nl > n) rc = fail(QR_EINVAL, "Gate inputs must be a subset of the TN sites");
+      else if (nl == 1) rc = qr_evolve_1site(c, s0, mats + 2 * off);
+      else rc = qr_evolve_2site(c, s0, mats + 2 * off, NAN, -1, 0, 0);
+      off += nl == 1 ? (size_t)d * d : (size_t)d * d * d * d;
+    }
+    if (!rc) rc = qr_overlap(c, h, out);
+    qr_chain_free(c);
+    return rc;
+  }
   typedef std::complex<double> cd;
   // per-site operator tensors (wl, o, i, wr), wl fastest
   std::vector<std::vector<cd>> W(n);

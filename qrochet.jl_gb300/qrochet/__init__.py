@@ -5,7 +5,7 @@ its C ABI (include/qrochet_gpu.h).  ``f!`` in Julia is ``f_`` here.
 """
 from ._lib import (ArgumentError, DimensionMismatch, GPUError, MissingSchmidtCoefficientsException,
                    launch_count)
-from .chain import (MPO, MPS, Chain, Open, Periodic, canonicality_error, canonize, canonize_,
+from .chain import (MPO, MPS, pMPS, Chain, Open, Periodic, canonicality_error, canonize, canonize_,
                     canonize_site, canonize_site_, contract_between, contract_between_, device_count,
                     evolve_, expect, isleftcanonical, isrightcanonical, mixed_canonize, mixed_canonize_,
                     mpo_expect, norm, normalize_, overlap, truncate, truncate_, zeros_chain,
@@ -17,7 +17,7 @@ from . import checkpoint
 
 __all__ = [
     "ArgumentError", "DimensionMismatch", "GPUError", "MissingSchmidtCoefficientsException",
-    "launch_count", "MPO", "MPS", "Chain", "Open", "Periodic", "canonicality_error", "canonize",
+    "launch_count", "MPO", "MPS", "pMPS", "Chain", "Open", "Periodic", "canonicality_error", "canonize",
     "canonize_", "canonize_site", "canonize_site_", "contract_between", "contract_between_",
     "device_count", "evolve_", "expect", "isleftcanonical", "isrightcanonical", "mixed_canonize",
     "mixed_canonize_", "mpo_expect", "norm", "normalize_", "overlap", "truncate", "truncate_",

@@ -58,6 +58,8 @@ SIGNATURES = {
     "qr_host_free": [_P],
     "qr_chain_create": [_I, _I, _PI, C.POINTER(_P)],
     "qr_chain_free": [_P],
+    "qr_chain_create_periodic": [_I, _I, _PI, C.POINTER(_P)],
+    "qr_chain_boundary": [_P, _PI],
     "qr_chain_copy": [_P, C.POINTER(_P)],
     "qr_chain_upload_site": [_P, _I, _PD, _S],
     "qr_chain_download_site": [_P, _I, _PD, _S],

@@ -23,7 +23,7 @@ class Open:
 
 
 class Periodic:
-    """Periodic boundary (not implemented on the GPU path)."""
+    """Periodic boundary: the last site's right bond is the first site's left bond."""
 
 
 _DIR = {"left": L.QR_DIR_LEFT, "right": L.QR_DIR_RIGHT}
@@ -47,14 +47,16 @@ def _site_id(s):
 
 
 class Chain:
-    """Open-boundary MPS in device memory (``Chain{Quantum, Open}`` with a ``State`` socket)."""
+    """MPS in device memory (``Chain{Quantum, Open}`` or ``Chain{Quantum, Periodic}`` with a
+    ``State`` socket)."""
 
-    def __init__(self, handle, n, d, phys=None, bonds=None):
+    def __init__(self, handle, n, d, phys=None, bonds=None, periodic=False):
         self._h = handle
         self.n = n
         self.d = d
+        self.periodic = bool(periodic)
         self._phys = phys or [nextindex() for _ in range(n)]
-        self._bonds = bonds or [nextindex() for _ in range(n - 1)]
+        self._bonds = bonds or [nextindex() for _ in range(n if self.periodic else n - 1)]
 
     # ---- construction ------------------------------------------------------------------------
     @classmethod
@@ -94,6 +96,36 @@ class Chain:
             check(lib().qr_chain_upload_site(h, i, dptr(buf), ordstr))
         return ch
 
+    @classmethod
+    def from_arrays_periodic(cls, arrays, order=("o", "l", "r")):
+        """``Chain(State(), Periodic(), arrays; order)`` (Chain.jl:36-62): every site is 3-d and
+        site n's right bond closes onto site 1's left bond."""
+        order = _norm_order(order, "olr")
+        n = len(arrays)
+        if n < 2:
+            raise ArgumentError("a Chain needs at least 2 sites")
+        arrays = [np.asarray(a) for a in arrays]
+        if any(a.ndim != 3 for a in arrays):
+            raise AssertionError("All arrays must have 3 dimensions")
+        dims = [dict(zip(order, a.shape)) for a in arrays]
+        d = dims[0]["o"]
+        bond = []
+        for i in range(n):
+            r, l = dims[i]["r"], dims[(i + 1) % n]["l"]
+            if r != l:
+                raise L.DimensionMismatch(f"bond {i + 1}: {r} != {l}")
+            bond.append(r)
+        if any(x["o"] != d for x in dims):
+            raise L.DimensionMismatch("all sites must share the physical dimension")
+        h = C.c_void_p()
+        check(lib().qr_chain_create_periodic(n, d, (C.c_int * n)(*bond), C.byref(h)))
+        ch = cls(h, n, d, periodic=True)
+        ordstr = "".join(order).encode()
+        for i, a in enumerate(arrays):
+            buf = np.asfortranarray(a, dtype=np.complex128)
+            check(lib().qr_chain_upload_site(h, i, dptr(buf), ordstr))
+        return ch
+
     def __del__(self):
         h = getattr(self, "_h", None)
         if h is not None and L._lib is not None:
@@ -106,7 +138,7 @@ class Chain:
     def copy(self):
         h = C.c_void_p()
         check(lib().qr_chain_copy(self._h, C.byref(h)))
-        return Chain(h, self.n, self.d, list(self._phys), list(self._bonds))
+        return Chain(h, self.n, self.d, list(self._phys), list(self._bonds), self.periodic)
 
     def save(self, path):
         """Checkpoint: the sites in the reference's ``(:o, :l, :r)`` layout, bond dimensions,
@@ -122,14 +154,19 @@ class Chain:
         check(lib().qr_chain_nsites(h, C.byref(n)))
         a, d, b = C.c_int(), C.c_int(), C.c_int()
         check(lib().qr_chain_site_dims(h, 0, C.byref(a), C.byref(d), C.byref(b)))
-        return cls(h, n.value, d.value)
+        per = C.c_int()
+        check(lib().qr_chain_boundary(h, C.byref(per)))
+        return cls(h, n.value, d.value, periodic=bool(per.value))
 
     __copy__ = copy
     __deepcopy__ = lambda self, memo: self.copy()  # noqa: E731
 
     # ---- bookkeeping -------------------------------------------------------------------------
     socket = State()
-    boundary = Open()
+
+    @property
+    def boundary(self):
+        return Periodic() if self.periodic else Open()
 
     def nsites(self):
         return self.n
@@ -138,7 +175,10 @@ class Chain:
         return [Site(i + 1) for i in range(self.n)]
 
     def bond_dims(self):
-        out = (C.c_int * (self.n - 1))()
+        """Bond sizes: bond b joins sites b+1 and b+2; a periodic chain has an n-th bond
+        between site n and site 1."""
+        nb = self.n if self.periodic else self.n - 1
+        out = (C.c_int * nb)()
         check(lib().qr_chain_bond_dims(self._h, out))
         return list(out)
 
@@ -163,19 +203,29 @@ class Chain:
         return a.value, d.value, b.value
 
     def leftsite(self, site):
+        """``leftsite`` (Chain.jl:185-188): wraps around on a periodic chain."""
         i = _site_id(site)
+        if self.periodic:
+            return Site((i - 2) % self.n + 1)
         return Site(i - 1) if 2 <= i <= self.n else None
 
     def rightsite(self, site):
         i = _site_id(site)
+        if self.periodic:
+            return Site(i % self.n + 1)
         return Site(i + 1) if 1 <= i <= self.n - 1 else None
 
     def leftindex(self, site):
+        """``leftindex`` (Chain.jl:195-197)."""
         i = _site_id(site)
+        if self.periodic:
+            return self._bonds[(i - 2) % self.n]
         return None if i == 1 else self._bonds[i - 2]
 
     def rightindex(self, site):
         i = _site_id(site)
+        if self.periodic:
+            return self._bonds[i - 1]
         return None if i == self.n else self._bonds[i - 1]
 
     def physindex(self, site):
@@ -184,6 +234,8 @@ class Chain:
     def bond_index(self, s1, s2):
         """``inds(tn; bond=(s1, s2))``: the shared index, or None when not adjacent."""
         a, b = sorted((_site_id(s1), _site_id(s2)))
+        if self.periodic and (a, b) == (1, self.n) and self.n > 2:
+            return self._bonds[self.n - 1]
         return self._bonds[a - 1] if b == a + 1 else None
 
     def index_size(self, name):
@@ -230,7 +282,8 @@ class Chain:
         i = _site_id(site) - 1
         cl, d, cr = self.site_dims(site)
         dims = {"l": cl, "o": d, "r": cr}
-        sub = [x for x in order if not ((i == 0 and x == "l") or (i == self.n - 1 and x == "r"))]
+        ends = not self.periodic
+        sub = [x for x in order if not ends or not ((i == 0 and x == "l") or (i == self.n - 1 and x == "r"))]
         out = np.empty([dims[x] for x in sub], dtype=np.complex128, order="F")
         check(lib().qr_chain_download_site(self._h, i, dptr(out), "".join(order).encode()))
         return out
@@ -276,6 +329,11 @@ class AdjointChain:
 def MPS(arrays, order=("o", "l", "r")):
     """``MPS(arrays)`` (Chain.jl:18)."""
     return Chain.from_arrays(arrays, order)
+
+
+def pMPS(arrays, order=("o", "l", "r")):
+    """``pMPS(arrays)`` (Chain.jl:19): a periodic MPS."""
+    return Chain.from_arrays_periodic(arrays, order)
 
 
 class MPO:

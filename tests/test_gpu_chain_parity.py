@@ -23,7 +23,7 @@ def _close(a, b, rtol=RTOL):
 
 def _sv(psi: Q.Chain):
     """State vector of a GPU chain (download + oracle contraction)."""
-    ch = O.from_reference_arrays(psi.arrays())
+    ch = (O.from_reference_arrays_periodic if psi.periodic else O.from_reference_arrays)(psi.arrays())
     for b, f in enumerate(psi.lambda_flags()):
         if f:
             ch.lam[b] = psi.lambda_between(b + 1, b + 2)
@@ -323,6 +323,69 @@ def test_rand_operator_on_device():
     ws += [np.transpose(arrays[-1], (2, 0, 1))[..., None]]
     dense = O.mpo_to_dense(ws)
     assert abs(np.linalg.norm(dense) - 1.0) <= 1e-12
+
+
+def _ring(n, chi, seed, closing=2):
+    g = R.rng(seed)
+    bonds = [chi] * (n - 1) + [closing]
+    arrays = [(g.standard_normal((2, bonds[i - 1], bonds[i])) + 1j * g.standard_normal((2, bonds[i - 1], bonds[i])))
+              / np.sqrt(2 * bonds[i - 1]) for i in range(n)]
+    arrays = [np.asfortranarray(a) for a in arrays]
+    return Q.pMPS(arrays), O.from_reference_arrays_periodic(arrays), arrays
+
+
+def test_periodic_construction_and_bookkeeping():
+    """pMPS / Chain(State(), Periodic(), arrays) (Chain_test.jl:2-36, 165-176): site sizes,
+    the closing bond, leftsite/rightsite/leftindex/rightindex wrapping around."""
+    g = R.rng(30)
+    arrays = [g.random((2, 1, 4)), g.random((2, 4, 3)), g.random((2, 3, 1))]
+    psi = Q.pMPS(arrays)
+    assert isinstance(psi.boundary, Q.Periodic)
+    assert [psi.site_array(i + 1).shape for i in range(3)] == [(2, 1, 4), (2, 4, 3), (2, 3, 1)]
+    assert psi.bond_dims() == [4, 3, 1]
+    assert psi.leftindex(1) == psi.rightindex(3) is not None
+    assert psi.leftindex(2) == psi.rightindex(1)
+    assert psi.leftindex(3) == psi.rightindex(2)
+    assert [psi.leftsite(i).id for i in (1, 2, 3)] == [3, 1, 2]
+    assert [psi.rightsite(i).id for i in (1, 2, 3)] == [2, 3, 1]
+    perm = Q.pMPS([np.transpose(a, (2, 0, 1)) for a in arrays], order=("r", "o", "l"))
+    assert [perm.site_array(i + 1, ("r", "o", "l")).shape for i in range(3)] == [(4, 2, 1), (3, 2, 4), (1, 2, 3)]
+    assert _close(_sv(perm), _sv(psi))
+    with pytest.raises(Q.ArgumentError):
+        Q.canonize_(psi)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_periodic_contractions_and_gates(precision):
+    """Ring contraction (norm, overlap), evolve! on inner bonds with truncation, and expect of
+    1- and 2-site observables on periodic chains, against the oracle."""
+    psi, ref, _ = _ring(5, 3, seed=31, closing=2)
+    phi, ref_phi, _ = _ring(5, 3, seed=32, closing=2)
+    psi.set_precision(precision)
+    assert abs(Q.norm(psi) - O.norm(ref)) <= RTOL * O.norm(ref)
+    ov, ov_ref = Q.overlap(psi, phi), O.overlap(ref, ref_phi)
+    assert abs(ov - ov_ref) <= RTOL * max(1.0, abs(ov_ref))
+    u = R.haar_unitary(R.rng(33), 4)
+    Q.evolve_(psi, Q.gate_from_matrix(u, [2, 3]), maxdim=4)
+    O.evolve_2site_(ref, 1, u, maxdim=4)
+    assert psi.bond_dims() == ref.bond_dims()
+    assert _close(_sv(psi), O.to_statevector(ref), 1e-10)
+    z = R.PAULI["Z"]
+    zz = np.kron(z, z)
+    e = Q.expect(psi, [Q.gate_from_matrix(z, [1]), Q.gate_from_matrix(zz, [4, 5])])
+    e_ref = O.expect(ref, [O.ODense(z, (O.OSite(1), O.OSite(1, True))),
+                           O.ODense(zz.reshape(2, 2, 2, 2), (O.OSite(4), O.OSite(5), O.OSite(4, True),
+                                                            O.OSite(5, True)))])
+    assert abs(e - e_ref) <= 1e-10 * max(1.0, abs(e_ref))
+
+
+def test_periodic_checkpoint(tmp_path):
+    psi, ref, arrays = _ring(4, 2, seed=34, closing=3)
+    path = tmp_path / "ring.qrchain"
+    psi.save(path)
+    back = Q.Chain.load(path)
+    assert back.periodic and back.bond_dims() == [2, 2, 2, 3]
+    assert _close(_sv(back), O.to_statevector(ref))
 
 
 def test_config1_pipeline():
