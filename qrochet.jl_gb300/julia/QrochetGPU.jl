@@ -34,27 +34,37 @@ end
 """
     GPUChain(arrays; order = (:o, :l, :r), precision = :fp64)
 
-Open-boundary MPS resident on the GPU, built from the same arrays as `MPS(arrays)`
-(`Chain(State(), Open(), arrays; order)`).
+MPS resident on the GPU, built from the same arrays as `MPS(arrays)`
+(`Chain(State(), Open(), arrays; order)`) or, with `boundary = Periodic()`, as `pMPS(arrays)`.
 """
 mutable struct GPUChain
     handle::Ptr{Cvoid}
     n::Int
     d::Int
+    periodic::Bool
 end
+GPUChain(h::Ptr{Cvoid}, n::Int, d::Int) = GPUChain(h, n, d, false)
 
-function GPUChain(arrays::Vector{<:AbstractArray}; order = (:o, :l, :r), precision = :fp64)
+function GPUChain(arrays::Vector{<:AbstractArray}; order = (:o, :l, :r), precision = :fp64,
+                  boundary = Qrochet.Open())
     n = length(arrays)
     ord = collect(order)
+    periodic = boundary isa Qrochet.Periodic
     dims = map(enumerate(arrays)) do (i, a)
-        sub = filter(x -> !((i == 1 && x == :l) || (i == n && x == :r)), ord)
+        sub = filter(x -> periodic || !((i == 1 && x == :l) || (i == n && x == :r)), ord)
         Dict(zip(sub, size(a)))
     end
     d = dims[1][:o]
-    bonds = Cint[dims[i][:r] for i in 1:n-1]
     h = Ref{Ptr{Cvoid}}(C_NULL)
-    check(ccall((:qr_chain_create, libqrochet), Cint, (Cint, Cint, Ptr{Cint}, Ref{Ptr{Cvoid}}), n, d, bonds, h))
-    chain = GPUChain(h[], n, d)
+    if periodic
+        bonds = Cint[dims[i][:r] for i in 1:n]
+        check(ccall((:qr_chain_create_periodic, libqrochet), Cint, (Cint, Cint, Ptr{Cint}, Ref{Ptr{Cvoid}}),
+                    n, d, bonds, h))
+    else
+        bonds = Cint[dims[i][:r] for i in 1:n-1]
+        check(ccall((:qr_chain_create, libqrochet), Cint, (Cint, Cint, Ptr{Cint}, Ref{Ptr{Cvoid}}), n, d, bonds, h))
+    end
+    chain = GPUChain(h[], n, d, periodic)
     finalizer(c -> ccall((:qr_chain_free, libqrochet), Cint, (Ptr{Cvoid},), c.handle), chain)
     ordstr = join(String.(ord))
     for (i, a) in enumerate(arrays)
@@ -73,15 +83,66 @@ setprecision!(c::GPUChain, p::Symbol) =
 function Base.copy(c::GPUChain)
     h = Ref{Ptr{Cvoid}}(C_NULL)
     check(ccall((:qr_chain_copy, libqrochet), Cint, (Ptr{Cvoid}, Ref{Ptr{Cvoid}}), c.handle, h))
-    out = GPUChain(h[], c.n, c.d)
+    out = GPUChain(h[], c.n, c.d, c.periodic)
     finalizer(x -> ccall((:qr_chain_free, libqrochet), Cint, (Ptr{Cvoid},), x.handle), out)
     return out
+end
+
+function wrap(h::Ptr{Cvoid})
+    n, cl, d, cr, per = Ref{Cint}(0), Ref{Cint}(0), Ref{Cint}(0), Ref{Cint}(0), Ref{Cint}(0)
+    check(ccall((:qr_chain_nsites, libqrochet), Cint, (Ptr{Cvoid}, Ref{Cint}), h, n))
+    check(ccall((:qr_chain_site_dims, libqrochet), Cint, (Ptr{Cvoid}, Cint, Ref{Cint}, Ref{Cint}, Ref{Cint}),
+                h, 0, cl, d, cr))
+    check(ccall((:qr_chain_boundary, libqrochet), Cint, (Ptr{Cvoid}, Ref{Cint}), h, per))
+    out = GPUChain(h, Int(n[]), Int(d[]), per[] != 0)
+    finalizer(x -> ccall((:qr_chain_free, libqrochet), Cint, (Ptr{Cvoid},), x.handle), out)
+    return out
+end
+
+"""`rand(Chain, Open, State; n, p, χ, eltype)` generated on the GPU (the reference's bond pattern
+and Gram-Schmidt isometries; the random stream is the library's own, keyed by `seed`)."""
+function Base.rand(::Type{GPUChain}, ::Type{Qrochet.Open}, ::Type{Qrochet.State}; n::Integer, χ::Integer,
+                   p::Integer = 2, eltype = Float64, seed::Integer = 0)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:qr_chain_random, libqrochet), Cint, (Cint, Cint, Cint, UInt64, Cint, Ref{Ptr{Cvoid}}),
+                n, p, χ, UInt64(seed), eltype <: Complex ? 1 : 0, h))
+    return wrap(h[])
+end
+
+"""Checkpoint: sites in the reference's (:o, :l, :r) layout, bond dimensions, Λ, precision."""
+save(c::GPUChain, path::AbstractString) =
+    check(ccall((:qr_chain_save, libqrochet), Cint, (Ptr{Cvoid}, Cstring), c.handle, path))
+
+function load(path::AbstractString)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:qr_chain_load, libqrochet), Cint, (Cstring, Ref{Ptr{Cvoid}}), path, h))
+    return wrap(h[])
+end
+
+"""Reads a checkpoint on the host (no GPU needed): returns `(arrays, Λs, periodic)` with the arrays
+exactly as `MPS(arrays)` / `pMPS(arrays)` take them (layout documented in INTEGRATION.md)."""
+function read_checkpoint(path::AbstractString)
+    open(path, "r") do io
+        String(read(io, 8)) == "QRCHAIN1" || throw(ArgumentError("not a chain checkpoint"))
+        n, d, _, per = (Int(read(io, Int32)) for _ in 1:4)
+        nb = per == 1 ? n : n - 1
+        bonds = [Int(read(io, Int32)) for _ in 1:nb]
+        flags = [read(io, UInt8) for _ in 1:n-1]
+        shapes = if per == 1
+            [(d, bonds[mod1(i - 1, n)], bonds[i]) for i in 1:n]
+        else
+            [i == 1 ? (d, bonds[1]) : i == n ? (d, bonds[n-1]) : (d, bonds[i-1], bonds[i]) for i in 1:n]
+        end
+        arrays = [(a = Array{ComplexF64}(undef, shp...); read!(io, a); a) for shp in shapes]
+        lams = [flags[b] == 1 ? (v = Vector{Float64}(undef, bonds[b]); read!(io, v); v) : nothing for b in 1:n-1]
+        return arrays, lams, per == 1
+    end
 end
 
 Qrochet.nsites(c::GPUChain) = c.n
 
 function bond_dims(c::GPUChain)
-    out = Vector{Cint}(undef, c.n - 1)
+    out = Vector{Cint}(undef, c.periodic ? c.n : c.n - 1)
     check(ccall((:qr_chain_bond_dims, libqrochet), Cint, (Ptr{Cvoid}, Ptr{Cint}), c.handle, out))
     return Int.(out)
 end
@@ -92,7 +153,7 @@ function sitearray(c::GPUChain, i::Integer; order = (:o, :l, :r))
     check(ccall((:qr_chain_site_dims, libqrochet), Cint, (Ptr{Cvoid}, Cint, Ref{Cint}, Ref{Cint}, Ref{Cint}),
                 c.handle, i - 1, cl, d, cr))
     dims = Dict(:l => cl[], :o => d[], :r => cr[])
-    sub = filter(x -> !((i == 1 && x == :l) || (i == c.n && x == :r)), collect(order))
+    sub = filter(x -> c.periodic || !((i == 1 && x == :l) || (i == c.n && x == :r)), collect(order))
     out = Array{ComplexF64}(undef, (dims[x] for x in sub)...)
     check(ccall((:qr_chain_download_site, libqrochet), Cint, (Ptr{Cvoid}, Cint, Ptr{ComplexF64}, Cstring),
                 c.handle, i - 1, out, join(String.(collect(order)))))
@@ -198,6 +259,6 @@ function Qrochet.expect(c::GPUChain, observables)
     return out[]
 end
 
-export GPUChain, bond_dims, sitearray, spectrum, setprecision!
+export GPUChain, bond_dims, sitearray, spectrum, setprecision!, save, load, read_checkpoint
 
 end # module
