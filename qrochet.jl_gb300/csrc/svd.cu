@@ -995,16 +995,17 @@ __device__ __forceinline__ bool rotation_params_df(dfl a, dfl b, dfl gr, dfl gi,
   float t = az > 1e18f ? 0.5f / az : 1.f / (az + sqrtf(1.f + az * az));
   t = zeta >= 0.f ? t : -t;
   if (!(t != 0.f)) return false;
+  P.tabs = fabsf(t);
+  if (fabsf(t) < 0x1p-24f) {  // the small-angle rotation uses s in FP32 only
+    const float rgf = rsqrtf(n2.h);
+    P.c = {1.f, 0.f};
+    P.sr = {t * grs.h * rgf, 0.f};
+    P.si = {t * gis.h * rgf, 0.f};
+    return true;
+  }
   // phase e^{i phi} = g / |g| in double-float
   const dfl rg = df_rsqrt(n2);
   const dfl er = df_mul(grs, rg), ei = df_mul(gis, rg);
-  P.tabs = fabsf(t);
-  if (fabsf(t) < 0x1p-24f) {
-    P.c = {1.f, 0.f};
-    P.sr = {t * er.h, 0.f};
-    P.si = {t * ei.h, 0.f};
-    return true;
-  }
   const float tt = __fmul_rn(t, t);
   const dfl u = df_add({1.f, 0.f}, {tt, fmaf(t, t, -tt)});  // 1 + t^2, t^2 exact as a pair
   const dfl c = df_rsqrt(u);
@@ -1015,12 +1016,29 @@ __device__ __forceinline__ bool rotation_params_df(dfl a, dfl b, dfl gr, dfl gi,
   return true;
 }
 
+// V's two columns (hi and lo, n rows each) are staged into shared memory (SV[4][n]) by cp.async
+// right after the column flags are acquired, so their L2 round trip overlaps the inner products,
+// the reduction and the rotation parameters (SV = nullptr: register-staged loads after them).
+__device__ __forceinline__ void cp_async16_l2(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+
 template <int NT, int RPT>
 __device__ __forceinline__ void jacobi_pair_df(float2* __restrict__ Bh, float2* __restrict__ Bl, long ldb, int m,
                                                int n, float2* __restrict__ Vh, float2* __restrict__ Vl, long ldv,
-                                               int p, int q, double tol, double smax, unsigned* __restrict__ count) {
+                                               int p, int q, double tol, double smax, unsigned* __restrict__ count,
+                                               float2* SV) {
   __shared__ float red[8][NT / 32];
   __shared__ DfParams P;
+  float2* const vcol[4] = {Vh + (long)p * ldv, Vl + (long)p * ldv, Vh + (long)q * ldv, Vl + (long)q * ldv};
+  if (SV) {
+    const int chunks = n / 2;  // 16-byte chunks per column (n even)
+#pragma unroll
+    for (int c = 0; c < 4; c++)
+      for (int h = threadIdx.x; h < chunks; h += NT) cp_async16_l2(SV + (long)c * n + 2 * h, vcol[c] + 2 * h);
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+  }
   float2 *bph = Bh + (long)p * ldb, *bpl = Bl + (long)p * ldb;
   float2 *bqh = Bh + (long)q * ldb, *bql = Bl + (long)q * ldb;
   const bool fits = m <= NT * RPT;
@@ -1050,7 +1068,10 @@ __device__ __forceinline__ void jacobi_pair_df(float2* __restrict__ Bh, float2* 
     if (l == 0) P.go = rotation_params_df(sa, sb, sgr, sgi, (float)tol, (float)smax, P) ? 1 : 0;
   }
   __syncthreads();
-  if (!P.go) return;
+  if (!P.go) {
+    if (SV) asm volatile("cp.async.wait_group 0;\n" ::: "memory");  // SV is refilled by the next pair
+    return;
+  }
   const dfl cd = P.c, srd = P.sr, sid = P.si;
   const bool small = P.tabs < 0x1p-24f;
   if (fits) {
@@ -1070,8 +1091,18 @@ __device__ __forceinline__ void jacobi_pair_df(float2* __restrict__ Bh, float2* 
     }
   }
   asm volatile("" ::: "memory");
-  df_rot_cols_staged<NT, RPT / 2>(Vh + (long)p * ldv, Vl + (long)p * ldv, Vh + (long)q * ldv, Vl + (long)q * ldv, n, cd,
-                              srd, sid, small);
+  if (SV) {
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    __syncthreads();  // rows were copied by other threads
+    for (int r = threadIdx.x; r < n; r += NT) {
+      float2 uh = SV[r], ul = SV[n + r], wh = SV[2 * n + r], wl = SV[3 * n + r];
+      if (small) df_rot_small(uh, ul, wh, wl, srd.h, sid.h);
+      else df_rot(uh, ul, wh, wl, cd, srd, sid);
+      __stcg(vcol[0] + r, uh); __stcg(vcol[1] + r, ul); __stcg(vcol[2] + r, wh); __stcg(vcol[3] + r, wl);
+    }
+  } else {
+    df_rot_cols_staged<NT, RPT / 2>(vcol[0], vcol[1], vcol[2], vcol[3], n, cd, srd, sid, small);
+  }
   if (threadIdx.x == 0) {
     atomicAdd(count, 1u);
     atomicMax(count + 1, __float_as_uint(P.tabs));
@@ -1087,6 +1118,10 @@ __global__ void __launch_bounds__(NT, 2) jacobi_sweep_df_k(float2* __restrict__ 
                                                         unsigned* __restrict__ state, int sweep,
                                                         unsigned* __restrict__ flags, int k0) {
   if (((volatile unsigned*)state)[0]) return;
+  extern __shared__ __align__(16) float2 df_sv[];
+  // the host allocates the staging buffer under exactly this condition (16-byte cp.async needs
+  // even columns; k <= 4096 keeps two CTAs per SM)
+  float2* SV = (n % 2 == 0 && ldv % 2 == 0 && n <= 4096) ? df_sv : nullptr;
   const double smax = smax_p[0] / smax_p[1];
   unsigned* cnt = state + 8 + 2 * sweep;
   const int npairs = np / 2;
@@ -1101,7 +1136,7 @@ __global__ void __launch_bounds__(NT, 2) jacobi_sweep_df_k(float2* __restrict__ 
     int p, q;
     pair_cols(np, round, pair, p, q);
     if (dataflow && !wait_cols(flags, p, q, n, base + round, state)) return;
-    if (q < n && p < k0) jacobi_pair_df<NT, RPT>(Bh, Bl, ldb, m, n, Vh, Vl, ldv, p, q, tol, smax, cnt);
+    if (q < n && p < k0) jacobi_pair_df<NT, RPT>(Bh, Bl, ldb, m, n, Vh, Vl, ldv, p, q, tol, smax, cnt, SV);
     if (dataflow) post_cols(flags, p, q, n, base + round + 1);
     else if (!grid_barrier(state + 2)) return;
   }
@@ -1372,13 +1407,19 @@ int jacobi_df(cudaStream_t s, SvdWork* w, float2* Bh, float2* Bl, long ldb, int 
   unsigned* state = w->cnt.as<unsigned>();
   unsigned* flags = state + nstate;
   QR_CUDA(cudaMemsetAsync(state, 0, sizeof(unsigned) * (nstate + np), s));
+  // V staging buffer: 4 columns (hi, lo of p and q) of k rows; k <= 4096 keeps two CTAs per SM
+  const size_t vsm = (k % 2 == 0 && ldv % 2 == 0 && k <= 4096) ? sizeof(float2) * 4 * (size_t)k : 0;
   static int per_sm = 0, sms = 0;
-  if (per_sm == 0) {
+  static size_t vsm_cached = (size_t)-1;
+  if (vsm != vsm_cached) {
     int dev = 0;
     QR_CUDA(cudaGetDevice(&dev));
     QR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    QR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, jacobi_sweep_df_k<NT, RPT>, NT, 0));
+    QR_CUDA(cudaFuncSetAttribute(jacobi_sweep_df_k<NT, RPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)sizeof(float2) * 4 * 4096));
+    QR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, jacobi_sweep_df_k<NT, RPT>, NT, vsm));
     if (per_sm < 1) return fail(QR_ECUDA, "double-float sweep kernel cannot be resident");
+    vsm_cached = vsm;
   }
   int grid = std::min(per_sm * sms, np / 2);
   if (grid < 1) grid = 1;
@@ -1393,7 +1434,7 @@ int jacobi_df(cudaStream_t s, SvdWork* w, float2* Bh, float2* Bl, long ldb, int 
     unsigned* fl = flags;
     int kz = k0;
     void* args[] = {&a1, &a2, &l1, &mm, &kk, &a3, &a4, &l2, &npp, &tl, &sm, &st, &sw, &fl, &kz};
-    QR_CUDA(cudaLaunchCooperativeKernel((const void*)jacobi_sweep_df_k<NT, RPT>, dim3(grid), dim3(NT), args, 0, s));
+    QR_CUDA(cudaLaunchCooperativeKernel((const void*)jacobi_sweep_df_k<NT, RPT>, dim3(grid), dim3(NT), args, vsm, s));
     count_launch();
   }
   prof_end(s, pr);
