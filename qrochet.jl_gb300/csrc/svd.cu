@@ -780,11 +780,11 @@ __global__ void __launch_bounds__(JB_NT, 1)
 
 size_t jb_smem_bytes(int m) { return ((sizeof(JbShared) + 15) & ~(size_t)15) + sizeof(float2) * (size_t)JB_C * m; }
 
-// Small problems (k <= 128 columns): the whole Jacobi iteration in one thread-block cluster of
-// up to 16 CTAs.  Each warp owns a pair of the round (1-4 warps per CTA, so a round's FP64 work
-// spreads over as many SMs as the cluster allows), the hardware cluster
-// barrier separates rounds, and sweeps repeat inside the kernel until one rotates nothing (FP64:
-// or rotates by less than 1e-8).  Cluster CTAs are co-scheduled by the hardware, so the barrier
+// Small problems (k <= 128 columns): the whole Jacobi iteration in one thread-block cluster of up
+// to 16 CTAs.  Each warp owns a pair of the round (1-4 warps per CTA, so a round's work spreads
+// over as many SMs as the cluster allows), the hardware
+// cluster barrier separates rounds, and sweeps repeat inside the kernel until one rotates nothing
+// or rotates by less than tan_stop.  Cluster CTAs are co-scheduled by the hardware, so the barrier
 // needs no co-residency argument; column reads go to L2 (ld.global.cg) so a CTA always sees the
 // rotations other CTAs made in the previous round.  state[0] = converged, state[1] = sweeps,
 // state[8 + s] = rotations of sweep s (global counters, shared by the cluster).
@@ -797,7 +797,7 @@ template <typename T>
 __global__ void __launch_bounds__(128) jacobi_cluster_k(cplx_t<T>* __restrict__ B, long ldb, int m, int n,
                                                         cplx_t<T>* __restrict__ V, long ldv, T tol,
                                                         const double* __restrict__ smax_p, int max_sweeps,
-                                                        unsigned* __restrict__ state) {
+                                                        unsigned* __restrict__ state, float tan_stop) {
   using C = cplx_t<T>;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpc = blockDim.x >> 5;
   const int gw = blockIdx.x * wpc + warp, nw = gridDim.x * wpc;
@@ -851,7 +851,7 @@ __global__ void __launch_bounds__(128) jacobi_cluster_k(cplx_t<T>* __restrict__ 
     }
     const unsigned h = __ldcg(cnt);
     const float tmax = __uint_as_float(__ldcg(cnt + 1));
-    conv = h == 0 || (sizeof(T) == 8 && tmax < 1e-8f);
+    conv = h == 0 || tmax < tan_stop;
     cluster_sync_all();  // everyone has read this sweep's counters
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -1270,13 +1270,13 @@ int jacobi(cudaStream_t s, SvdWork* w, cplx_t<T>* B, long ldb, int rows, int k, 
     QR_CHECK_LAUNCH("pow2_scale_k");
   }
   int pr = prof_begin(s, kind, 0.0, 0.0);
-  const bool small = k <= 128;
+  const bool small = k <= 128;  // (at 256 columns the FP32 block kernel is 2x faster than the cluster)
   if (small) {
     // one cluster of up to 16 CTAs with one warp per pair of a round: as many CTAs as pairs (up
     // to 16), then 2-4 warps per CTA
     const int npairs = np / 2 > 0 ? np / 2 : 1;
     const int cl = npairs < 16 ? npairs : 16;
-    const int wpc = (npairs + cl - 1) / cl;
+    const int wpc = std::min(4, (npairs + cl - 1) / cl);  // __launch_bounds__(128): warps loop over pairs
     static bool nonportable_set[2] = {false, false};
     if (cl > 8 && !nonportable_set[sizeof(T) == 8]) {
       QR_CUDA(cudaFuncSetAttribute(jacobi_cluster_k<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
@@ -1295,7 +1295,7 @@ int jacobi(cudaStream_t s, SvdWork* w, cplx_t<T>* B, long ldb, int rows, int k, 
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     QR_CUDA(cudaLaunchKernelEx(&cfg, jacobi_cluster_k<T>, B, ldb, rows, k, V, ldv, tol, (const double*)smax_d,
-                               max_sweeps, state));
+                               max_sweeps, state, tan_stop));
     count_launch();
   } else if (sizeof(T) == 4 && rows <= JB_MAXROWS && rows % 2 == 0 && ldb % 2 == 0) {
     // FP32 with the rows in shared memory: block Jacobi (JB_W-column blocks, pairs of blocks)
@@ -1482,6 +1482,8 @@ static int reorthonormalize(cudaStream_t s, SvdWork* w, double2* L, long ldl, in
 // sweeps only turn near-degenerate pairs that FP32 cannot separate and the double-float polish
 // turns again in its first sweep.
 constexpr float kPrecondTanStop = 0.15f;
+// Smallest block (columns) that takes the mixed path; below it the FP64 cluster Jacobi is as fast.
+constexpr int kMixedMinCols = 16;
 
 int zsvd_thin(cudaStream_t s, SvdWork* w, int mode, const double2* A, int m, int n, long lda,
               double2* U, long ldu, double* S, double2* Vh, long ldvh, int keep) {
@@ -1508,10 +1510,9 @@ int zsvd_thin(cudaStream_t s, SvdWork* w, int mode, const double2* A, int m, int
     QR_TRY(ztranspose(s, A, lda, m, n, B, rows, 1));
   }
 
-  // The FP32-preconditioned path pays off only for larger blocks: below k = 128 its DMMA
-  // Newton-Schulz GEMMs run on a handful of SMs at the per-SM FP64 rate and cost more than the
-  // FP64 sweeps they replace, so small blocks take the FP64 Jacobi directly (same accuracy).
-  if (mode == QR_FP64 || k <= 128) {
+  // The FP32-preconditioned path pays off above a few dozen columns; tiny blocks take the FP64
+  // Jacobi directly (same accuracy).
+  if (mode == QR_FP64 || k <= kMixedMinCols) {
     QR_TRY(zset_identity(s, V, k, k, k));
     double tol = sqrt((double)rows) * Eps<double>::v;
     QR_TRY(jacobi<double>(s, w, B, rows, rows, k, V, k, 40, tol));
