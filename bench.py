@@ -131,10 +131,10 @@ class DevTimer:
 
 
 # DRAM bytes (read + write) per launch from one ncu capture of each kernel on a 1024 x 1024 mixed
-# SVD (profiles/jacobi_sweep_fp32_1024.md, jacobi_sweep_df_1024.md, zgemm_df_1024.md).  The
+# SVD (profiles/jacobi_block_sweep_fp32_1024.md, jacobi_sweep_df_1024.md, zgemm_df_1024.md).  The
 # sweeps' traffic is the first touch of B and V and the GEMM's the first touch of its operands,
 # so it scales with the operand size: (k / 1024)^2 at k columns.
-NCU_TRAFFIC_1024 = {"jacobi_fp32": 16.821248e6 + 2.321920e6, "jacobi_df": 33.656064e6 + 7.758592e6,
+NCU_TRAFFIC_1024 = {"jacobi_fp32": 16.843776e6 + 256.0, "jacobi_df": 33.711360e6 + 28.087296e6,
                     "zgemm_df": 16.850432e6}
 
 
