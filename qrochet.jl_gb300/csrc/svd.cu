@@ -595,44 +595,144 @@ __device__ __forceinline__ bool rotation_params_f32(float a, float b, float gr, 
   return true;
 }
 
-// ---- block Jacobi sweep (FP32 preconditioner) ------------------------------------------------
-// The k columns form blocks of JB_W; a work item is a pair of blocks.  Its 2 JB_W columns of B are
-// staged once in shared memory (cp.async, L2 only), every pair among them is rotated there by one
-// group of four warps per pair (the two columns in registers between the inner products and the
-// rotation), the 8 x 8 product J of the rotations is accumulated, and V's columns are updated once
-// as V[:, cols] <- V[:, cols] J.  Per sweep this moves each column through L2 (nb - 1) times
-// instead of (k - 1) times and synchronises (nb - 1) rounds instead of (k - 1).  Block rounds use
-// the same ordering as the scalar sweep (per-block flags or the grid barrier).
-constexpr int JB_W = 4, JB_C = 2 * JB_W, JB_NT = 512, JB_GROUPS = JB_NT / 128, JB_RPT = 16;
-constexpr int JB_MAXROWS = 128 * JB_RPT;  // 2048
+// ---- block Jacobi sweep (FP32 preconditioner, rows <= 2048) ------------------------------------
+// The k columns form blocks of JR_W = 4; a work item is a pair of blocks.  Each of the 512 threads
+// holds 4 rows of the item's 8 columns in registers, so a local round moves no column data
+// through memory: the four pairs' inner products come from registers, one transposed butterfly
+// reduces the 16 sums per warp, lanes 0-3 of warp 0 form the four rotations in parallel, and
+// every thread rotates its rows in place.  Round 0 of a sweep (where every block appears once)
+// takes all 28 pairs of the 8 columns (7 local rounds); later rounds take the 16 cross pairs (4
+// local rounds), so every pair is met once per sweep.  The 8 x 8 product J of the rotations is
+// accumulated in shared memory and V's 8 columns are updated once as V[:, cols] <- V[:, cols] J.
+// Per sweep each column moves through L2 (nb - 1) times instead of (k - 1) times and (nb - 1)
+// rounds are synchronised instead of (k - 1), with the same two orderings as the scalar sweep
+// (per-block flags or the grid barrier).  Pair indices are compile-time constants (unrolled local
+// rounds), so the column arrays stay in registers.
+constexpr int JR_NT = 512, JR_RPT = 4, JR_C = 8, JR_W = 4;
+constexpr int JR_MAXROWS = JR_NT * JR_RPT;  // 2048
 
-struct JbShared {
-  float red[JB_GROUPS][4][4];
-  RotParams<float> P[JB_GROUPS];
-  float2 J[JB_C][JB_C];  // J[col][row]
-  int col[JB_C];         // global column of each local column (-1: absent)
+__host__ __device__ constexpr int jr_p(bool full, int ir, int g) {
+  return full ? (g == 0 ? ir : ((ir + g) % 7 < (ir - g + 7) % 7 ? (ir + g) % 7 : (ir - g + 7) % 7)) : g;
+}
+__host__ __device__ constexpr int jr_q(bool full, int ir, int g) {
+  return full ? (g == 0 ? 7 : ((ir + g) % 7 > (ir - g + 7) % 7 ? (ir + g) % 7 : (ir - g + 7) % 7))
+              : JR_W + (g + ir) % JR_W;
+}
+
+struct JrShared {
+  float red[16][JR_NT / 32];
+  RotParams<float> P[4];
+  float2 J[JR_C][JR_C];  // J[col][row]
+  int col[JR_C];
   int rotated;
 };
 
-__device__ __forceinline__ void cp_async16_cg(void* smem, const void* gmem) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+// Warp sum of 16 values by a transposed butterfly: afterwards lanes 2v and 2v + 1 hold the warp
+// total of value v (v = 0..15).
+__device__ __forceinline__ float jr_warp_sum16(float (&v)[16]) {
+  const int l = threadIdx.x & 31;
+  float a8[8], a4[4], a2[2];
+  const bool h16 = l & 16, h8 = l & 8, h4 = l & 4, h2 = l & 2;
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    const float keep = h16 ? v[8 + i] : v[i], send = h16 ? v[i] : v[8 + i];
+    a8[i] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+  }
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const float keep = h8 ? a8[4 + i] : a8[i], send = h8 ? a8[i] : a8[4 + i];
+    a4[i] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+  }
+#pragma unroll
+  for (int i = 0; i < 2; i++) {
+    const float keep = h4 ? a4[2 + i] : a4[i], send = h4 ? a4[i] : a4[2 + i];
+    a2[i] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+  }
+  float a1 = h2 ? a2[1] : a2[0];
+  a1 += __shfl_xor_sync(0xffffffffu, h2 ? a2[0] : a2[1], 2);
+  a1 += __shfl_xor_sync(0xffffffffu, a1, 1);
+  return a1;  // value index ((l >> 4) & 1) * 8 + ((l >> 3) & 1) * 4 + ((l >> 2) & 1) * 2 + ((l >> 1) & 1)
 }
 
-__global__ void __launch_bounds__(JB_NT, 1)
-    jacobi_block_sweep_k(float2* __restrict__ B, long ldb, int m, int n, float2* __restrict__ V, long ldv,
-                         int nbp, float tol, const double* __restrict__ smax_p, unsigned* __restrict__ state,
-                         int sweep, unsigned* __restrict__ flags, float tan_stop) {
-  extern __shared__ __align__(16) unsigned char jb_raw[];
-  JbShared& sh = *reinterpret_cast<JbShared*>(jb_raw);
-  float2* S = reinterpret_cast<float2*>(jb_raw + ((sizeof(JbShared) + 15) & ~(size_t)15));  // S[l * m + r]
+template <bool FULL, int IR>
+__device__ __forceinline__ void jr_local_round(float2 (&x)[JR_C][JR_RPT], JrShared& sh, float tol, float smax,
+                                               unsigned* cnt) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  float v[16];
+#pragma unroll
+  for (int g = 0; g < 4; g++) {
+    constexpr int dummy = 0;
+    (void)dummy;
+    const int p = jr_p(FULL, IR, g), q = jr_q(FULL, IR, g);
+    float a = 0.f, b = 0.f, gr = 0.f, gi = 0.f;
+#pragma unroll
+    for (int j = 0; j < JR_RPT; j++) {
+      const float2 xx = x[p][j], yy = x[q][j];
+      a += xx.x * xx.x + xx.y * xx.y;
+      b += yy.x * yy.x + yy.y * yy.y;
+      gr += xx.x * yy.x + xx.y * yy.y;
+      gi += xx.x * yy.y - xx.y * yy.x;
+    }
+    v[4 * g] = a; v[4 * g + 1] = b; v[4 * g + 2] = gr; v[4 * g + 3] = gi;
+  }
+  const float k = jr_warp_sum16(v);
+  if ((lane & 1) == 0) {
+    const int vi = ((lane >> 4) & 1) * 8 + ((lane >> 3) & 1) * 4 + ((lane >> 2) & 1) * 2 + ((lane >> 1) & 1);
+    sh.red[vi][warp] = k;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    float tot = 0.f;
+    if (lane < 16) {
+#pragma unroll
+      for (int w = 0; w < JR_NT / 32; w++) tot += sh.red[lane][w];
+    }
+    const int g = lane & 3;
+    const float sa = __shfl_sync(0xffffffffu, tot, 4 * g), sb = __shfl_sync(0xffffffffu, tot, 4 * g + 1);
+    const float sgr = __shfl_sync(0xffffffffu, tot, 4 * g + 2), sgi = __shfl_sync(0xffffffffu, tot, 4 * g + 3);
+    if (lane < 4) {
+      const int p = jr_p(FULL, IR, lane), q = jr_q(FULL, IR, lane);
+      float c = 1.f, sr = 0.f, si = 0.f, tabs = 0.f;
+      const bool live = sh.col[p] >= 0 && sh.col[q] >= 0;
+      const bool go = live && rotation_params_f32(sa, sb, sgr, sgi, tol, smax, c, sr, si, tabs);
+      sh.P[lane].c = c; sh.P[lane].sr = sr; sh.P[lane].si = si; sh.P[lane].tabs = tabs; sh.P[lane].go = go ? 1 : 0;
+      if (go) {
+        atomicAdd(cnt, 1u);
+        atomicMax(cnt + 1, __float_as_uint(tabs));
+        sh.rotated = 1;
+      }
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int g = 0; g < 4; g++) {
+    const int p = jr_p(FULL, IR, g), q = jr_q(FULL, IR, g);
+    if (sh.P[g].go) {
+      const float c = sh.P[g].c, sr = sh.P[g].sr, si = sh.P[g].si;
+#pragma unroll
+      for (int j = 0; j < JR_RPT; j++) rot(x[p][j], x[q][j], c, sr, si);
+      if (tid < JR_C) {  // columns p, q of J, row tid (J is read only after a later barrier)
+        float2 u = sh.J[p][tid], w = sh.J[q][tid];
+        rot(u, w, c, sr, si);
+        sh.J[p][tid] = u;
+        sh.J[q][tid] = w;
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(JR_NT, 1)
+    jacobi_block_reg_k(float2* __restrict__ B, long ldb, int m, int n, float2* __restrict__ V, long ldv, int nbp,
+                       float tol, const double* __restrict__ smax_p, unsigned* __restrict__ state, int sweep,
+                       unsigned* __restrict__ flags, float tan_stop) {
+  __shared__ JrShared sh;
   if (((volatile unsigned*)state)[0]) return;
   const float smax = (float)(smax_p[0] / smax_p[1]);
   unsigned* cnt = state + 8 + 2 * sweep;
-  const int nb = (n + JB_W - 1) / JB_W;
+  const int nb = (n + JR_W - 1) / JR_W;
   const int npairs = nbp / 2;
   const unsigned base = (unsigned)sweep * (unsigned)(nbp - 1);
-  const int tid = threadIdx.x, g = tid >> 7, tg = tid & 127, wg = (tid >> 5) & 3, lane = tid & 31;
+  const int tid = threadIdx.x;
   const bool dataflow = npairs > (int)gridDim.x;
   const long nit = dataflow ? ((long)(nbp - 1) * npairs - blockIdx.x + gridDim.x - 1) / gridDim.x : (long)(nbp - 1);
   for (long t = 0; t < nit; t++) {
@@ -642,126 +742,74 @@ __global__ void __launch_bounds__(JB_NT, 1)
     pair_cols(nbp, round, pair, bp, bq);
     if (dataflow && !wait_cols(flags, bp, bq, nb, base + round, state)) return;
     if (bp < nb) {
-      // ---- stage the block pair's columns
-      if (tid < JB_C) {
-        const int blk = tid < JB_W ? bp : bq, c = blk * JB_W + (tid % JB_W);
+      if (tid < JR_C) {
+        const int blk = tid < JR_W ? bp : bq, c = blk * JR_W + (tid % JR_W);
         sh.col[tid] = (blk < nb && c < n) ? c : -1;
       }
-      if (tid < JB_C * JB_C) sh.J[tid / JB_C][tid % JB_C] = make_float2((tid / JB_C) == (tid % JB_C) ? 1.f : 0.f, 0.f);
+      if (tid < JR_C * JR_C) sh.J[tid / JR_C][tid % JR_C] = make_float2((tid / JR_C) == (tid % JR_C) ? 1.f : 0.f, 0.f);
       if (tid == 0) sh.rotated = 0;
       __syncthreads();
-      const int chunks = m / 2;  // 16-byte chunks per column (m even)
-      for (int l = 0; l < JB_C; l++) {
+      float2 x[JR_C][JR_RPT];
+#pragma unroll
+      for (int l = 0; l < JR_C; l++) {
         const int c = sh.col[l];
-        if (c < 0) continue;
-        const float2* src = B + (long)c * ldb;
-        for (int h = tid; h < chunks; h += JB_NT) cp_async16_cg(S + (long)l * m + 2 * h, src + 2 * h);
-      }
-      asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
-      __syncthreads();
-      // ---- pairs among the 2 JB_W local columns, one group of four warps per pair.  Round 0 of a
-      // sweep (where every block appears once) takes all pairs, including those inside each
-      // block; later rounds take the JB_W^2 cross pairs only, so every pair is met once a sweep.
-      const int nlr = round == 0 ? JB_C - 1 : JB_W;
-      for (int ir = 0; ir < nlr; ir++) {
-        int lp, lq;
-        if (round == 0) pair_cols(JB_C, ir, g, lp, lq);
-        else { lp = g; lq = JB_W + (g + ir) % JB_W; }
-        const int cp_ = sh.col[lp], cq_ = sh.col[lq];
-        const bool live = cp_ >= 0 && cq_ >= 0;  // uniform across the group
-        float2 x[JB_RPT], y[JB_RPT];
-        float a = 0.f, b = 0.f, gr = 0.f, gi = 0.f;
-        if (live) {
-          const float2* sp = S + (long)lp * m;
-          const float2* sq = S + (long)lq * m;
 #pragma unroll
-          for (int j = 0; j < JB_RPT; j++) {
-            const int r = tg + 128 * j;
-            if (r < m) { x[j] = sp[r]; y[j] = sq[r]; }
-            else { x[j] = y[j] = make_float2(0.f, 0.f); }
-            a += x[j].x * x[j].x + x[j].y * x[j].y;
-            b += y[j].x * y[j].x + y[j].y * y[j].y;
-            gr += x[j].x * y[j].x + x[j].y * y[j].y;
-            gi += x[j].x * y[j].y - x[j].y * y[j].x;
-          }
-          const float kk = warp_sum4_t<float>(a, b, gr, gi);
-          if ((lane & 7) == 0) sh.red[g][lane >> 3][wg] = kk;
+        for (int j = 0; j < JR_RPT; j++) {
+          const int r = tid + JR_NT * j;
+          x[l][j] = (c >= 0 && r < m) ? __ldcg(B + (long)c * ldb + r) : make_float2(0.f, 0.f);
         }
-        asm volatile("bar.sync %0, 128;" ::"r"(1 + g) : "memory");
-        if (live && wg == 0) {
-          float v = 0.f;
-          if (lane < 4) v = sh.red[g][lane][0] + sh.red[g][lane][1] + sh.red[g][lane][2] + sh.red[g][lane][3];
-          const float sa = __shfl_sync(0xffffffffu, v, 0), sb = __shfl_sync(0xffffffffu, v, 1);
-          const float sgr = __shfl_sync(0xffffffffu, v, 2), sgi = __shfl_sync(0xffffffffu, v, 3);
-          if (lane == 0) {
-            float c, sr, si, tabs = 0.f;
-            const bool go = rotation_params_f32(sa, sb, sgr, sgi, tol, smax, c, sr, si, tabs);
-            sh.P[g].c = c; sh.P[g].sr = sr; sh.P[g].si = si; sh.P[g].tabs = tabs; sh.P[g].go = go ? 1 : 0;
-          }
-        }
-        asm volatile("bar.sync %0, 128;" ::"r"(1 + g) : "memory");
-        if (live && sh.P[g].go) {
-          const float c = sh.P[g].c, sr = sh.P[g].sr, si = sh.P[g].si;
-          float2* sp = S + (long)lp * m;
-          float2* sq = S + (long)lq * m;
-#pragma unroll
-          for (int j = 0; j < JB_RPT; j++) {
-            const int r = tg + 128 * j;
-            if (r < m) {
-              rot(x[j], y[j], c, sr, si);
-              sp[r] = x[j];
-              sq[r] = y[j];
-            }
-          }
-          if (tg < JB_C) {  // columns lp, lq of J, row tg
-            float2 u = sh.J[lp][tg], w = sh.J[lq][tg];
-            rot(u, w, c, sr, si);
-            sh.J[lp][tg] = u;
-            sh.J[lq][tg] = w;
-          }
-          if (tg == 0) {
-            atomicAdd(cnt, 1u);
-            atomicMax(cnt + 1, __float_as_uint(sh.P[g].tabs));
-            sh.rotated = 1;
-          }
-        }
-        __syncthreads();  // the next local round pairs columns across groups
       }
-      // ---- write back B and apply J to V (only if anything rotated)
+      if (round == 0) {
+        jr_local_round<true, 0>(x, sh, tol, smax, cnt);
+        jr_local_round<true, 1>(x, sh, tol, smax, cnt);
+        jr_local_round<true, 2>(x, sh, tol, smax, cnt);
+        jr_local_round<true, 3>(x, sh, tol, smax, cnt);
+        jr_local_round<true, 4>(x, sh, tol, smax, cnt);
+        jr_local_round<true, 5>(x, sh, tol, smax, cnt);
+        jr_local_round<true, 6>(x, sh, tol, smax, cnt);
+      } else {
+        jr_local_round<false, 0>(x, sh, tol, smax, cnt);
+        jr_local_round<false, 1>(x, sh, tol, smax, cnt);
+        jr_local_round<false, 2>(x, sh, tol, smax, cnt);
+        jr_local_round<false, 3>(x, sh, tol, smax, cnt);
+      }
+      __syncthreads();  // J and the rotated flag are final
       if (sh.rotated) {
-        for (int l = 0; l < JB_C; l++) {
+#pragma unroll
+        for (int l = 0; l < JR_C; l++) {
           const int c = sh.col[l];
           if (c < 0) continue;
-          float4* dst = reinterpret_cast<float4*>(B + (long)c * ldb);
-          const float4* sv = reinterpret_cast<const float4*>(S + (long)l * m);
-          for (int h = tid; h < chunks; h += JB_NT) __stcg(dst + h, sv[h]);
+#pragma unroll
+          for (int j = 0; j < JR_RPT; j++) {
+            const int r = tid + JR_NT * j;
+            if (r < m) __stcg(B + (long)c * ldb + r, x[l][j]);
+          }
         }
-        // two rows per thread per pass: all 16 loads are in flight before the first store
-        for (int r0 = tid; r0 < n; r0 += 2 * JB_NT) {
-          float2 vin[2][JB_C];
+        for (int r0 = tid; r0 < n; r0 += 2 * JR_NT) {
+          float2 vin[2][JR_C];
 #pragma unroll
           for (int h = 0; h < 2; h++) {
-            const int r = r0 + h * JB_NT;
+            const int r = r0 + h * JR_NT;
 #pragma unroll
-            for (int l = 0; l < JB_C; l++) {
+            for (int l = 0; l < JR_C; l++) {
               const int c = sh.col[l];
               vin[h][l] = (c >= 0 && r < n) ? __ldcg(V + (long)c * ldv + r) : make_float2(0.f, 0.f);
             }
           }
 #pragma unroll
           for (int h = 0; h < 2; h++) {
-            const int r = r0 + h * JB_NT;
+            const int r = r0 + h * JR_NT;
             if (r >= n) continue;
 #pragma unroll
-            for (int l2 = 0; l2 < JB_C; l2++) {
+            for (int l2 = 0; l2 < JR_C; l2++) {
               const int c = sh.col[l2];
               if (c < 0) continue;
               float2 o = make_float2(0.f, 0.f);
 #pragma unroll
-              for (int l = 0; l < JB_C; l++) {
-                const float2 j = sh.J[l2][l];
-                o.x += vin[h][l].x * j.x - vin[h][l].y * j.y;
-                o.y += vin[h][l].x * j.y + vin[h][l].y * j.x;
+              for (int l = 0; l < JR_C; l++) {
+                const float2 jv = sh.J[l2][l];
+                o.x += vin[h][l].x * jv.x - vin[h][l].y * jv.y;
+                o.y += vin[h][l].x * jv.y + vin[h][l].y * jv.x;
               }
               __stcg(V + (long)c * ldv + r, o);
             }
@@ -778,7 +826,6 @@ __global__ void __launch_bounds__(JB_NT, 1)
   finish_sweep(state, cnt, sweep, tan_stop);
 }
 
-size_t jb_smem_bytes(int m) { return ((sizeof(JbShared) + 15) & ~(size_t)15) + sizeof(float2) * (size_t)JB_C * m; }
 
 // Small problems (k <= 128 columns): the whole Jacobi iteration in one thread-block cluster of up
 // to 16 CTAs.  Each warp owns a pair of the round (1-4 warps per CTA, so a round's work spreads
@@ -1297,21 +1344,15 @@ int jacobi(cudaStream_t s, SvdWork* w, cplx_t<T>* B, long ldb, int rows, int k, 
     QR_CUDA(cudaLaunchKernelEx(&cfg, jacobi_cluster_k<T>, B, ldb, rows, k, V, ldv, tol, (const double*)smax_d,
                                max_sweeps, state, tan_stop));
     count_launch();
-  } else if (sizeof(T) == 4 && rows <= JB_MAXROWS && rows % 2 == 0 && ldb % 2 == 0) {
-    // FP32 with the rows in shared memory: block Jacobi (JB_W-column blocks, pairs of blocks)
-    const int nb = (k + JB_W - 1) / JB_W, nbp = nb + (nb & 1);
-    const size_t smem = jb_smem_bytes(rows);
-    static size_t smem_set = 0;
+  } else if (sizeof(T) == 4 && rows <= JR_MAXROWS) {
+    // FP32 with the rows in registers: block Jacobi (4-column blocks, pairs of blocks)
+    const int nb = (k + JR_W - 1) / JR_W, nbp = nb + (nb & 1);
     static int per_sm = 0, sms = 0;
-    if (smem > smem_set) {
-      QR_CUDA(cudaFuncSetAttribute(jacobi_block_sweep_k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)jb_smem_bytes(JB_MAXROWS)));
-      smem_set = jb_smem_bytes(JB_MAXROWS);
+    if (per_sm == 0) {
       int dev = 0;
       QR_CUDA(cudaGetDevice(&dev));
       QR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-      QR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, jacobi_block_sweep_k, JB_NT,
-                                                            jb_smem_bytes(JB_MAXROWS)));
+      QR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, jacobi_block_reg_k, JR_NT, 0));
       if (per_sm < 1) return fail(QR_ECUDA, "block Jacobi sweep kernel cannot be resident");
     }
     int grid = std::min(per_sm * sms, nbp / 2);
@@ -1326,7 +1367,7 @@ int jacobi(cudaStream_t s, SvdWork* w, cplx_t<T>* B, long ldb, int rows, int k, 
       unsigned* st = state;
       unsigned* fl = flags;
       void* args[] = {&Bp, &ldbb, &mm, &kk2, &Vp, &ldvv, &nbb, &tl, &sm, &st, &sw, &fl, &ts};
-      QR_CUDA(cudaLaunchCooperativeKernel((const void*)jacobi_block_sweep_k, dim3(grid), dim3(JB_NT), args, smem, s));
+      QR_CUDA(cudaLaunchCooperativeKernel((const void*)jacobi_block_reg_k, dim3(grid), dim3(JR_NT), args, 0, s));
       count_launch();
     }
   } else {
