@@ -131,10 +131,10 @@ class DevTimer:
 
 
 # DRAM bytes (read + write) per launch from one ncu capture of each kernel on a 1024 x 1024 mixed
-# SVD (profiles/jacobi_block_sweep_fp32_1024.md, jacobi_sweep_df_1024.md, zgemm_df_1024.md).  The
+# SVD (profiles/jacobi_block_reg_fp32_1024.md, jacobi_sweep_df_1024.md, zgemm_df_1024.md).  The
 # sweeps' traffic is the first touch of B and V and the GEMM's the first touch of its operands,
 # so it scales with the operand size: (k / 1024)^2 at k columns.
-NCU_TRAFFIC_1024 = {"jacobi_fp32": 16.843776e6 + 256.0, "jacobi_df": 33.711360e6 + 28.087296e6,
+NCU_TRAFFIC_1024 = {"jacobi_fp32": 16.937472e6 + 15.872e3, "jacobi_df": 33.711360e6 + 28.087296e6,
                     "zgemm_df": 16.850432e6}
 
 
@@ -504,7 +504,7 @@ def run_ours(args, chi):
         line = {"metric": METRIC, "value": value, "unit": "gate-steps/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1e3 * dt_max / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None,
-                "dtype": "complex64 Jacobi preconditioner + double-float (FP32-pair) Newton-Schulz, B = A X and Jacobi polish; complex128 theta (FP64 DMMA)",
+                "dtype": "complex64 Jacobi preconditioner + double-float (FP32-pair) theta GEMM, Newton-Schulz, B = A X and Jacobi polish; complex128 gate and results",
                 "data": "synthetic",
                 "config": {"workload": f"tebd_gate_step_chi{chi}", "chi": chi, "theta": f"{2 * chi}x{2 * chi}",
                            "maxdim": maxdim, "threshold": CUTOFF, "n_sites": N_SITES, "precision": "mixed",

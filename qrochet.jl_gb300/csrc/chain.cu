@@ -342,6 +342,24 @@ int normalize_impl(qr_chain* h, int root) {
 }
 
 // ---- evolve_2site! (Chain.jl:606-661) + Vidal helpers (Chain.jl:669-722) ------------------------
+// theta (m x nn, FP64 result) = A_l diag(Lambda) A_r through the double-float GEMM
+int theta_df(qr_chain* h, int sl, int sr, int m, int nn, int cb, double2* th) {
+  cudaStream_t s = h->stream;
+  float2 *al = nullptr, *ar = nullptr, *tt = nullptr;
+  const size_t nal = (size_t)m * cb, nar = (size_t)cb * nn, ntt = (size_t)m * nn;
+  int rc = dalloc((void**)&al, sizeof(float2) * 2 * nal, s);
+  if (!rc) rc = dalloc((void**)&ar, sizeof(float2) * 2 * nar, s);
+  if (!rc) rc = dalloc((void**)&tt, sizeof(float2) * 2 * ntt, s);
+  if (!rc) rc = z2df_cols(s, h->site[sl], m, m, cb, h->lam[sl], al, al + nal, m);
+  if (!rc) rc = z2df_cols(s, h->site[sr], cb, cb, nn, nullptr, ar, ar + nar, cb);
+  if (!rc) rc = zgemm_df(s, DF_STORE, OP_N, m, nn, cb, al, al + nal, m, ar, ar + nar, cb, tt, tt + ntt, m);
+  if (!rc) rc = df2z(s, tt, tt + ntt, m, m, nn, nullptr, th, m);
+  if (al) cudaFreeAsync(al, s);
+  if (ar) cudaFreeAsync(ar, s);
+  if (tt) cudaFreeAsync(tt, s);
+  return rc;
+}
+
 int evolve2_impl(qr_chain* h, int sl, const double* g, double threshold, int maxdim, int iscanonical,
                  int renormalize) {
   if (!h) return fail(QR_EINVAL, "null chain");
@@ -364,7 +382,13 @@ int evolve2_impl(qr_chain* h, int sl, const double* g, double threshold, int max
   double* S = (double*)(th + (size_t)m * nn);
   const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
   // theta = A_l diag(Lambda) A_r  [(l,o1) x (o2,r)]
-  QR_TRY(zgemm(s, OP_N, OP_N, m, nn, cb, one, h->site[sl], m, 0, h->site[sr], cb, 0, zero, th, m, 0, 1, h->lam[sl]));
+  if (svd_mode(h) == QR_MIXED && k > 16) {
+    // The mixed SVD splits theta into double-float before B = A X, so theta is formed there
+    // directly: the double-float GEMM on the FP32 pipes (~2^-48 relative) instead of the FP64 one
+    QR_TRY(theta_df(h, sl, sr, m, nn, cb, th));
+  } else {
+    QR_TRY(zgemm(s, OP_N, OP_N, m, nn, cb, one, h->site[sl], m, 0, h->site[sr], cb, 0, zero, th, m, 0, 1, h->lam[sl]));
+  }
   QR_TRY(zgate2(s, th, cl, d, cr, h->gate));
   double2 *U = nullptr, *Vh = nullptr;
   QR_TRY(dalloc((void**)&U, sizeof(double2) * (size_t)m * k, s));

@@ -223,6 +223,21 @@ __global__ void to_df_scaled_k(const double2* __restrict__ src, long lds, int ro
   }
 }
 
+// hi/lo of src[:, j] * colscale[j] (the Lambda of a bond folded into a site's columns)
+__global__ void to_df_cols_k(const double2* __restrict__ src, long lds, int rows, int cols,
+                             const double* __restrict__ colscale, float2* __restrict__ hi, float2* __restrict__ lo,
+                             long ldd) {
+  const long total = (long)rows * cols;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+    const long i = t % rows, j = t / rows;
+    const double f = colscale ? colscale[j] : 1.0;
+    const double2 v = src[i + j * lds];
+    const dfl re = df_from(v.x * f), im = df_from(v.y * f);
+    hi[i + j * ldd] = make_float2(re.h, im.h);
+    lo[i + j * ldd] = make_float2(re.l, im.l);
+  }
+}
+
 __global__ void from_df_scaled_k(const float2* __restrict__ hi, const float2* __restrict__ lo, long lds, int rows,
                                  int cols, const double* __restrict__ scale, double2* __restrict__ dst, long ldd) {
   const double f = scale ? scale[0] : 1.0;
@@ -277,6 +292,14 @@ int z2df(cudaStream_t s, const double2* src, long lds, int rows, int cols, const
   if (rows <= 0 || cols <= 0) return QR_OK;
   to_df_scaled_k<<<grid_for((long)rows * cols), TPB, 0, s>>>(src, lds, rows, cols, scale, hi, lo, ldd);
   QR_CHECK_LAUNCH("to_df_scaled_k");
+  return QR_OK;
+}
+
+int z2df_cols(cudaStream_t s, const double2* src, long lds, int rows, int cols, const double* colscale, float2* hi,
+              float2* lo, long ldd) {
+  if (rows <= 0 || cols <= 0) return QR_OK;
+  to_df_cols_k<<<grid_for((long)rows * cols), TPB, 0, s>>>(src, lds, rows, cols, colscale, hi, lo, ldd);
+  QR_CHECK_LAUNCH("to_df_cols_k");
   return QR_OK;
 }
 

@@ -29,6 +29,9 @@ int z2df(cudaStream_t s, const double2* src, long lds, int rows, int cols, const
          float2* lo, long ldd);
 int df2z(cudaStream_t s, const float2* hi, const float2* lo, long lds, int rows, int cols, const double* scale,
          double2* dst, long ldd);
+// hi/lo of src with column j multiplied by colscale[j] (colscale may be null)
+int z2df_cols(cudaStream_t s, const double2* src, long lds, int rows, int cols, const double* colscale, float2* hi,
+              float2* lo, long ldd);
 
 // ---- random.cu: E (rows x N, ld rows) = scale * the Gram-Schmidt orthonormalised rows of a
 // uniform [0,1) random rows x N matrix (complex entries when cplx), from stream `stream` of `seed`
