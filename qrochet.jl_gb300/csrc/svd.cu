@@ -833,12 +833,17 @@ __global__ void __launch_bounds__(JR_NT, 1)
 // cluster barrier separates rounds, and sweeps repeat inside the kernel until one rotates nothing
 // or rotates by less than tan_stop.  Cluster CTAs are co-scheduled by the hardware, so the barrier
 // needs no co-residency argument; column reads go to L2 (ld.global.cg) so a CTA always sees the
-// rotations other CTAs made in the previous round.  state[0] = converged, state[1] = sweeps,
-// state[8 + s] = rotations of sweep s (global counters, shared by the cluster).
+// rotations other CTAs made in the previous round.  Up to 128 rows, a pair's rows of B and of V
+// are loaded into registers together at the start of the pair (4 rows per lane) and stay there
+// through the rotation, so a round costs one L2 round trip instead of three.  state[0] =
+// converged, state[1] = sweeps, state[8 + s] = rotations of sweep s (global counters, shared by
+// the cluster).
 __device__ __forceinline__ void cluster_sync_all() {
   asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
   asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
 }
+
+constexpr int CCR = 4;  // rows per lane held in registers by the cluster kernels (m <= 128)
 
 template <typename T>
 __global__ void __launch_bounds__(128) jacobi_cluster_k(cplx_t<T>* __restrict__ B, long ldb, int m, int n,
@@ -863,6 +868,53 @@ __global__ void __launch_bounds__(128) jacobi_cluster_k(cplx_t<T>* __restrict__ 
         if (p > q) { int t = p; p = q; q = t; }
         C* bp = B + (long)p * ldb;
         C* bq = B + (long)q * ldb;
+        C* vp = V + (long)p * ldv;
+        C* vq = V + (long)q * ldv;
+        if (m <= 32 * CCR) {
+          // rows in registers: one L2 round trip per round for B and V together
+          C x[CCR], y[CCR], u[CCR], w[CCR];
+#pragma unroll
+          for (int j = 0; j < CCR; j++) {
+            const int r = lane + 32 * j;
+            x[j].x = x[j].y = y[j].x = y[j].y = u[j].x = u[j].y = w[j].x = w[j].y = T(0);
+            if (r < m) { x[j] = __ldcg(bp + r); y[j] = __ldcg(bq + r); }
+            if (r < n) { u[j] = __ldcg(vp + r); w[j] = __ldcg(vq + r); }
+          }
+          T a = 0, b = 0, gr = 0, gi = 0;
+#pragma unroll
+          for (int j = 0; j < CCR; j++) {
+            if (32 * j >= m) break;  // warp-uniform: no arithmetic on padding rows
+            a += x[j].x * x[j].x + x[j].y * x[j].y;
+            b += y[j].x * y[j].x + y[j].y * y[j].y;
+            gr += x[j].x * y[j].x + x[j].y * y[j].y;
+            gi += x[j].x * y[j].y - x[j].y * y[j].x;
+          }
+          const T k4 = warp_sum4_t<T>(a, b, gr, gi);
+          a = __shfl_sync(0xffffffffu, k4, 0);
+          b = __shfl_sync(0xffffffffu, k4, 8);
+          gr = __shfl_sync(0xffffffffu, k4, 16);
+          gi = __shfl_sync(0xffffffffu, k4, 24);
+          T c, sr, si;
+          float tabs;
+          if (!rotation_params<T>(a, b, gr, gi, tol, smax, c, sr, si, tabs)) continue;
+#pragma unroll
+          for (int j = 0; j < CCR; j++) {
+            const int r = lane + 32 * j;
+            if (32 * j < m) {
+              rot(x[j], y[j], c, sr, si);
+              if (r < m) { __stcg(bp + r, x[j]); __stcg(bq + r, y[j]); }
+            }
+            if (32 * j < n) {
+              rot(u[j], w[j], c, sr, si);
+              if (r < n) { __stcg(vp + r, u[j]); __stcg(vq + r, w[j]); }
+            }
+          }
+          if (lane == 0) {
+            atomicAdd(cnt, 1u);
+            atomicMax(cnt + 1, __float_as_uint(tabs));
+          }
+          continue;
+        }
         T a = 0, b = 0, gr = 0, gi = 0;
         for (int r = lane; r < m; r += 32) {
           C x = __ldcg(bp + r), y = __ldcg(bq + r);
@@ -881,8 +933,6 @@ __global__ void __launch_bounds__(128) jacobi_cluster_k(cplx_t<T>* __restrict__ 
           __stcg(bp + r, x);
           __stcg(bq + r, y);
         }
-        C* vp = V + (long)p * ldv;
-        C* vq = V + (long)q * ldv;
         for (int r = lane; r < n; r += 32) {
           C x = __ldcg(vp + r), y = __ldcg(vq + r);
           rot(x, y, c, sr, si);
@@ -1158,6 +1208,86 @@ __device__ __forceinline__ void jacobi_pair_df(float2* __restrict__ Bh, float2* 
 
 // One polish sweep in double-float, convergence decided on the device (state layout as in
 // jacobi_sweep_dev_k; sigma_max of the pre-scaled columns is smax_p[0] / smax_p[1]).
+// Double-float polish for k <= 128 columns of at most 128 rows: the whole iteration in one
+// thread-block cluster, laid out as jacobi_cluster_k (one warp per pair of a round, the hardware
+// cluster barrier between rounds, all sweeps in one launch).  A pair's rows of B and V (hi and lo,
+// 4 rows per lane) are loaded together and stay in registers through the rotation; every lane
+// forms the same rotation parameters from the broadcast double-float sums, so a pair needs no
+// shared memory and no CTA barrier.  Pairs with both columns at or beyond k0 are skipped, and the
+// iteration stops after a sweep that rotates nothing or whose largest tangent is below tan_stop.
+// state as in jacobi_cluster_k.
+__global__ void __launch_bounds__(128) jacobi_cluster_df_k(float2* __restrict__ Bh, float2* __restrict__ Bl,
+                                                           long ldb, int m, int n, float2* __restrict__ Vh,
+                                                           float2* __restrict__ Vl, long ldv, float tol,
+                                                           const double* __restrict__ smax_p, int max_sweeps,
+                                                           unsigned* __restrict__ state, int k0, float tan_stop) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpc = blockDim.x >> 5;
+  const int gw = blockIdx.x * wpc + warp, nw = gridDim.x * wpc;
+  const int np = n + (n & 1), npairs = np / 2;
+  const float smax = (float)(smax_p[0] / smax_p[1]);
+  int sweep = 0;
+  bool conv = false;
+  for (; sweep < max_sweeps && !conv; sweep++) {
+    unsigned* cnt = state + 8 + 2 * sweep;
+    for (int round = 0; round < np - 1; round++) {
+      for (int pair = gw; pair < npairs; pair += nw) {
+        int p, q;
+        pair_cols(np, round, pair, p, q);
+        if (q >= n || p >= k0) continue;
+        float2 *bph = Bh + (long)p * ldb, *bpl = Bl + (long)p * ldb;
+        float2 *bqh = Bh + (long)q * ldb, *bql = Bl + (long)q * ldb;
+        float2 *vph = Vh + (long)p * ldv, *vpl = Vl + (long)p * ldv;
+        float2 *vqh = Vh + (long)q * ldv, *vql = Vl + (long)q * ldv;
+        float2 xh[CCR], xl[CCR], yh[CCR], yl[CCR], uh[CCR], ul[CCR], wh[CCR], wl[CCR];
+#pragma unroll
+        for (int j = 0; j < CCR; j++) {
+          const int r = lane + 32 * j;
+          const float2 z = make_float2(0.f, 0.f);
+          xh[j] = xl[j] = yh[j] = yl[j] = uh[j] = ul[j] = wh[j] = wl[j] = z;
+          if (r < m) { xh[j] = __ldcg(bph + r); xl[j] = __ldcg(bpl + r); yh[j] = __ldcg(bqh + r); yl[j] = __ldcg(bql + r); }
+          if (r < n) { uh[j] = __ldcg(vph + r); ul[j] = __ldcg(vpl + r); wh[j] = __ldcg(vqh + r); wl[j] = __ldcg(vql + r); }
+        }
+        DotAcc a{0.f, 0.f}, b{0.f, 0.f}, gr{0.f, 0.f}, gi{0.f, 0.f};
+#pragma unroll
+        for (int j = 0; j < CCR; j++)
+          if (32 * j < m) df_dot_acc(xh[j], xl[j], yh[j], yl[j], a, b, gr, gi);  // warp-uniform test
+        const dfl k4 = df_warp_sum4_t(dot_final(a), dot_final(b), dot_final(gr), dot_final(gi));
+        DfParams P;
+        if (!rotation_params_df(df_shfl(k4, 0), df_shfl(k4, 8), df_shfl(k4, 16), df_shfl(k4, 24), tol, smax, P))
+          continue;
+        const bool small = P.tabs < 0x1p-24f;
+#pragma unroll
+        for (int j = 0; j < CCR; j++) {
+          const int r = lane + 32 * j;
+          if (32 * j < m) {
+            if (small) df_rot_small(xh[j], xl[j], yh[j], yl[j], P.sr.h, P.si.h);
+            else df_rot(xh[j], xl[j], yh[j], yl[j], P.c, P.sr, P.si);
+            if (r < m) { __stcg(bph + r, xh[j]); __stcg(bpl + r, xl[j]); __stcg(bqh + r, yh[j]); __stcg(bql + r, yl[j]); }
+          }
+          if (32 * j < n) {
+            if (small) df_rot_small(uh[j], ul[j], wh[j], wl[j], P.sr.h, P.si.h);
+            else df_rot(uh[j], ul[j], wh[j], wl[j], P.c, P.sr, P.si);
+            if (r < n) { __stcg(vph + r, uh[j]); __stcg(vpl + r, ul[j]); __stcg(vqh + r, wh[j]); __stcg(vql + r, wl[j]); }
+          }
+        }
+        if (lane == 0) {
+          atomicAdd(cnt, 1u);
+          atomicMax(cnt + 1, __float_as_uint(P.tabs));
+        }
+      }
+      cluster_sync_all();
+    }
+    const unsigned h = __ldcg(cnt);
+    const float tmax = __uint_as_float(__ldcg(cnt + 1));
+    conv = h == 0 || tmax < tan_stop;
+    cluster_sync_all();  // everyone has read this sweep's counters
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    state[0] = conv ? 1u : 0u;
+    state[1] = sweep;
+  }
+}
+
 template <int NT, int RPT>
 __global__ void __launch_bounds__(NT, 2) jacobi_sweep_df_k(float2* __restrict__ Bh, float2* __restrict__ Bl, long ldb,
                                                         int m, int n, float2* __restrict__ Vh, float2* __restrict__ Vl,
@@ -1465,7 +1595,34 @@ int jacobi_df(cudaStream_t s, SvdWork* w, float2* Bh, float2* Bl, long ldb, int 
   int grid = std::min(per_sm * sms, np / 2);
   if (grid < 1) grid = 1;
   int pr = prof_begin(s, PK_JACOBI_DF, 0.0, 0.0);
-  for (int sweep = 0; sweep < max_sweeps; sweep++) {
+  const bool cluster = k <= 128 && rows <= 32 * CCR;
+  if (cluster) {
+    // one cluster of up to 16 CTAs, one warp per pair of a round (as in jacobi<T>)
+    const int npairs = np / 2 > 0 ? np / 2 : 1;
+    const int cl = npairs < 16 ? npairs : 16;
+    const int wpc = std::min(4, (npairs + cl - 1) / cl);
+    static bool nonportable_set = false;
+    if (cl > 8 && !nonportable_set) {
+      QR_CUDA(cudaFuncSetAttribute(jacobi_cluster_df_k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+      nonportable_set = true;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(cl);
+    cfg.blockDim = dim3(32 * wpc);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = cl;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    QR_CUDA(cudaLaunchKernelEx(&cfg, jacobi_cluster_df_k, Bh, Bl, ldb, rows, k, Vh, Vl, ldv, (float)tol, smax_d,
+                               max_sweeps, state, k0, 1e-7f));
+    count_launch();
+  }
+  for (int sweep = 0; sweep < (cluster ? 0 : max_sweeps); sweep++) {
     float2 *a1 = Bh, *a2 = Bl, *a3 = Vh, *a4 = Vl;
     long l1 = ldb, l2 = ldv;
     int mm = rows, kk = k, npp = np, sw = sweep;
