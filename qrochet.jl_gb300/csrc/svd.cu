@@ -619,8 +619,9 @@ __host__ __device__ constexpr int jr_q(bool full, int ir, int g) {
               : JR_W + (g + ir) % JR_W;
 }
 
+template <int NT>
 struct JrShared {
-  float red[16][JR_NT / 32];
+  float red[16][NT / 32];
   RotParams<float> P[4];
   float2 J[JR_C][JR_C];  // J[col][row]
   int col[JR_C];
@@ -654,8 +655,8 @@ __device__ __forceinline__ float jr_warp_sum16(float (&v)[16]) {
   return a1;  // value index ((l >> 4) & 1) * 8 + ((l >> 3) & 1) * 4 + ((l >> 2) & 1) * 2 + ((l >> 1) & 1)
 }
 
-template <bool FULL, int IR>
-__device__ __forceinline__ void jr_local_round(float2 (&x)[JR_C][JR_RPT], JrShared& sh, float tol, float smax,
+template <int NT, int RPT, bool FULL, int IR>
+__device__ __forceinline__ void jr_local_round(float2 (&x)[JR_C][RPT], JrShared<NT>& sh, float tol, float smax,
                                                unsigned* cnt) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   float v[16];
@@ -666,7 +667,7 @@ __device__ __forceinline__ void jr_local_round(float2 (&x)[JR_C][JR_RPT], JrShar
     const int p = jr_p(FULL, IR, g), q = jr_q(FULL, IR, g);
     float a = 0.f, b = 0.f, gr = 0.f, gi = 0.f;
 #pragma unroll
-    for (int j = 0; j < JR_RPT; j++) {
+    for (int j = 0; j < RPT; j++) {
       const float2 xx = x[p][j], yy = x[q][j];
       a += xx.x * xx.x + xx.y * xx.y;
       b += yy.x * yy.x + yy.y * yy.y;
@@ -685,7 +686,7 @@ __device__ __forceinline__ void jr_local_round(float2 (&x)[JR_C][JR_RPT], JrShar
     float tot = 0.f;
     if (lane < 16) {
 #pragma unroll
-      for (int w = 0; w < JR_NT / 32; w++) tot += sh.red[lane][w];
+      for (int w = 0; w < NT / 32; w++) tot += sh.red[lane][w];
     }
     const int g = lane & 3;
     const float sa = __shfl_sync(0xffffffffu, tot, 4 * g), sb = __shfl_sync(0xffffffffu, tot, 4 * g + 1);
@@ -710,7 +711,7 @@ __device__ __forceinline__ void jr_local_round(float2 (&x)[JR_C][JR_RPT], JrShar
     if (sh.P[g].go) {
       const float c = sh.P[g].c, sr = sh.P[g].sr, si = sh.P[g].si;
 #pragma unroll
-      for (int j = 0; j < JR_RPT; j++) rot(x[p][j], x[q][j], c, sr, si);
+      for (int j = 0; j < RPT; j++) rot(x[p][j], x[q][j], c, sr, si);
       if (tid < JR_C) {  // columns p, q of J, row tid (J is read only after a later barrier)
         float2 u = sh.J[p][tid], w = sh.J[q][tid];
         rot(u, w, c, sr, si);
@@ -721,18 +722,125 @@ __device__ __forceinline__ void jr_local_round(float2 (&x)[JR_C][JR_RPT], JrShar
   }
 }
 
+// One work item: block pair (bp, bq) of round `round`.  VPRE (n <= NT): V's rows of the 8
+// columns are loaded with B's, before the local rounds, so their L2 round trip overlaps them.
+template <int NT, int RPT, bool VPRE>
+__device__ __forceinline__ void jr_block_pair(float2* __restrict__ B, long ldb, int m, int n, float2* __restrict__ V,
+                                              long ldv, int nb, int bp, int bq, int round, float tol, float smax,
+                                              unsigned* cnt, JrShared<NT>& sh) {
+  const int tid = threadIdx.x;
+  if (tid < JR_C) {
+    const int blk = tid < JR_W ? bp : bq, c = blk * JR_W + (tid % JR_W);
+    sh.col[tid] = (blk < nb && c < n) ? c : -1;
+  }
+  if (tid < JR_C * JR_C) sh.J[tid / JR_C][tid % JR_C] = make_float2((tid / JR_C) == (tid % JR_C) ? 1.f : 0.f, 0.f);
+  if (tid == 0) sh.rotated = 0;
+  __syncthreads();
+  float2 x[JR_C][RPT];
+#pragma unroll
+  for (int l = 0; l < JR_C; l++) {
+    const int c = sh.col[l];
+#pragma unroll
+    for (int j = 0; j < RPT; j++) {
+      const int r = tid + NT * j;
+      x[l][j] = (c >= 0 && r < m) ? __ldcg(B + (long)c * ldb + r) : make_float2(0.f, 0.f);
+    }
+  }
+  float2 vpre[VPRE ? JR_C : 1];
+  if constexpr (VPRE) {
+#pragma unroll
+    for (int l = 0; l < JR_C; l++) {
+      const int c = sh.col[l];
+      vpre[l] = (c >= 0 && tid < n) ? __ldcg(V + (long)c * ldv + tid) : make_float2(0.f, 0.f);
+    }
+  }
+  if (round == 0) {
+    jr_local_round<NT, RPT, true, 0>(x, sh, tol, smax, cnt);
+    jr_local_round<NT, RPT, true, 1>(x, sh, tol, smax, cnt);
+    jr_local_round<NT, RPT, true, 2>(x, sh, tol, smax, cnt);
+    jr_local_round<NT, RPT, true, 3>(x, sh, tol, smax, cnt);
+    jr_local_round<NT, RPT, true, 4>(x, sh, tol, smax, cnt);
+    jr_local_round<NT, RPT, true, 5>(x, sh, tol, smax, cnt);
+    jr_local_round<NT, RPT, true, 6>(x, sh, tol, smax, cnt);
+  } else {
+    jr_local_round<NT, RPT, false, 0>(x, sh, tol, smax, cnt);
+    jr_local_round<NT, RPT, false, 1>(x, sh, tol, smax, cnt);
+    jr_local_round<NT, RPT, false, 2>(x, sh, tol, smax, cnt);
+    jr_local_round<NT, RPT, false, 3>(x, sh, tol, smax, cnt);
+  }
+  __syncthreads();  // J and the rotated flag are final
+  if (!sh.rotated) return;
+#pragma unroll
+  for (int l = 0; l < JR_C; l++) {
+    const int c = sh.col[l];
+    if (c < 0) continue;
+#pragma unroll
+    for (int j = 0; j < RPT; j++) {
+      const int r = tid + NT * j;
+      if (r < m) __stcg(B + (long)c * ldb + r, x[l][j]);
+    }
+  }
+  if constexpr (VPRE) {
+    if (tid < n) {
+#pragma unroll
+      for (int l2 = 0; l2 < JR_C; l2++) {
+        const int c = sh.col[l2];
+        if (c < 0) continue;
+        float2 o = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int l = 0; l < JR_C; l++) {
+          const float2 jv = sh.J[l2][l];
+          o.x += vpre[l].x * jv.x - vpre[l].y * jv.y;
+          o.y += vpre[l].x * jv.y + vpre[l].y * jv.x;
+        }
+        __stcg(V + (long)c * ldv + tid, o);
+      }
+    }
+  } else {
+    for (int r0 = tid; r0 < n; r0 += 2 * NT) {
+      float2 vin[2][JR_C];
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int r = r0 + h * NT;
+#pragma unroll
+        for (int l = 0; l < JR_C; l++) {
+          const int c = sh.col[l];
+          vin[h][l] = (c >= 0 && r < n) ? __ldcg(V + (long)c * ldv + r) : make_float2(0.f, 0.f);
+        }
+      }
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int r = r0 + h * NT;
+        if (r >= n) continue;
+#pragma unroll
+        for (int l2 = 0; l2 < JR_C; l2++) {
+          const int c = sh.col[l2];
+          if (c < 0) continue;
+          float2 o = make_float2(0.f, 0.f);
+#pragma unroll
+          for (int l = 0; l < JR_C; l++) {
+            const float2 jv = sh.J[l2][l];
+            o.x += vin[h][l].x * jv.x - vin[h][l].y * jv.y;
+            o.y += vin[h][l].x * jv.y + vin[h][l].y * jv.x;
+          }
+          __stcg(V + (long)c * ldv + r, o);
+        }
+      }
+    }
+  }
+}
+
 __global__ void __launch_bounds__(JR_NT, 1)
     jacobi_block_reg_k(float2* __restrict__ B, long ldb, int m, int n, float2* __restrict__ V, long ldv, int nbp,
                        float tol, const double* __restrict__ smax_p, unsigned* __restrict__ state, int sweep,
                        unsigned* __restrict__ flags, float tan_stop) {
-  __shared__ JrShared sh;
+  __shared__ JrShared<JR_NT> sh;
   if (((volatile unsigned*)state)[0]) return;
   const float smax = (float)(smax_p[0] / smax_p[1]);
   unsigned* cnt = state + 8 + 2 * sweep;
   const int nb = (n + JR_W - 1) / JR_W;
   const int npairs = nbp / 2;
   const unsigned base = (unsigned)sweep * (unsigned)(nbp - 1);
-  const int tid = threadIdx.x;
   const bool dataflow = npairs > (int)gridDim.x;
   const long nit = dataflow ? ((long)(nbp - 1) * npairs - blockIdx.x + gridDim.x - 1) / gridDim.x : (long)(nbp - 1);
   for (long t = 0; t < nit; t++) {
@@ -741,82 +849,7 @@ __global__ void __launch_bounds__(JR_NT, 1)
     int bp, bq;
     pair_cols(nbp, round, pair, bp, bq);
     if (dataflow && !wait_cols(flags, bp, bq, nb, base + round, state)) return;
-    if (bp < nb) {
-      if (tid < JR_C) {
-        const int blk = tid < JR_W ? bp : bq, c = blk * JR_W + (tid % JR_W);
-        sh.col[tid] = (blk < nb && c < n) ? c : -1;
-      }
-      if (tid < JR_C * JR_C) sh.J[tid / JR_C][tid % JR_C] = make_float2((tid / JR_C) == (tid % JR_C) ? 1.f : 0.f, 0.f);
-      if (tid == 0) sh.rotated = 0;
-      __syncthreads();
-      float2 x[JR_C][JR_RPT];
-#pragma unroll
-      for (int l = 0; l < JR_C; l++) {
-        const int c = sh.col[l];
-#pragma unroll
-        for (int j = 0; j < JR_RPT; j++) {
-          const int r = tid + JR_NT * j;
-          x[l][j] = (c >= 0 && r < m) ? __ldcg(B + (long)c * ldb + r) : make_float2(0.f, 0.f);
-        }
-      }
-      if (round == 0) {
-        jr_local_round<true, 0>(x, sh, tol, smax, cnt);
-        jr_local_round<true, 1>(x, sh, tol, smax, cnt);
-        jr_local_round<true, 2>(x, sh, tol, smax, cnt);
-        jr_local_round<true, 3>(x, sh, tol, smax, cnt);
-        jr_local_round<true, 4>(x, sh, tol, smax, cnt);
-        jr_local_round<true, 5>(x, sh, tol, smax, cnt);
-        jr_local_round<true, 6>(x, sh, tol, smax, cnt);
-      } else {
-        jr_local_round<false, 0>(x, sh, tol, smax, cnt);
-        jr_local_round<false, 1>(x, sh, tol, smax, cnt);
-        jr_local_round<false, 2>(x, sh, tol, smax, cnt);
-        jr_local_round<false, 3>(x, sh, tol, smax, cnt);
-      }
-      __syncthreads();  // J and the rotated flag are final
-      if (sh.rotated) {
-#pragma unroll
-        for (int l = 0; l < JR_C; l++) {
-          const int c = sh.col[l];
-          if (c < 0) continue;
-#pragma unroll
-          for (int j = 0; j < JR_RPT; j++) {
-            const int r = tid + JR_NT * j;
-            if (r < m) __stcg(B + (long)c * ldb + r, x[l][j]);
-          }
-        }
-        for (int r0 = tid; r0 < n; r0 += 2 * JR_NT) {
-          float2 vin[2][JR_C];
-#pragma unroll
-          for (int h = 0; h < 2; h++) {
-            const int r = r0 + h * JR_NT;
-#pragma unroll
-            for (int l = 0; l < JR_C; l++) {
-              const int c = sh.col[l];
-              vin[h][l] = (c >= 0 && r < n) ? __ldcg(V + (long)c * ldv + r) : make_float2(0.f, 0.f);
-            }
-          }
-#pragma unroll
-          for (int h = 0; h < 2; h++) {
-            const int r = r0 + h * JR_NT;
-            if (r >= n) continue;
-#pragma unroll
-            for (int l2 = 0; l2 < JR_C; l2++) {
-              const int c = sh.col[l2];
-              if (c < 0) continue;
-              float2 o = make_float2(0.f, 0.f);
-#pragma unroll
-              for (int l = 0; l < JR_C; l++) {
-                const float2 jv = sh.J[l2][l];
-                o.x += vin[h][l].x * jv.x - vin[h][l].y * jv.y;
-                o.y += vin[h][l].x * jv.y + vin[h][l].y * jv.x;
-              }
-              __stcg(V + (long)c * ldv + r, o);
-            }
-          }
-        }
-      }
-    }
+    if (bp < nb) jr_block_pair<JR_NT, JR_RPT, false>(B, ldb, m, n, V, ldv, nb, bp, bq, round, tol, smax, cnt, sh);
     if (dataflow) post_cols(flags, bp, bq, nb, base + round + 1);
     else {
       __syncthreads();
@@ -826,6 +859,51 @@ __global__ void __launch_bounds__(JR_NT, 1)
   finish_sweep(state, cnt, sweep, tan_stop);
 }
 
+
+// Barrier over all threads of a thread-block cluster; release/acquire orders the global-memory
+// writes of a round before the reads of the next one.
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
+  asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
+
+// FP32 block Jacobi for k <= 128 columns of at most 128 rows: the whole iteration in one
+// thread-block cluster with one 128-thread CTA per block pair of a round (one row per thread,
+// V's rows prefetched with B's), the hardware cluster barrier between block rounds and all sweeps
+// in one launch.  A sweep has nb - 1 block rounds (nb = k / 4 blocks) instead of the scalar
+// kernel's k - 1 rounds; the local rounds inside a block pair need only CTA barriers.  state as in
+// jacobi_cluster_k.
+constexpr int JC_NT = 128;
+__global__ void __launch_bounds__(JC_NT) jacobi_block_cluster_k(float2* __restrict__ B, long ldb, int m, int n,
+                                                                float2* __restrict__ V, long ldv, float tol,
+                                                                const double* __restrict__ smax_p, int max_sweeps,
+                                                                unsigned* __restrict__ state, float tan_stop) {
+  __shared__ JrShared<JC_NT> sh;
+  const float smax = (float)(smax_p[0] / smax_p[1]);
+  const int nb = (n + JR_W - 1) / JR_W, nbp = nb + (nb & 1), npairs = nbp / 2;
+  int sweep = 0;
+  bool conv = false;
+  for (; sweep < max_sweeps && !conv; sweep++) {
+    unsigned* cnt = state + 8 + 2 * sweep;
+    for (int round = 0; round < nbp - 1; round++) {
+      for (int pair = blockIdx.x; pair < npairs; pair += gridDim.x) {
+        int bp, bq;
+        pair_cols(nbp, round, pair, bp, bq);
+        if (bp < nb) jr_block_pair<JC_NT, 1, true>(B, ldb, m, n, V, ldv, nb, bp, bq, round, tol, smax, cnt, sh);
+        __syncthreads();  // shared state is reused by the next item
+      }
+      cluster_sync_all();
+    }
+    const unsigned h = __ldcg(cnt);
+    const float tmax = __uint_as_float(__ldcg(cnt + 1));
+    conv = h == 0 || tmax < tan_stop;
+    cluster_sync_all();  // everyone has read this sweep's counters
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    state[0] = conv ? 1u : 0u;
+    state[1] = sweep;
+  }
+}
 
 // Small problems (k <= 128 columns): the whole Jacobi iteration in one thread-block cluster of up
 // to 16 CTAs.  Each warp owns a pair of the round (1-4 warps per CTA, so a round's work spreads
@@ -838,10 +916,6 @@ __global__ void __launch_bounds__(JR_NT, 1)
 // through the rotation, so a round costs one L2 round trip instead of three.  state[0] =
 // converged, state[1] = sweeps, state[8 + s] = rotations of sweep s (global counters, shared by
 // the cluster).
-__device__ __forceinline__ void cluster_sync_all() {
-  asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
-  asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
-}
 
 constexpr int CCR = 4;  // rows per lane held in registers by the cluster kernels (m <= 128)
 
@@ -1451,13 +1525,18 @@ int jacobi(cudaStream_t s, SvdWork* w, cplx_t<T>* B, long ldb, int rows, int k, 
   if (small) {
     // one cluster of up to 16 CTAs with one warp per pair of a round: as many CTAs as pairs (up
     // to 16), then 2-4 warps per CTA
-    const int npairs = np / 2 > 0 ? np / 2 : 1;
+    // FP32 with at most 128 rows: the block form (one CTA per block pair of 4-column blocks)
+    const bool blk = sizeof(T) == 4 && rows <= JC_NT && k > 2 * JR_W;
+    const int nbk = (k + JR_W - 1) / JR_W;
+    const int npairs = blk ? (nbk + (nbk & 1)) / 2 : (np / 2 > 0 ? np / 2 : 1);
     const int cl = npairs < 16 ? npairs : 16;
-    const int wpc = std::min(4, (npairs + cl - 1) / cl);  // __launch_bounds__(128): warps loop over pairs
-    static bool nonportable_set[2] = {false, false};
-    if (cl > 8 && !nonportable_set[sizeof(T) == 8]) {
-      QR_CUDA(cudaFuncSetAttribute(jacobi_cluster_k<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-      nonportable_set[sizeof(T) == 8] = true;
+    const int wpc = blk ? JC_NT / 32 : std::min(4, (npairs + cl - 1) / cl);  // warps loop over pairs
+    static bool nonportable_set[3] = {false, false, false};
+    const int ns = blk ? 2 : (sizeof(T) == 8);
+    if (cl > 8 && !nonportable_set[ns]) {
+      if (blk) QR_CUDA(cudaFuncSetAttribute(jacobi_block_cluster_k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+      else QR_CUDA(cudaFuncSetAttribute(jacobi_cluster_k<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+      nonportable_set[ns] = true;
     }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(cl);
@@ -1471,8 +1550,13 @@ int jacobi(cudaStream_t s, SvdWork* w, cplx_t<T>* B, long ldb, int rows, int k, 
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    QR_CUDA(cudaLaunchKernelEx(&cfg, jacobi_cluster_k<T>, B, ldb, rows, k, V, ldv, tol, (const double*)smax_d,
-                               max_sweeps, state, tan_stop));
+    if (blk) {
+      QR_CUDA(cudaLaunchKernelEx(&cfg, jacobi_block_cluster_k, (float2*)B, ldb, rows, k, (float2*)V, ldv, (float)tol,
+                                 (const double*)smax_d, max_sweeps, state, tan_stop));
+    } else {
+      QR_CUDA(cudaLaunchKernelEx(&cfg, jacobi_cluster_k<T>, B, ldb, rows, k, V, ldv, tol, (const double*)smax_d,
+                                 max_sweeps, state, tan_stop));
+    }
     count_launch();
   } else if (sizeof(T) == 4 && rows <= JR_MAXROWS) {
     // FP32 with the rows in registers: block Jacobi (4-column blocks, pairs of blocks)

@@ -89,6 +89,10 @@ CASES = {
     "graded12": lambda g: _graded(g, 80, 80, 12),
     "zero_cols": lambda g: np.hstack([R.complex_gaussian(g, (40, 10)), np.zeros((40, 6))]),
     "tiny": lambda g: R.complex_gaussian(g, (2, 1)),
+    # cluster kernels for <= 128 columns of <= 128 rows: an odd number of 4-column blocks with a
+    # partial last block, and the largest size (16 block pairs, 10 decades of singular values)
+    "blocks_odd": lambda g: R.complex_gaussian(g, (120, 33)),
+    "graded128": lambda g: _graded(g, 128, 128, 10),
     # above 128 columns the mixed mode takes the FP32-preconditioned path with the polish sweeps
     "square300": lambda g: R.complex_gaussian(g, (300, 300)),
     "wide200x400": lambda g: R.complex_gaussian(g, (200, 400)),
