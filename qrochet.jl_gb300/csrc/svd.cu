@@ -20,6 +20,7 @@
 // column's phase, which moves the represented matrix by O(eps sigma_max) only.
 #include <vector>
 #include <algorithm>
+#include <functional>
 #include <cstdio>
 #include <cstring>
 #include <cstdlib>
@@ -49,7 +50,7 @@ struct DBuf {
 };
 
 struct SvdWork {
-  DBuf B, V, B32, V32, X, Rm, E, T1, nrm, perm, cnt, tau, qtmp, host_sig, Bl;
+  DBuf B, V, B32, V32, X, Rm, E, T1, nrm, perm, cnt, tau, qtmp, host_sig, Bl, Qp;
   std::vector<double> hs;
   std::vector<unsigned> hc;
   cudaStream_t last = nullptr;
@@ -252,23 +253,44 @@ __global__ void __launch_bounds__(NT) jacobi_sweep_k(cplx_t<T>* __restrict__ B, 
 // steps, so the rotation is unitary to working precision while FP64 square roots and divisions --
 // expensive on this part -- are avoided.  A slightly inexact angle only leaves a coupling a
 // factor ~1e-7 smaller, which the next sweep removes.
+// |g| without forming |g|^2: in FP32 the squared coupling of two tiny columns underflows
+template <typename T>
+__device__ __forceinline__ T cabs_safe(T gr, T gi) {
+  const T x = fabs(gr), y = fabs(gi);
+  const T mx = x > y ? x : y, mn = x > y ? y : x;
+  if (!(mx > T(0))) return T(0);
+  const T r = mn / mx;
+  return mx * sqrt(T(1) + r * r);
+}
+
+// tol < 0 selects the relative test |g| > |tol| sqrt(a b) (every pair is driven to the same
+// relative orthogonality whatever its norms; used on the R^H of a QR preconditioning, where FP32
+// keeps the small columns to full relative precision); otherwise the absolute test below.
 template <typename T>
 __device__ __forceinline__ bool rotation_params(T a, T b, T gr, T gi, T tol, T smax, T& c, T& sr, T& si, float& tabs) {
-  const T g2 = gr * gr + gi * gi;
-  const T fl = T(4) * Eps<T>::v * smax;
-  const T mn = a < b ? a : b;
-  // g > tol smax sqrt(min(a, b)) + fl^2, compared in squares
-  if (!(a > 0) || !(b > 0) || !(g2 > tol * tol * smax * smax * mn + fl * fl * fl * fl)) return false;
-  // 1/|gamma| in working precision: FP32 seed of the exponent-normalised g2 (exact scaling), then
-  // two Newton steps; gamma may be far below FP32 range while still above the rotation floor
-  int e2 = 0;
-  const T g2n = frexp(g2, &e2);  // g2 = g2n * 2^e2, g2n in [0.5, 1)
-  const int h = e2 / 2;
-  const T g2s = ldexp(g2n, e2 - 2 * h);  // in [0.25, 2)
-  T rg = (T)rsqrtf((float)g2s);
-  rg = rg * (T(1.5) - T(0.5) * g2s * rg * rg);
-  rg = rg * (T(1.5) - T(0.5) * g2s * rg * rg);
-  rg = ldexp(rg, -h);
+  if (!(a > 0) || !(b > 0)) return false;
+  T rg;
+  if (tol < T(0)) {
+    const T gabs = cabs_safe(gr, gi);
+    if (!(gabs > -tol * sqrt(a) * sqrt(b))) return false;
+    rg = T(1) / gabs;
+  } else {
+    const T g2 = gr * gr + gi * gi;
+    const T fl = T(4) * Eps<T>::v * smax;
+    const T mn = a < b ? a : b;
+    // g > tol smax sqrt(min(a, b)) + fl^2, compared in squares
+    if (!(g2 > tol * tol * smax * smax * mn + fl * fl * fl * fl)) return false;
+    // 1/|gamma| in working precision: FP32 seed of the exponent-normalised g2 (exact scaling), then
+    // two Newton steps; gamma may be far below FP32 range while still above the rotation floor
+    int e2 = 0;
+    const T g2n = frexp(g2, &e2);  // g2 = g2n * 2^e2, g2n in [0.5, 1)
+    const int h = e2 / 2;
+    const T g2s = ldexp(g2n, e2 - 2 * h);  // in [0.25, 2)
+    rg = (T)rsqrtf((float)g2s);
+    rg = rg * (T(1.5) - T(0.5) * g2s * rg * rg);
+    rg = rg * (T(1.5) - T(0.5) * g2s * rg * rg);
+    rg = ldexp(rg, -h);
+  }
   const float zeta = (float)(T(0.5) * (b - a) * rg);
   const float tf = (zeta >= 0.f ? 1.f : -1.f) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
   if (!(tf != 0.f)) return false;  // angle below FP32 resolution of the tangent: nothing to do
@@ -321,8 +343,13 @@ template <typename T>
 struct RotParams {
   T c, sr, si;
   float tabs;
+  float rel;  // |g|^2 / (a b): the pair's relative coupling, squared
   int go;
 };
+
+// Per-sweep counters: state[8 + SW_STRIDE s + 0..2] = rotations, largest rotation tangent and
+// largest |g|^2 / (a b) of a rotated pair (float bits; the last is recorded by the FP32 kernels).
+constexpr int SW_STRIDE = 4;
 
 // Rotates rows [0, len) of the column pair (xp, xq) in chunks of NT * RPT rows: each chunk's
 // loads are all issued before its first store, so a chunk costs one L2 round trip.
@@ -410,6 +437,7 @@ __device__ __forceinline__ void jacobi_pair_fast(cplx_t<T>* __restrict__ B, long
       float tabs = 0.f;
       const bool go = rotation_params<T>(sa, sb, sgr, sgi, tol, smax, c, sr, si, tabs);
       P.c = c; P.sr = sr; P.si = si; P.tabs = tabs; P.go = go ? 1 : 0;
+      P.rel = (float)((sgr * sgr + sgi * sgi) / (sa * sb));
     }
   }
   __syncthreads();
@@ -435,6 +463,7 @@ __device__ __forceinline__ void jacobi_pair_fast(cplx_t<T>* __restrict__ B, long
   if (threadIdx.x == 0) {
     atomicAdd(count, 1u);
     atomicMax(count + 1, __float_as_uint(P.tabs));
+    atomicMax(count + 2, __float_as_uint(P.rel));
   }
 }
 
@@ -542,8 +571,8 @@ __device__ __forceinline__ void finish_sweep(unsigned* state, const unsigned* cn
 // sweep that finds no rotation, or, in FP64, whose largest rotation tangent is < 1e-8; later
 // sweeps then return at once), state[1] = sweeps run, state[2..3] = grid barrier, state[4] /
 // [5] = wait (flag or barrier) timeout / abort,
-// state[6] = CTAs done with the sweep, state[8 + 2 s] / [9 + 2 s] = rotations / largest tangent
-// (float bits) of sweep s; flags[c] = rounds completed by column c (dataflow ordering above).
+// state[6] = CTAs done with the sweep, state[8 + SW_STRIDE s ...] = the sweep's counters;
+// flags[c] = rounds completed by column c (dataflow ordering above).
 template <typename T, int NT, int RPT>
 __global__ void __launch_bounds__(NT, 512 / NT) jacobi_sweep_dev_k(cplx_t<T>* __restrict__ B, long ldb, int m, int n,
                                                          cplx_t<T>* __restrict__ V, long ldv, int np, T tol,
@@ -552,7 +581,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) jacobi_sweep_dev_k(cplx_t<T>* __
                                                          unsigned* __restrict__ flags, float tan_stop) {
   if (((volatile unsigned*)state)[0]) return;
   const T smax = (T)(smax_p[0] / smax_p[1]);  // sigma_max of the pre-scaled columns (~1)
-  unsigned* cnt = state + 8 + 2 * sweep;
+  unsigned* cnt = state + 8 + SW_STRIDE * sweep;
   const int npairs = np / 2;
   const unsigned base = (unsigned)sweep * (unsigned)(np - 1);
   // dataflow: work items in (round, pair) order dealt round-robin to the CTAs, so the surplus
@@ -577,11 +606,19 @@ __global__ void __launch_bounds__(NT, 512 / NT) jacobi_sweep_dev_k(cplx_t<T>* __
 // underflows where a rotation is due and the textbook formulas need no rescaling or Newton steps.
 __device__ __forceinline__ bool rotation_params_f32(float a, float b, float gr, float gi, float tol, float smax,
                                                     float& c, float& sr, float& si, float& tabs) {
-  const float g2 = gr * gr + gi * gi;
-  const float fl = 4.f * Eps<float>::v * smax;
-  const float mn = fminf(a, b);
-  if (!(a > 0.f) || !(b > 0.f) || !(g2 > tol * tol * smax * smax * mn + fl * fl * fl * fl)) return false;
-  const float rg = rsqrtf(g2);  // 1 / |g|
+  if (!(a > 0.f) || !(b > 0.f)) return false;
+  float rg;  // 1 / |g|
+  if (tol < 0.f) {  // relative test (see rotation_params)
+    const float gabs = cabs_safe(gr, gi);
+    if (!(gabs > -tol * sqrtf(a) * sqrtf(b))) return false;
+    rg = 1.f / gabs;
+  } else {
+    const float g2 = gr * gr + gi * gi;
+    const float fl = 4.f * Eps<float>::v * smax;
+    const float mn = fminf(a, b);
+    if (!(g2 > tol * tol * smax * smax * mn + fl * fl * fl * fl)) return false;
+    rg = rsqrtf(g2);
+  }
   const float zeta = 0.5f * (b - a) * rg;
   const float az = fabsf(zeta);
   float t = az > 1e18f ? 0.5f / az : 1.f / (az + sqrtf(1.f + az * az));
@@ -700,6 +737,7 @@ __device__ __forceinline__ void jr_local_round(float2 (&x)[JR_C][RPT], JrShared<
       if (go) {
         atomicAdd(cnt, 1u);
         atomicMax(cnt + 1, __float_as_uint(tabs));
+        atomicMax(cnt + 2, __float_as_uint((sgr * sgr + sgi * sgi) / (sa * sb)));
         sh.rotated = 1;
       }
     }
@@ -837,7 +875,7 @@ __global__ void __launch_bounds__(JR_NT, 1)
   __shared__ JrShared<JR_NT> sh;
   if (((volatile unsigned*)state)[0]) return;
   const float smax = (float)(smax_p[0] / smax_p[1]);
-  unsigned* cnt = state + 8 + 2 * sweep;
+  unsigned* cnt = state + 8 + SW_STRIDE * sweep;
   const int nb = (n + JR_W - 1) / JR_W;
   const int npairs = nbp / 2;
   const unsigned base = (unsigned)sweep * (unsigned)(nbp - 1);
@@ -884,7 +922,7 @@ __global__ void __launch_bounds__(JC_NT) jacobi_block_cluster_k(float2* __restri
   int sweep = 0;
   bool conv = false;
   for (; sweep < max_sweeps && !conv; sweep++) {
-    unsigned* cnt = state + 8 + 2 * sweep;
+    unsigned* cnt = state + 8 + SW_STRIDE * sweep;
     for (int round = 0; round < nbp - 1; round++) {
       for (int pair = blockIdx.x; pair < npairs; pair += gridDim.x) {
         int bp, bq;
@@ -932,7 +970,7 @@ __global__ void __launch_bounds__(128) jacobi_cluster_k(cplx_t<T>* __restrict__ 
   int sweep = 0;
   bool conv = false;
   for (; sweep < max_sweeps && !conv; sweep++) {
-    unsigned* cnt = state + 8 + 2 * sweep;
+    unsigned* cnt = state + 8 + SW_STRIDE * sweep;
     for (int round = 0; round < np1; round++) {
       for (int pair = gw; pair < npairs; pair += nw) {
         int p, q;
@@ -986,6 +1024,7 @@ __global__ void __launch_bounds__(128) jacobi_cluster_k(cplx_t<T>* __restrict__ 
           if (lane == 0) {
             atomicAdd(cnt, 1u);
             atomicMax(cnt + 1, __float_as_uint(tabs));
+            atomicMax(cnt + 2, __float_as_uint((float)((gr * gr + gi * gi) / (a * b))));
           }
           continue;
         }
@@ -1016,6 +1055,7 @@ __global__ void __launch_bounds__(128) jacobi_cluster_k(cplx_t<T>* __restrict__ 
         if (lane == 0) {
           atomicAdd(cnt, 1u);
           atomicMax(cnt + 1, __float_as_uint(tabs));
+          atomicMax(cnt + 2, __float_as_uint((float)((gr * gr + gi * gi) / (a * b))));
         }
       }
       cluster_sync_all();
@@ -1302,7 +1342,7 @@ __global__ void __launch_bounds__(128) jacobi_cluster_df_k(float2* __restrict__ 
   int sweep = 0;
   bool conv = false;
   for (; sweep < max_sweeps && !conv; sweep++) {
-    unsigned* cnt = state + 8 + 2 * sweep;
+    unsigned* cnt = state + 8 + SW_STRIDE * sweep;
     for (int round = 0; round < np - 1; round++) {
       for (int pair = gw; pair < npairs; pair += nw) {
         int p, q;
@@ -1374,7 +1414,7 @@ __global__ void __launch_bounds__(NT, 2) jacobi_sweep_df_k(float2* __restrict__ 
   // even columns; k <= 4096 keeps two CTAs per SM)
   float2* SV = (n % 2 == 0 && ldv % 2 == 0 && n <= 4096) ? df_sv : nullptr;
   const double smax = smax_p[0] / smax_p[1];
-  unsigned* cnt = state + 8 + 2 * sweep;
+  unsigned* cnt = state + 8 + SW_STRIDE * sweep;
   const int npairs = np / 2;
   const unsigned base = (unsigned)sweep * (unsigned)(np - 1);
   // dataflow: work items in (round, pair) order dealt round-robin to the CTAs, so the surplus
@@ -1493,14 +1533,15 @@ inline unsigned gs(long n) {
 // whose convergence is decided on the device.  One host synchronisation per call.
 template <typename T>
 int jacobi(cudaStream_t s, SvdWork* w, cplx_t<T>* B, long ldb, int rows, int k, cplx_t<T>* V,
-           long ldv, int max_sweeps, T tol, bool must_converge = true, float tan_stop = -1.f) {
+           long ldv, int max_sweeps, T tol, bool must_converge = true, float tan_stop = -1.f,
+           int* converged = nullptr, double* last_frac = nullptr) {
   if (tan_stop < 0.f) tan_stop = sizeof(T) == 8 ? 1e-8f : 0.f;
   const int np = k + (k & 1);
   constexpr int NT = sizeof(T) == 8 ? 256 : 128;
   constexpr int RPT = sizeof(T) == 8 ? 8 : 16;
   const int kind = sizeof(T) == 8 ? PK_JACOBI64 : PK_JACOBI32;
   const double pairs = 0.5 * (double)k * (k - 1);
-  const int nstate = 8 + 2 * max_sweeps;
+  const int nstate = 8 + SW_STRIDE * max_sweeps;
   // [state (nstate) | column flags (np) | pad | smax, scale (2 doubles)]
   const int soff = nstate + np + ((nstate + np) & 1);
   QR_TRY(w->cnt.ensure(sizeof(unsigned) * soff + 2 * sizeof(double) + 128, s));
@@ -1628,12 +1669,13 @@ int jacobi(cudaStream_t s, SvdWork* w, cplx_t<T>* B, long ldb, int rows, int k, 
   const int ran = (int)hs[1];
   double rotated = 0;
   for (int sw = 0; sw < ran; sw++) {
-    rotated += hs[8 + 2 * sw];
+    rotated += hs[8 + SW_STRIDE * sw];
     if (debug_on()) {
-      float tmax;
-      memcpy(&tmax, &hs[9 + 2 * sw], sizeof(float));
-      fprintf(stderr, "[qr] jacobi<%s> %dx%d sweep %d rotations %u max tan %.2e\n", sizeof(T) == 8 ? "f64" : "f32",
-              rows, k, sw, hs[8 + 2 * sw], tmax);
+      float tmax, rmax;
+      memcpy(&tmax, &hs[9 + SW_STRIDE * sw], sizeof(float));
+      memcpy(&rmax, &hs[10 + SW_STRIDE * sw], sizeof(float));
+      fprintf(stderr, "[qr] jacobi<%s> %dx%d sweep %d rotations %u max tan %.2e max coupling %.2e\n",
+              sizeof(T) == 8 ? "f64" : "f32", rows, k, sw, hs[8 + SW_STRIDE * sw], tmax, sqrtf(rmax));
     }
   }
   if (debug_on() && small) fprintf(stderr, "[qr] jacobi_cluster<%s> %dx%d sweeps %d\n", sizeof(T) == 8 ? "f64" : "f32", rows, k, ran);
@@ -1641,6 +1683,8 @@ int jacobi(cudaStream_t s, SvdWork* w, cplx_t<T>* B, long ldb, int rows, int k, 
   // column rotations of B and V per rotated pair (20 flops per row and column)
   prof_account(pr, 16.0 * rows * pairs * ran + 40.0 * rotated * (rows + k),
                sizeof(cplx_t<T>) * ((double)rows + k) * 2.0 * (pairs * ran + rotated));
+  if (converged) *converged = hs[0] ? 1 : 0;
+  if (last_frac) *last_frac = ran > 0 && pairs > 0 ? hs[8 + SW_STRIDE * (ran - 1)] / pairs : 0.0;
   if (!hs[0] && must_converge) return fail(QR_ENOCONV, "Jacobi SVD did not converge");
   return QR_OK;
 }
@@ -1657,7 +1701,7 @@ int jacobi_df(cudaStream_t s, SvdWork* w, float2* Bh, float2* Bl, long ldb, int 
   constexpr int NT = 256, RPT = 8;
   const int np = k + (k & 1);
   const double pairs = 0.5 * (double)k * (k - 1);
-  const int nstate = 8 + 2 * max_sweeps;
+  const int nstate = 8 + SW_STRIDE * max_sweeps;
   QR_TRY(w->cnt.ensure(sizeof(unsigned) * (nstate + np) + 128, s));
   unsigned* state = w->cnt.as<unsigned>();
   unsigned* flags = state + nstate;
@@ -1728,11 +1772,11 @@ int jacobi_df(cudaStream_t s, SvdWork* w, float2* Bh, float2* Bl, long ldb, int 
   const int ran = (int)hs[1];
   double rotated = 0;
   for (int sw = 0; sw < ran; sw++) {
-    rotated += hs[8 + 2 * sw];
+    rotated += hs[8 + SW_STRIDE * sw];
     if (debug_on()) {
       float tmax;
-      memcpy(&tmax, &hs[9 + 2 * sw], sizeof(float));
-      fprintf(stderr, "[qr] jacobi<df> %dx%d sweep %d rotations %u max tan %.2e\n", rows, k, sw, hs[8 + 2 * sw], tmax);
+      memcpy(&tmax, &hs[9 + SW_STRIDE * sw], sizeof(float));
+      fprintf(stderr, "[qr] jacobi<df> %dx%d sweep %d rotations %u max tan %.2e\n", rows, k, sw, hs[8 + SW_STRIDE * sw], tmax);
     }
   }
   // FP32 operations: ~96 per row per inner-product pass (compensated sums) and ~100-340 per row
@@ -1766,14 +1810,43 @@ static int reorthonormalize(cudaStream_t s, SvdWork* w, double2* L, long ldl, in
 constexpr float kPrecondTanStop = 0.15f;
 // Smallest block (columns) that takes the mixed path; below it the FP64 cluster Jacobi is as fast.
 constexpr int kMixedMinCols = 16;
+// QR preconditioning (Drmac and Veselic): B = Q R, then the one-sided Jacobi runs on W = R^H.
+// When B's singular values are spread over many decades and its right singular vectors are not
+// aligned with its columns (theta of a state with a decaying Schmidt spectrum), Hestenes sweeps on
+// B need 30-40+ sweeps; on R^H they need ~10 (measured on a CPU model of these sweeps: 10
+// decades at n = 320, 37 -> 10 sweeps; Gaussian, 13 -> 11).  The FP64 path always
+// preconditions above kPrecondMinCols columns (the QR costs less than one FP64 sweep).
+// The mixed path's cost on such matrices is the double-float polish, not the FP32 stage: the FP32
+// test is absolute (tol * sigma_max), so FP32 never rotates pairs of columns far below sigma_max
+// and the polish has to diagonalise that block from scratch (22 double-float sweeps at 2048
+// columns over 10 decades).  So when the FP32 stage has not converged after kMixedProbeSweeps
+// sweeps and more than kSmallColFrac of the columns the polish will touch are below
+// kSmallCol * sigma_max, the FP32 stage restarts on R^H with a relative test, which FP32 resolves
+// there (the polish then takes 2-3 sweeps).
+constexpr int kPrecondMinCols = 32;
+constexpr int kMixedProbeSweeps = 11;
+constexpr double kSmallCol = 1e-4;
+constexpr double kSmallColFrac = 0.1;
+
+// B (rows x k, rows >= k) = Q R with Q in w->Qp (rows x k); B is replaced by W = R^H (k x k, ld k)
+static int qr_precondition(cudaStream_t s, SvdWork* w, double2* B, int rows, int k) {
+  QR_TRY(w->Qp.ensure(sizeof(double2) * (size_t)rows * k, s));
+  QR_TRY(w->qtmp.ensure(sizeof(double2) * (size_t)k * k, s));
+  QR_TRY(w->tau.ensure(sizeof(double2) * (size_t)k, s));
+  double2* Rr = w->qtmp.as<double2>();
+  QR_TRY(zqr_thin(s, B, rows, k, rows, w->Qp.as<double2>(), rows, Rr, k, w->tau.as<double2>()));
+  return ztranspose(s, Rr, k, k, k, B, k, 1);
+}
 
 int zsvd_thin(cudaStream_t s, SvdWork* w, int mode, const double2* A, int m, int n, long lda,
               double2* U, long ldu, double* S, double2* Vh, long ldvh, int keep) {
   if (m <= 0 || n <= 0) return QR_OK;
   const bool tall = m >= n;
-  const int rows = tall ? m : n;  // B = A (tall) or A^H (wide): rows x k
+  const int rows0 = tall ? m : n;  // B = A (tall) or A^H (wide): rows0 x k
   const int k = tall ? n : m;
-  QR_TRY(w->B.ensure(sizeof(double2) * (size_t)rows * k, s));
+  int rows = rows0;  // rows of the matrix the Jacobi runs on: rows0, or k after QR preconditioning
+  bool pre = false;
+  QR_TRY(w->B.ensure(sizeof(double2) * (size_t)rows0 * k, s));
   QR_TRY(w->V.ensure(sizeof(double2) * (size_t)k * k, s));
   QR_TRY(w->nrm.ensure(sizeof(double) * (size_t)k * 2, s));
   QR_TRY(w->perm.ensure(sizeof(int) * (size_t)k, s));
@@ -1795,9 +1868,14 @@ int zsvd_thin(cudaStream_t s, SvdWork* w, int mode, const double2* A, int m, int
   // The FP32-preconditioned path pays off above a few dozen columns; tiny blocks take the FP64
   // Jacobi directly (same accuracy).
   if (mode == QR_FP64 || k <= kMixedMinCols) {
+    if (k > kPrecondMinCols) {
+      QR_TRY(qr_precondition(s, w, B, rows0, k));
+      rows = k;
+      pre = true;
+    }
     QR_TRY(zset_identity(s, V, k, k, k));
     double tol = sqrt((double)rows) * Eps<double>::v;
-    QR_TRY(jacobi<double>(s, w, B, rows, rows, k, V, k, 40, tol));
+    QR_TRY(jacobi<double>(s, w, B, rows, rows, k, V, k, 60, tol));
   } else {
     // ---- FP32 Jacobi preconditioner
     QR_TRY(w->B32.ensure(sizeof(float2) * (size_t)rows * k, s));
@@ -1809,7 +1887,43 @@ int zsvd_thin(cudaStream_t s, SvdWork* w, int mode, const double2* A, int m, int
     // a preconditioner: 1e-5 relative orthogonality is plenty for the FP64 refinement, and sits
     // above the FP32 rounding floor (~sqrt(m) eps32) so sweeps stop once rotations are noise
     float tol32 = fmaxf(4e-6f, 2.0f * sqrtf((float)rows) * Eps<float>::v);
-    QR_TRY(jacobi<float>(s, w, B32, rows, rows, k, V32, k, 20, tol32, false, kPrecondTanStop));
+    int conv32 = 0;
+    double frac32 = 0.0;
+    QR_TRY(jacobi<float>(s, w, B32, rows, rows, k, V32, k, kMixedProbeSweeps, tol32, false, kPrecondTanStop,
+                         &conv32, &frac32));
+    // columns the polish rotates: all, or the leading keep + margin (see below)
+    const int k0 = keep > 0 && keep < k ? std::min(k, keep + std::max(32, keep / 8)) : k;
+    bool slow = false;
+    if (!conv32) {
+      col_norms_k<float2><<<ceil_div((long)k * 32, TPB), TPB, 0, s>>>(B32, rows, rows, k, nrm);
+      QR_CHECK_LAUNCH("col_norms_k");
+      w->hs.resize(k);
+      QR_CUDA(cudaMemcpyAsync(w->hs.data(), nrm, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+      QR_CUDA(cudaStreamSynchronize(s));
+      std::vector<double> sn(w->hs.begin(), w->hs.end());
+      std::sort(sn.begin(), sn.end(), std::greater<double>());
+      int small = 0;
+      for (int j = 0; j < k0; j++) small += sn[j] < kSmallCol * sn[0];
+      slow = small > kSmallColFrac * k0;
+      if (debug_on())
+        fprintf(stderr, "[qr] mixed %dx%d: FP32 probe: last sweep rotated %.4f of the pairs; %d of the %d polished "
+                "columns below %.0e sigma_max -> %s\n", rows, k, frac32, small, k0, kSmallCol,
+                slow ? "QR preconditioning" : "continue");
+    }
+    if (!conv32 && !slow) {
+      QR_TRY(jacobi<float>(s, w, B32, rows, rows, k, V32, k, 20 - kMixedProbeSweeps, tol32, false,
+                           kPrecondTanStop));
+    } else if (!conv32) {
+      // slow convergence (widely spread spectrum): precondition in FP64 and start over on R^H
+      QR_TRY(qr_precondition(s, w, B, rows0, k));
+      rows = k;
+      pre = true;
+      tol32 = fmaxf(4e-6f, 2.0f * sqrtf((float)rows) * Eps<float>::v);
+      QR_TRY(z2c(s, B, rows, B32, rows, rows, k));
+      QR_TRY(cset_identity(s, V32, k, k, k));
+      // relative test: on R^H the small columns are exact to FP32 precision, not rounding noise
+      QR_TRY(jacobi<float>(s, w, B32, rows, rows, k, V32, k, 20, -tol32, false, kPrecondTanStop));
+    }
     // X = V32 with columns sorted by the FP32 column norms (descending), as a double-float
     // matrix (low parts zero); the Newton-Schulz steps and B = A X run in double-float on the
     // FP32 pipes and B goes straight into the double-float polish
@@ -1857,7 +1971,6 @@ int zsvd_thin(cudaStream_t s, SvdWork* w, int mode, const double2* A, int m, int
     // trailing block need no rotation: the cross pairs still decouple that block from the leading
     // columns, and every tail column's norm stays below the tail's largest sigma, so the final
     // sort separates the two sets.  The margin covers FP32 misordering at the boundary.
-    const int k0 = keep > 0 && keep < k ? std::min(k, keep + std::max(32, keep / 8)) : k;
     QR_TRY(jacobi_df(s, w, Bh, Bl, rows, rows, k, Xh, Xl, k, 40, 32.0 * sqrt((double)rows) * Eps<double>::v,
                      smax_d, k0));
     QR_TRY(df2z(s, Bh, Bl, rows, rows, k, smax_d + 1, B, rows));
@@ -1884,6 +1997,30 @@ int zsvd_thin(cudaStream_t s, SvdWork* w, int mode, const double2* A, int m, int
   // left factor L (rows x k) = B[:, perm] / sigma ; right factor Rf (k x k) = V[:, perm]
   QR_TRY(w->E.ensure(sizeof(double2) * (size_t)k * k, s));
   double2* Rf = w->E.as<double2>();
+  if (pre) {
+    // W = R^H = L Sigma Rf^H  =>  B0 = Q R = (Q Rf) Sigma L^H: the left factor of B0 is Q Rf
+    // (orthonormal: Householder Q times accumulated rotations) and its right factor is L
+    QR_TRY(w->Rm.ensure(sizeof(double2) * (size_t)k * k, s));
+    double2* L = w->Rm.as<double2>();
+    gather_cols_k<double2><<<gs((long)k * k), TPB, 0, s>>>(B, k, k, k, perm, sorted, L, k);
+    QR_CHECK_LAUNCH("gather_cols_k");
+    if (reorth) QR_TRY(reorthonormalize(s, w, L, k, k, kk));
+    gather_cols_k<double2><<<gs((long)k * k), TPB, 0, s>>>(V, k, k, k, perm, nullptr, Rf, k);
+    QR_CHECK_LAUNCH("gather_cols_k");
+    const double2 one = make_double2(1.0, 0.0), zero = make_double2(0.0, 0.0);
+    if (tall) {  // A = B0: U = Q Rf (m x k), Vh = L^H
+      QR_TRY(zgemm(s, OP_N, OP_N, rows0, k, k, one, w->Qp.as<double2>(), rows0, 0, Rf, k, 0, zero, U, ldu, 0, 1,
+                   nullptr));
+      QR_TRY(ztranspose(s, L, k, k, k, Vh, ldvh, 1));
+    } else {  // A = B0^H = L Sigma (Q Rf)^H: U = L (m x m), Vh = (Q Rf)^H (m x n); B is free
+      QR_TRY(zgemm(s, OP_N, OP_N, rows0, k, k, one, w->Qp.as<double2>(), rows0, 0, Rf, k, 0, zero, B, rows0, 0, 1,
+                   nullptr));
+      QR_CUDA(cudaMemcpy2DAsync(U, sizeof(double2) * ldu, L, sizeof(double2) * k, sizeof(double2) * k, k,
+                                cudaMemcpyDeviceToDevice, s));
+      QR_TRY(ztranspose(s, B, rows0, rows0, k, Vh, ldvh, 1));
+    }
+    return QR_OK;
+  }
   if (tall) {
     gather_cols_k<double2><<<gs((long)rows * k), TPB, 0, s>>>(B, rows, rows, k, perm, sorted, U, ldu);
     QR_CHECK_LAUNCH("gather_cols_k");

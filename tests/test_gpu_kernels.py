@@ -97,6 +97,10 @@ CASES = {
     "square300": lambda g: R.complex_gaussian(g, (300, 300)),
     "wide200x400": lambda g: R.complex_gaussian(g, (200, 400)),
     "graded300": lambda g: _graded(g, 300, 300, 10),
+    # 12 decades with random singular vectors: plain Hestenes sweeps converge slowly here, so the
+    # FP64 path runs on R^H of a QR and the mixed path falls back to it after its FP32 probe
+    "graded600": lambda g: _graded(g, 600, 600, 12),
+    "graded_wide": lambda g: _graded(g, 180, 400, 12),
 }
 
 
