@@ -25,6 +25,30 @@ static thread_local std::string t_err;
 std::atomic<uint64_t> g_launches{0};
 
 void set_error(const std::string& msg) { t_err = msg; }
+
+struct HostScratch {
+  void* p = nullptr;
+  size_t cap = 0;
+  ~HostScratch() {
+    if (p) cudaFreeHost(p);
+  }
+};
+static thread_local HostScratch t_scratch;
+
+void* host_scratch(size_t bytes) {
+  if (bytes > t_scratch.cap) {
+    if (t_scratch.p) cudaFreeHost(t_scratch.p);
+    t_scratch.p = nullptr;
+    t_scratch.cap = 0;
+    const size_t want = std::max<size_t>(bytes + bytes / 2, 4096);
+    if (cudaMallocHost(&t_scratch.p, want) != cudaSuccess) {
+      t_scratch.p = nullptr;
+      return nullptr;
+    }
+    t_scratch.cap = want;
+  }
+  return t_scratch.p;
+}
 int fail(int code, const std::string& msg) {
   t_err = msg;
   return code;
@@ -283,9 +307,11 @@ int truncate_impl(qr_chain* h, int s1, int s2, double threshold, int maxdim) {
   const int b = s1;
   if (!h->lam[b]) return fail(QR_ENO_SCHMIDT, "Can't access the spectrum on bond");
   const int dim = h->lamlen[b];
-  std::vector<double> lam(dim);
-  QR_CUDA(cudaMemcpyAsync(lam.data(), h->lam[b], sizeof(double) * dim, cudaMemcpyDeviceToHost, h->stream));
+  double* hl = static_cast<double*>(host_scratch(sizeof(double) * dim));
+  if (!hl) return fail(QR_ENOMEM, "page-locked host scratch");
+  QR_CUDA(cudaMemcpyAsync(hl, h->lam[b], sizeof(double) * dim, cudaMemcpyDeviceToHost, h->stream));
   QR_CUDA(cudaStreamSynchronize(h->stream));
+  const std::vector<double> lam(hl, hl + dim);
   int upto = (maxdim >= 0) ? (maxdim < dim ? maxdim : dim) : dim;
   if (std::isnan(threshold)) threshold = 1e-16;
   std::vector<int> keep;
@@ -538,11 +564,12 @@ int env_sweep_ring(const qr_chain* a, const qr_chain* b, cudaStream_t s, double 
     unsigned g = (unsigned)std::min<long>((S + 255) / 256, 4864);
     ring_trace_k<<<g, 256, 0, s>>>(E0, c0a, c0b, tr);
     count_launch();
-    std::vector<double2> h(S);
-    rc = cuda_ok(cudaMemcpyAsync(h.data(), tr, sizeof(double2) * S, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
+    double2* h = static_cast<double2*>(host_scratch(sizeof(double2) * S));
+    if (!h) rc = fail(QR_ENOMEM, "page-locked host scratch");
+    if (!rc) rc = cuda_ok(cudaMemcpyAsync(h, tr, sizeof(double2) * S, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
     if (!rc) rc = cuda_ok(cudaStreamSynchronize(s), "cudaStreamSynchronize");
     double re = 0, im = 0;
-    for (const double2& v : h) { re += v.x; im += v.y; }
+    for (long i = 0; !rc && i < S; i++) { re += h[i].x; im += h[i].y; }
     out[0] = re;
     out[1] = im;
   }
@@ -614,11 +641,12 @@ int env_sweep(const qr_chain* a, const qr_chain* b, const EnvOps* ops, cudaStrea
   }
   if (rc == QR_OK) {
     QR_CUDA(cudaGetLastError());
-    double2 r;
-    QR_CUDA(cudaMemcpyAsync(&r, E0, sizeof(double2), cudaMemcpyDeviceToHost, s));
+    double2* r = static_cast<double2*>(host_scratch(sizeof(double2)));
+    if (!r) return fail(QR_ENOMEM, "page-locked host scratch");
+    QR_CUDA(cudaMemcpyAsync(r, E0, sizeof(double2), cudaMemcpyDeviceToHost, s));
     QR_CUDA(cudaStreamSynchronize(s));
-    out[0] = r.x;
-    out[1] = r.y;
+    out[0] = r->x;
+    out[1] = r->y;
   }
   cudaFreeAsync(E0, s);
   cudaFreeAsync(E1, s);

@@ -35,6 +35,13 @@ void set_error(const std::string& msg);
 int fail(int code, const std::string& msg);
 int cuda_fail(cudaError_t e, const char* what);
 
+// Page-locked host scratch owned by the calling thread, for the small device-to-host reads on the
+// hot path (sweep counters, singular values, a scalar result).  A read into pageable memory goes
+// through the driver's staging buffer after the stream's earlier kernels; with many chains served
+// by concurrent threads those reads serialise.  Valid until the thread's next call; nullptr if the
+// allocation fails.
+void* host_scratch(size_t bytes);
+
 extern std::atomic<uint64_t> g_launches;
 inline void count_launch(uint64_t n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 

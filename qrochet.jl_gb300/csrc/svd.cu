@@ -51,8 +51,6 @@ struct DBuf {
 
 struct SvdWork {
   DBuf B, V, B32, V32, X, Rm, E, T1, nrm, perm, cnt, tau, qtmp, host_sig, Bl, Qp;
-  std::vector<double> hs;
-  std::vector<unsigned> hc;
   cudaStream_t last = nullptr;
 };
 
@@ -1661,9 +1659,9 @@ int jacobi(cudaStream_t s, SvdWork* w, cplx_t<T>* B, long ldb, int rows, int k, 
     pow2_scale_k<cplx_t<T>><<<g > 4864 ? 4864 : g, TPB, 0, s>>>(B, ldb, rows, k, smax_d, smax_d + 1, 1);
     QR_CHECK_LAUNCH("pow2_scale_k");
   }
-  std::vector<unsigned>& hs = w->hc;
-  hs.assign(nstate, 0u);
-  QR_CUDA(cudaMemcpyAsync(hs.data(), state, sizeof(unsigned) * nstate, cudaMemcpyDeviceToHost, s));
+  unsigned* hs = static_cast<unsigned*>(host_scratch(sizeof(unsigned) * nstate));
+  if (!hs) return fail(QR_ENOMEM, "page-locked host scratch");
+  QR_CUDA(cudaMemcpyAsync(hs, state, sizeof(unsigned) * nstate, cudaMemcpyDeviceToHost, s));
   QR_CUDA(cudaStreamSynchronize(s));
   if (hs[4]) return fail(QR_ECUDA, "Jacobi sweep: a column wait timed out");
   const int ran = (int)hs[1];
@@ -1764,9 +1762,9 @@ int jacobi_df(cudaStream_t s, SvdWork* w, float2* Bh, float2* Bl, long ldb, int 
     count_launch();
   }
   prof_end(s, pr);
-  std::vector<unsigned>& hs = w->hc;
-  hs.assign(nstate, 0u);
-  QR_CUDA(cudaMemcpyAsync(hs.data(), state, sizeof(unsigned) * nstate, cudaMemcpyDeviceToHost, s));
+  unsigned* hs = static_cast<unsigned*>(host_scratch(sizeof(unsigned) * nstate));
+  if (!hs) return fail(QR_ENOMEM, "page-locked host scratch");
+  QR_CUDA(cudaMemcpyAsync(hs, state, sizeof(unsigned) * nstate, cudaMemcpyDeviceToHost, s));
   QR_CUDA(cudaStreamSynchronize(s));
   if (hs[4]) return fail(QR_ECUDA, "double-float Jacobi sweep: a column wait timed out");
   const int ran = (int)hs[1];
@@ -1897,10 +1895,11 @@ int zsvd_thin(cudaStream_t s, SvdWork* w, int mode, const double2* A, int m, int
     if (!conv32) {
       col_norms_k<float2><<<ceil_div((long)k * 32, TPB), TPB, 0, s>>>(B32, rows, rows, k, nrm);
       QR_CHECK_LAUNCH("col_norms_k");
-      w->hs.resize(k);
-      QR_CUDA(cudaMemcpyAsync(w->hs.data(), nrm, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+      double* hn = static_cast<double*>(host_scratch(sizeof(double) * k));
+      if (!hn) return fail(QR_ENOMEM, "page-locked host scratch");
+      QR_CUDA(cudaMemcpyAsync(hn, nrm, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
       QR_CUDA(cudaStreamSynchronize(s));
-      std::vector<double> sn(w->hs.begin(), w->hs.end());
+      std::vector<double> sn(hn, hn + k);
       std::sort(sn.begin(), sn.end(), std::greater<double>());
       int small = 0;
       for (int j = 0; j < k0; j++) small += sn[j] < kSmallCol * sn[0];
@@ -1984,13 +1983,14 @@ int zsvd_thin(cudaStream_t s, SvdWork* w, int mode, const double2* A, int m, int
   QR_CHECK_LAUNCH("rank_sort_k");
   QR_CUDA(cudaMemcpyAsync(S, sorted, sizeof(double) * k, cudaMemcpyDeviceToDevice, s));
   // decide on re-orthonormalisation from the spectrum
-  w->hs.resize(k);
-  QR_CUDA(cudaMemcpyAsync(w->hs.data(), sorted, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+  double* hsg = static_cast<double*>(host_scratch(sizeof(double) * k));
+  if (!hsg) return fail(QR_ENOMEM, "page-locked host scratch");
+  QR_CUDA(cudaMemcpyAsync(hsg, sorted, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
   QR_CUDA(cudaStreamSynchronize(s));
   // columns that truncation may retain must be orthonormal to ~1e-11: B/sigma columns are
   // orthogonal to tol * sigma_max / sigma_j, so re-orthonormalise when sigma_keep < 1e-3 sigma_max
   const int kk = (keep > 0 && keep < k) ? keep : k;
-  const double smax = w->hs[0], smin = w->hs[kk - 1];
+  const double smax = hsg[0], smin = hsg[kk - 1];
   if (!(smax >= 0.0) || !std::isfinite(smax)) return fail(QR_ENOCONV, "non-finite singular values");
   const bool reorth = !(smin > 1e-3 * smax);
 
