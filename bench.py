@@ -50,7 +50,7 @@ def parse():
     p.add_argument("--quick", action="store_true", help="small chi for a fast functional run")
     p.add_argument("--launch-list", action="store_true",
                    help="only the warm-up and timed steps of the mixed path (for ncu launch lists)")
-    p.add_argument("--batched", type=int, default=32, help="requests in the batched sample (0: skip)")
+    p.add_argument("--batched", type=int, default=128, help="requests in the batched sample (0: skip)")
     p.add_argument("--serve", type=int, default=32, help="requests in the serving sample (0: skip)")
     p.add_argument("--mpo-sites", type=int, default=128, help="sites of the MPO environment sweep (0: skip)")
     p.add_argument("--workers", type=int, default=16)
