@@ -52,6 +52,8 @@ def parse():
                    help="only the warm-up and timed steps of the mixed path (for ncu launch lists)")
     p.add_argument("--batched", type=int, default=128, help="requests in the batched sample (0: skip)")
     p.add_argument("--serve", type=int, default=32, help="requests in the serving sample (0: skip)")
+    p.add_argument("--serve-sat", type=int, default=96,
+                   help="requests in the saturated mixed-precision serving sample (0: skip)")
     p.add_argument("--mpo-sites", type=int, default=128, help="sites of the MPO environment sweep (0: skip)")
     p.add_argument("--workers", type=int, default=16)
     return p.parse_args()
@@ -239,15 +241,22 @@ def run_batched(args, Q, dist, rank, world):
 def run_serving(args, Q, dist, rank, world):
     """Serving: Poisson arrivals at 200 req/s of random brick-wall circuits with 8 Pauli strings of
     weight 1-4; p50/p99 latency and solves/s for the FP64 and mixed forms.  Bounded sample:
-    n ~ U[16,64], depth ~ U[4,16], chi_max in {32, 128}."""
+    n ~ U[16,64], depth ~ U[4,16], chi_max in {32, 128}.  With `--serve` requests (2x the
+    workers by default) half the requests start at once, so p99/p50 mostly shows the spread of the
+    requests' own service times; the `mixed_saturated` sample (`--serve-sat`, 6x the workers)
+    keeps a queue in front of every worker for most of the run, the regime in which a serving loop
+    is judged at saturation."""
     from qrochet import serve as S
     from qrochet import random as R
 
     out = {}
-    for prec in ("fp64", "mixed"):
+    runs = [("fp64", "fp64", args.serve), ("mixed", "mixed", args.serve)]
+    if args.serve_sat > 0:
+        runs.append(("mixed_saturated", "mixed", args.serve_sat))
+    for name, prec, nreq in runs:
         g = R.rng(5)
         reqs = [S.random_request(g, n_range=(16, 64), depth_range=(4, 16), chi_choices=(32, 128), nobs=8)
-                for _ in range(args.serve)]
+                for _ in range(nreq)]
         # arrivals at 200 req/s in total: each replica sees its share of the Poisson stream
         gaps = shard(g.exponential(1.0 / 200.0, size=len(reqs)).cumsum(), rank, world)
         reqs = shard(reqs, rank, world)
@@ -263,7 +272,7 @@ def run_serving(args, Q, dist, rank, world):
             res = [sv.wait(t) for t in tickets]
             dt = dist.max(time.perf_counter() - t0)
         lat = np.array(dist.gather([x["latency_ms"] for x in res]))
-        out[prec] = {"requests": len(lat), "solves_per_s": len(lat) / dt, "p50_ms": float(np.percentile(lat, 50)),
+        out[name] = {"requests": len(lat), "solves_per_s": len(lat) / dt, "p50_ms": float(np.percentile(lat, 50)),
                      "p99_ms": float(np.percentile(lat, 99)),
                      "p99_over_p50": float(np.percentile(lat, 99) / np.percentile(lat, 50)),
                      "values": [x["values"] for x in res]}

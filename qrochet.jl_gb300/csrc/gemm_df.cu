@@ -18,6 +18,9 @@
 // Tiling: a CTA of 256 threads owns a 64 x 64 block of C, each thread a 4 x 4 sub-block (rows
 // tx + 16 i, columns ty + 16 j); K advances in steps of 16 through double-buffered shared
 // memory filled by cp.async (8-byte copies, zero-filled outside the matrix).
+// Split K: when C has too few tiles to occupy the GPU (the small blocks of a gate at chi <= 128),
+// blockIdx.z takes a K-chunk, each CTA writes its unrounded double-float partial sums, and a second
+// kernel adds the chunks in double-float and applies the mode's epilogue.
 #include "kernels.cuh"
 #include "df.cuh"
 #include "prof.cuh"
@@ -73,12 +76,37 @@ __device__ __forceinline__ void load_tile(DfSmem& sm, int st, int M, int N, int 
   }
 }
 
+// The mode's output for element (row, col) from its double-float sums
+template <int MODE>
+__device__ __forceinline__ void df_epilogue(int row, int col, bool mirror, DotAcc re, DotAcc im, float2* Ch,
+                                            float2* Cl, long ldc, const float2* Dh, const float2* Dl, long ldd,
+                                            float alpha) {
+  const long o = (long)row + (long)col * ldc;
+  if (MODE == DF_STORE) {
+    const dfl r = dot_final(re), m = dot_final(im);
+    Ch[o] = make_float2(r.h, m.h);
+    Cl[o] = make_float2(r.l, m.l);
+  } else if (MODE == DF_I_MINUS || MODE == DF_GRAM) {
+    const dfl r = df_add({row == col ? 1.f : 0.f, 0.f}, df_neg(dot_final(re)));
+    const dfl m = df_neg(dot_final(im));
+    Ch[o] = make_float2(r.h + r.l, m.h + m.l);
+    if (MODE == DF_GRAM && mirror) Ch[(long)col + (long)row * ldc] = make_float2(r.h + r.l, -(m.h + m.l));
+  } else {
+    const long od = (long)row + (long)col * ldd;
+    const float2 dh = Dh[od], dl = Dl[od];
+    const dfl r = df_add_f({dh.x, dl.x}, alpha * re.s);
+    const dfl m = df_add_f({dh.y, dl.y}, alpha * im.s);
+    Ch[o] = make_float2(r.h, m.h);
+    Cl[o] = make_float2(r.l, m.l);
+  }
+}
+
 template <int OPA, int MODE>
 __global__ void __launch_bounds__(DNT, 2)
     zgemm_df_k(int M, int N, int K, const float2* __restrict__ Ah, const float2* __restrict__ Al, long lda,
                const float2* __restrict__ Bh, const float2* __restrict__ Bl, long ldb, float2* __restrict__ Ch,
                float2* __restrict__ Cl, long ldc, const float2* __restrict__ Dh, const float2* __restrict__ Dl,
-               long ldd, float alpha) {
+               long ldd, float alpha, int kc, float4* __restrict__ P) {
   constexpr bool LO = MODE != DF_F32_AXPY;
   constexpr float CJ = OPA == OP_C ? -1.f : 1.f;  // conjugation of A's imaginary part
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -99,13 +127,16 @@ __global__ void __launch_bounds__(DNT, 2)
 #pragma unroll
     for (int j = 0; j < 4; j++) re[i][j] = im[i][j] = DotAcc{0.f, 0.f};
 
-  const int nk = (K + DBK - 1) / DBK;
-  load_tile<OPA, LO>(sm, 0, M, N, K, m0, n0, 0, Ah, Al, lda, Bh, Bl, ldb);
+  // K-chunk of this CTA: [kb, ke) (the whole K without split)
+  const int kb = P ? (int)blockIdx.z * kc : 0;
+  const int ke = P ? min(K, kb + kc) : K;
+  const int nk = (ke - kb + DBK - 1) / DBK;
+  load_tile<OPA, LO>(sm, 0, M, N, ke, m0, n0, kb, Ah, Al, lda, Bh, Bl, ldb);
   cp_async_commit();
   for (int t = 0; t < nk; t++) {
     const int st = t & 1;
     if (t + 1 < nk) {
-      load_tile<OPA, LO>(sm, st ^ 1, M, N, K, m0, n0, (t + 1) * DBK, Ah, Al, lda, Bh, Bl, ldb);
+      load_tile<OPA, LO>(sm, st ^ 1, M, N, ke, m0, n0, kb + (t + 1) * DBK, Ah, Al, lda, Bh, Bl, ldb);
       cp_async_commit();
       cp_async_wait<1>();
     } else {
@@ -166,25 +197,33 @@ __global__ void __launch_bounds__(DNT, 2)
     for (int j = 0; j < 4; j++) {
       const int col = n0 + ty + 16 * j;
       if (col >= N) continue;
-      const long o = (long)row + (long)col * ldc;
-      if (MODE == DF_STORE) {
-        const dfl r = dot_final(re[i][j]), m = dot_final(im[i][j]);
-        Ch[o] = make_float2(r.h, m.h);
-        Cl[o] = make_float2(r.l, m.l);
-      } else if (MODE == DF_I_MINUS || MODE == DF_GRAM) {
-        const dfl r = df_add({row == col ? 1.f : 0.f, 0.f}, df_neg(dot_final(re[i][j])));
-        const dfl m = df_neg(dot_final(im[i][j]));
-        Ch[o] = make_float2(r.h + r.l, m.h + m.l);
-        if (MODE == DF_GRAM && bx != by) Ch[(long)col + (long)row * ldc] = make_float2(r.h + r.l, -(m.h + m.l));
+      if (P) {  // partial sums of this K-chunk, unrounded
+        P[((long)blockIdx.z * N + col) * M + row] = make_float4(re[i][j].s, re[i][j].lo, im[i][j].s, im[i][j].lo);
       } else {
-        const long od = (long)row + (long)col * ldd;
-        const float2 dh = Dh[od], dl = Dl[od];
-        const dfl r = df_add_f({dh.x, dl.x}, alpha * re[i][j].s);
-        const dfl m = df_add_f({dh.y, dl.y}, alpha * im[i][j].s);
-        Ch[o] = make_float2(r.h, m.h);
-        Cl[o] = make_float2(r.l, m.l);
+        df_epilogue<MODE>(row, col, bx != by, re[i][j], im[i][j], Ch, Cl, ldc, Dh, Dl, ldd, alpha);
       }
     }
+  }
+}
+
+// Sum of the nz K-chunk partials of element (row, col) in double-float, then the mode's epilogue.
+// DF_GRAM: only elements of tiles on or above the diagonal were computed; they are mirrored.
+template <int MODE>
+__global__ void zgemm_df_reduce_k(int M, int N, int nz, const float4* __restrict__ P, float2* __restrict__ Ch,
+                                  float2* __restrict__ Cl, long ldc, const float2* __restrict__ Dh,
+                                  const float2* __restrict__ Dl, long ldd, float alpha) {
+  const long total = (long)M * N;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+    const int row = (int)(t % M), col = (int)(t / M);
+    const int tr = row / DBM, tc = col / DBN;
+    if (MODE == DF_GRAM && tr > tc) continue;
+    dfl r{0.f, 0.f}, m{0.f, 0.f};
+    for (int z = 0; z < nz; z++) {
+      const float4 v = P[((long)z * N + col) * M + row];
+      r = df_add(r, df_fast_two_sum(v.x, v.y));
+      m = df_add(m, df_fast_two_sum(v.z, v.w));
+    }
+    df_epilogue<MODE>(row, col, tr != tc, DotAcc{r.h, r.l}, DotAcc{m.h, m.l}, Ch, Cl, ldc, Dh, Dl, ldd, alpha);
   }
 }
 
@@ -203,10 +242,39 @@ int launch_df(cudaStream_t s, int M, int N, int K, const float2* Ah, const float
     const int tiles = (M + DBM - 1) / DBM;
     grid = dim3(tiles * (tiles + 1) / 2, 1);
   }
+  // split K until the grid covers the SMs about once (chunks of at least one K step)
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0;
+    QR_CUDA(cudaGetDevice(&dev));
+    QR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  }
+  const int tiles = (int)(grid.x * grid.y), ksteps = (K + DBK - 1) / DBK;
+  int nz = std::min(ksteps, std::max(1, sms / tiles));
+  const int kc = ((ksteps + nz - 1) / nz) * DBK;
+  nz = (K + kc - 1) / kc;
+  if (nz < 2) {
+    zgemm_df_k<OPA, MODE><<<grid, DNT, bytes, s>>>(M, N, K, Ah, Al, lda, Bh, Bl, ldb, Ch, Cl, ldc, Dh, Dl, ldd,
+                                                   alpha, K, nullptr);
+    QR_CHECK_LAUNCH("zgemm_df_k");
+    return QR_OK;
+  }
+  float4* P = nullptr;
+  QR_CUDA(cudaMallocAsync(&P, sizeof(float4) * (size_t)nz * M * N, s));
+  grid.z = nz;
   zgemm_df_k<OPA, MODE><<<grid, DNT, bytes, s>>>(M, N, K, Ah, Al, lda, Bh, Bl, ldb, Ch, Cl, ldc, Dh, Dl, ldd,
-                                                 alpha);
-  QR_CHECK_LAUNCH("zgemm_df_k");
-  return QR_OK;
+                                                 alpha, kc, P);
+  int rc = cudaGetLastError() == cudaSuccess ? QR_OK : fail(QR_ECUDA, "zgemm_df_k launch");
+  count_launch();
+  if (!rc) {
+    const long total = (long)M * N;
+    const unsigned g = (unsigned)std::min<long>((total + TPB - 1) / TPB, 4864);
+    zgemm_df_reduce_k<MODE><<<g, TPB, 0, s>>>(M, N, nz, P, Ch, Cl, ldc, Dh, Dl, ldd, alpha);
+    rc = cudaGetLastError() == cudaSuccess ? QR_OK : fail(QR_ECUDA, "zgemm_df_reduce_k launch");
+    count_launch();
+  }
+  cudaFreeAsync(P, s);
+  return rc;
 }
 
 __global__ void to_df_scaled_k(const double2* __restrict__ src, long lds, int rows, int cols,
