@@ -38,6 +38,61 @@ __global__ void permute_k(const double2* __restrict__ src, double2* __restrict__
   }
 }
 
+// Tiled permute for a layout change whose source-contiguous dimension `a` is not the
+// destination's first dimension: per batch index (the other dimensions), a tile of TA elements
+// along `a` by T0 = 1024 / TA along dimension 0 is read with consecutive threads on consecutive
+// source addresses (dimension a), staged in shared memory, and written with consecutive threads
+// on consecutive destination addresses (dimension 0).  For the site layouts (o,l,r) <-> (l,o,r)
+// with d = 2 the tile is 1024 x 2 and both sides are fully contiguous.  Each thread issues its
+// eight loads of a tile before the first shared-memory store, so a tile costs one DRAM round trip.
+constexpr int PT_THREADS = 256, PT_PER = 8, PT_ELEMS = PT_THREADS * PT_PER;
+__global__ void __launch_bounds__(PT_THREADS) permute_tiled_k(const double2* __restrict__ src,
+                                                              double2* __restrict__ dst, Perm p, int a, int ta,
+                                                              long nbatch) {
+  // rows of ta + 1 elements: the store phase reads column-wise with a stride of ta + 1 elements,
+  // which spreads a quarter-warp's 16-byte reads over all banks
+  __shared__ double2 tile[PT_ELEMS + PT_ELEMS / 2];
+  const int t0 = PT_ELEMS / ta, tp = ta + 1;
+  const long d0 = p.dims[0], da = p.dims[a];
+  long dstride[4];
+  dstride[0] = 1;
+  for (int k = 1; k < p.nd; k++) dstride[k] = dstride[k - 1] * p.dims[k - 1];
+  const long ss0 = p.src_stride[0], dsa = dstride[a];
+  const long tiles0 = (d0 + t0 - 1) / t0, tilesa = (da + ta - 1) / ta;
+  const long ntiles = tiles0 * tilesa * nbatch;
+  for (long tt = blockIdx.x; tt < ntiles; tt += gridDim.x) {
+    const long i0t = tt % tiles0, iat = (tt / tiles0) % tilesa;
+    long bidx = tt / (tiles0 * tilesa);
+    long sbase = 0, dbase = 0;
+    for (int k = 1; k < p.nd; k++) {
+      if (k == a) continue;
+      const long c = bidx % p.dims[k];
+      bidx /= p.dims[k];
+      sbase += c * p.src_stride[k];
+      dbase += c * dstride[k];
+    }
+    const long o0 = i0t * t0, a0 = iat * ta;
+    double2 v[PT_PER];
+#pragma unroll
+    for (int q = 0; q < PT_PER; q++) {  // consecutive threads: along a
+      const int e = threadIdx.x + q * PT_THREADS, ia = e % ta, i0 = e / ta;
+      if (o0 + i0 < d0 && a0 + ia < da) v[q] = src[sbase + (a0 + ia) + (o0 + i0) * ss0];
+    }
+#pragma unroll
+    for (int q = 0; q < PT_PER; q++) {
+      const int e = threadIdx.x + q * PT_THREADS, ia = e % ta, i0 = e / ta;
+      if (o0 + i0 < d0 && a0 + ia < da) tile[i0 * tp + ia] = v[q];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < PT_PER; q++) {  // consecutive threads: along dim 0
+      const int e = threadIdx.x + q * PT_THREADS, i0 = e % t0, ia = e / t0;
+      if (o0 + i0 < d0 && a0 + ia < da) dst[dbase + (o0 + i0) + (a0 + ia) * dsa] = tile[i0 * tp + ia];
+    }
+    __syncthreads();  // the tile is refilled by the next iteration
+  }
+}
+
 __global__ void scale_bond_k(double2* A, int cl, int d, int cr, const double* __restrict__ lam,
                              int side, int inv, double atol) {
   long total = (long)cl * d * cr;
@@ -180,6 +235,20 @@ int zpermute(cudaStream_t s, const double2* src, double2* dst, const Perm& p) {
   long total = 1;
   for (int k = 0; k < p.nd; k++) total *= p.dims[k];
   if (total == 0) return QR_OK;
+  // the destination dimension the source stores contiguously
+  int a = -1;
+  for (int k = 0; k < p.nd; k++)
+    if (p.src_stride[k] == 1 && p.dims[k] > 1) a = k;
+  if (a > 0 && p.dims[0] > 1) {
+    const int ta = p.dims[a] >= 32 ? 32 : (p.dims[a] >= 16 ? 16 : (p.dims[a] >= 8 ? 8 : (p.dims[a] >= 4 ? 4 : 2)));
+    const long t0 = PT_ELEMS / ta;
+    const long tiles = ((p.dims[0] + t0 - 1) / t0) * ((p.dims[a] + ta - 1) / ta);
+    const long nbatch = total / (p.dims[0] * p.dims[a]);
+    const long g = std::min<long>(tiles * nbatch, 152L * 8);
+    permute_tiled_k<<<(unsigned)g, PT_THREADS, 0, s>>>(src, dst, p, a, ta, nbatch);
+    QR_CHECK_LAUNCH("permute_tiled_k");
+    return QR_OK;
+  }
   permute_k<<<grid_for(total), TPB, 0, s>>>(src, dst, p, total);
   QR_CHECK_LAUNCH("permute_k");
   return QR_OK;

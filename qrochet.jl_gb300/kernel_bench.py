@@ -3,6 +3,8 @@
     python qrochet.jl_gb300/kernel_bench.py zgemm M N K [iters]
     python qrochet.jl_gb300/kernel_bench.py svd fp64|mixed N [M]
     python qrochet.jl_gb300/kernel_bench.py qr M N
+    python qrochet.jl_gb300/kernel_bench.py zgemm_split M N K [iters]
+    python qrochet.jl_gb300/kernel_bench.py upload CHI
 
 Inputs are seeded complex Gaussians; prints one JSON line with the event-timed duration, the
 algorithmic flop count and the achieved rate.  Used for ncu captures of single kernels.
@@ -58,6 +60,27 @@ def main(argv):
         ms = C.c_double()
         _lib.check(L.qr_test_qr(m, n, p(A), p(Q), p(Rm), C.byref(ms)))
         out = {"op": "qr", "m": m, "n": n, "ms": ms.value}
+    elif what == "zgemm_split":
+        M, N, K = (int(x) for x in argv[1:4])
+        iters = int(argv[4]) if len(argv) > 4 else 3
+        A = np.asfortranarray(R.complex_gaussian(g, (M, K)))
+        B = np.asfortranarray(R.complex_gaussian(g, (K, N)))
+        Cm = np.zeros((M, N), dtype=np.complex128, order="F")
+        ms = C.c_double()
+        _lib.check(L.qr_test_zgemm_split(0, 0, M, N, K, p(A), M, p(B), K, p(Cm), M, iters, C.byref(ms)))
+        fl = 8.0 * M * N * K
+        out = {"op": "zgemm_split", "M": M, "N": N, "K": K, "ms": ms.value, "tflops_complex_equiv": fl / ms.value / 1e9}
+    elif what == "upload":
+        # a 3-site chain whose middle site is (2, chi, chi) in the reference's (o, l, r) order: the
+        # upload permutes it to the device layout (l, o, r)
+        import qrochet as Q
+        chi = int(argv[1])
+        arrays = [R.complex_gaussian(g, (2, chi)), R.complex_gaussian(g, (2, chi, chi)), R.complex_gaussian(g, (2, chi))]
+        psi = Q.MPS(arrays)
+        psi.sync()
+        back = psi.site_array(2)
+        out = {"op": "upload", "chi": chi, "bytes_per_permute": 2 * 16 * 2 * chi * chi,
+               "roundtrip_exact": bool(np.array_equal(back, arrays[1]))}
     else:
         raise SystemExit(__doc__)
     print(json.dumps(out))

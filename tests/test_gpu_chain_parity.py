@@ -67,6 +67,24 @@ def test_upload_download_roundtrip(order):
         assert np.array_equal(psi2.site_array(i + 1, order), perm[i])
 
 
+@pytest.mark.parametrize("order", [("o", "l", "r"), ("r", "o", "l"), ("l", "r", "o"), ("r", "l", "o")])
+def test_upload_download_large_sites(order):
+    """Site layouts large enough for the shared-memory tiled permute to take several tiles per
+    dimension with ragged edges (bonds 600 and 45); bit-exact both ways."""
+    g = R.rng(11)
+    shapes = [(2, 600), (2, 600, 45), (2, 45)]
+    arrays = [R.complex_gaussian(g, sh) for sh in shapes]
+    perm = []
+    for i, a in enumerate(arrays):
+        src = [x for x in ("o", "l", "r") if not ((i == 0 and x == "l") or (i == 2 and x == "r"))]
+        dst = [x for x in order if not ((i == 0 and x == "l") or (i == 2 and x == "r"))]
+        perm.append(np.ascontiguousarray(np.transpose(a, [src.index(x) for x in dst])))
+    psi = Q.MPS(perm, order=order)
+    for i in range(3):
+        assert np.array_equal(psi.site_array(i + 1), arrays[i])
+        assert np.array_equal(psi.site_array(i + 1, order), perm[i])
+
+
 @pytest.mark.parametrize("method", ["qr", "svd"])
 @pytest.mark.parametrize("site,direction", [(1, "right"), (2, "right"), (2, "left"), (3, "left")])
 def test_canonize_site(method, site, direction):
