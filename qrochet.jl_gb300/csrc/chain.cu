@@ -17,6 +17,8 @@
 #include <cstdlib>
 #include <algorithm>
 #include <mutex>
+#include <map>
+#include <tuple>
 #include "kernels.cuh"
 
 namespace qr {
@@ -34,6 +36,52 @@ struct HostScratch {
   }
 };
 static thread_local HostScratch t_scratch;
+
+static std::mutex g_cfg_mu;
+static std::map<int, int> g_sms;
+static std::map<std::tuple<int, const void*, int, size_t>, int> g_occ;
+static std::map<std::tuple<int, const void*, int>, int> g_attr;
+
+int device_sm_count(int* out) {
+  int dev = 0;
+  QR_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_cfg_mu);
+  auto it = g_sms.find(dev);
+  if (it == g_sms.end()) {
+    int v = 0;
+    QR_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
+    it = g_sms.emplace(dev, v).first;
+  }
+  *out = it->second;
+  return QR_OK;
+}
+
+int blocks_per_sm(const void* func, int threads, size_t smem, int* out) {
+  int dev = 0;
+  QR_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_cfg_mu);
+  const auto key = std::make_tuple(dev, func, threads, smem);
+  auto it = g_occ.find(key);
+  if (it == g_occ.end()) {
+    int v = 0;
+    QR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, func, threads, smem));
+    it = g_occ.emplace(key, v).first;
+  }
+  *out = it->second;
+  return QR_OK;
+}
+
+int set_func_attr_once(const void* func, cudaFuncAttribute attr, int value) {
+  int dev = 0;
+  QR_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_cfg_mu);
+  const auto key = std::make_tuple(dev, func, (int)attr);
+  auto it = g_attr.find(key);
+  if (it != g_attr.end() && it->second == value) return QR_OK;
+  QR_CUDA(cudaFuncSetAttribute(func, attr, value));
+  g_attr[key] = value;
+  return QR_OK;
+}
 
 void* host_scratch(size_t bytes) {
   if (bytes > t_scratch.cap) {

@@ -42,6 +42,14 @@ int cuda_fail(cudaError_t e, const char* what);
 // allocation fails.
 void* host_scratch(size_t bytes);
 
+// Launch-configuration caches for the current device, safe to call from concurrent threads (the
+// request server's workers): the SM count, a kernel's resident blocks per SM at a block size and
+// dynamic shared-memory size, and function attributes set once per device (CUDA keeps them per
+// device context).
+int device_sm_count(int* out);
+int blocks_per_sm(const void* func, int threads, size_t smem, int* out);
+int set_func_attr_once(const void* func, cudaFuncAttribute attr, int value);
+
 extern std::atomic<uint64_t> g_launches;
 inline void count_launch(uint64_t n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 

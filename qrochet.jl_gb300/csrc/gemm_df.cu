@@ -231,24 +231,16 @@ template <int OPA, int MODE>
 int launch_df(cudaStream_t s, int M, int N, int K, const float2* Ah, const float2* Al, long lda, const float2* Bh,
               const float2* Bl, long ldb, float2* Ch, float2* Cl, long ldc, const float2* Dh, const float2* Dl,
               long ldd, float alpha) {
-  static bool attr = false;
   const int bytes = (int)sizeof(DfSmem);
-  if (!attr) {
-    QR_CUDA(cudaFuncSetAttribute(zgemm_df_k<OPA, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-    attr = true;
-  }
+  QR_TRY(set_func_attr_once((const void*)zgemm_df_k<OPA, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
   dim3 grid((M + DBM - 1) / DBM, (N + DBN - 1) / DBN);
   if (MODE == DF_GRAM) {
     const int tiles = (M + DBM - 1) / DBM;
     grid = dim3(tiles * (tiles + 1) / 2, 1);
   }
   // split K until the grid covers the SMs about once (chunks of at least one K step)
-  static int sms = 0;
-  if (sms == 0) {
-    int dev = 0;
-    QR_CUDA(cudaGetDevice(&dev));
-    QR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  }
+  int sms = 0;
+  QR_TRY(device_sm_count(&sms));
   const int tiles = (int)(grid.x * grid.y), ksteps = (K + DBK - 1) / DBK;
   int nz = std::min(ksteps, std::max(1, sms / tiles));
   const int kc = ((ksteps + nz - 1) / nz) * DBK;

@@ -70,9 +70,8 @@ constexpr int TPB = 256;
 
 // QR_DEBUG=1 in the environment prints sweep counts and refinement residuals to stderr
 bool debug_on() {
-  static int v = -1;
-  if (v < 0) v = getenv("QR_DEBUG") ? 1 : 0;
-  return v == 1;
+  static const bool v = getenv("QR_DEBUG") != nullptr;
+  return v;
 }
 
 template <typename T> struct Eps;
@@ -1570,12 +1569,9 @@ int jacobi(cudaStream_t s, SvdWork* w, cplx_t<T>* B, long ldb, int rows, int k, 
     const int npairs = blk ? (nbk + (nbk & 1)) / 2 : (np / 2 > 0 ? np / 2 : 1);
     const int cl = npairs < 16 ? npairs : 16;
     const int wpc = blk ? JC_NT / 32 : std::min(4, (npairs + cl - 1) / cl);  // warps loop over pairs
-    static bool nonportable_set[3] = {false, false, false};
-    const int ns = blk ? 2 : (sizeof(T) == 8);
-    if (cl > 8 && !nonportable_set[ns]) {
-      if (blk) QR_CUDA(cudaFuncSetAttribute(jacobi_block_cluster_k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-      else QR_CUDA(cudaFuncSetAttribute(jacobi_cluster_k<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-      nonportable_set[ns] = true;
+    if (cl > 8) {
+      const void* f = blk ? (const void*)jacobi_block_cluster_k : (const void*)jacobi_cluster_k<T>;
+      QR_TRY(set_func_attr_once(f, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(cl);
@@ -1600,14 +1596,10 @@ int jacobi(cudaStream_t s, SvdWork* w, cplx_t<T>* B, long ldb, int rows, int k, 
   } else if (sizeof(T) == 4 && rows <= JR_MAXROWS) {
     // FP32 with the rows in registers: block Jacobi (4-column blocks, pairs of blocks)
     const int nb = (k + JR_W - 1) / JR_W, nbp = nb + (nb & 1);
-    static int per_sm = 0, sms = 0;
-    if (per_sm == 0) {
-      int dev = 0;
-      QR_CUDA(cudaGetDevice(&dev));
-      QR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-      QR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, jacobi_block_reg_k, JR_NT, 0));
-      if (per_sm < 1) return fail(QR_ECUDA, "block Jacobi sweep kernel cannot be resident");
-    }
+    int per_sm = 0, sms = 0;
+    QR_TRY(device_sm_count(&sms));
+    QR_TRY(blocks_per_sm((const void*)jacobi_block_reg_k, JR_NT, 0, &per_sm));
+    if (per_sm < 1) return fail(QR_ECUDA, "block Jacobi sweep kernel cannot be resident");
     int grid = std::min(per_sm * sms, nbp / 2);
     if (grid < 1) grid = 1;
     for (int sweep = 0; sweep < max_sweeps; sweep++) {
@@ -1624,17 +1616,11 @@ int jacobi(cudaStream_t s, SvdWork* w, cplx_t<T>* B, long ldb, int rows, int k, 
       count_launch();
     }
   } else {
-    static int per_sm_cache[2] = {0, 0};
-    static int sms_cache = 0;
-    int& per_sm = per_sm_cache[sizeof(T) == 8 ? 1 : 0];
-    if (per_sm == 0 || sms_cache == 0) {
-      int dev = 0;
-      QR_CUDA(cudaGetDevice(&dev));
-      QR_CUDA(cudaDeviceGetAttribute(&sms_cache, cudaDevAttrMultiProcessorCount, dev));
-      QR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, jacobi_sweep_dev_k<T, NT, RPT>, NT, 0));
-      if (per_sm < 1) return fail(QR_ECUDA, "Jacobi sweep kernel cannot be resident");
-    }
-    int grid = per_sm * sms_cache;
+    int per_sm = 0, sms = 0;
+    QR_TRY(device_sm_count(&sms));
+    QR_TRY(blocks_per_sm((const void*)jacobi_sweep_dev_k<T, NT, RPT>, NT, 0, &per_sm));
+    if (per_sm < 1) return fail(QR_ECUDA, "Jacobi sweep kernel cannot be resident");
+    int grid = per_sm * sms;
     if (grid > np / 2) grid = np / 2;
     if (grid < 1) grid = 1;
     for (int sweep = 0; sweep < max_sweeps; sweep++) {
@@ -1706,18 +1692,12 @@ int jacobi_df(cudaStream_t s, SvdWork* w, float2* Bh, float2* Bl, long ldb, int 
   QR_CUDA(cudaMemsetAsync(state, 0, sizeof(unsigned) * (nstate + np), s));
   // V staging buffer: 4 columns (hi, lo of p and q) of k rows; k <= 4096 keeps two CTAs per SM
   const size_t vsm = (k % 2 == 0 && ldv % 2 == 0 && k <= 4096) ? sizeof(float2) * 4 * (size_t)k : 0;
-  static int per_sm = 0, sms = 0;
-  static size_t vsm_cached = (size_t)-1;
-  if (vsm != vsm_cached) {
-    int dev = 0;
-    QR_CUDA(cudaGetDevice(&dev));
-    QR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    QR_CUDA(cudaFuncSetAttribute(jacobi_sweep_df_k<NT, RPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)sizeof(float2) * 4 * 4096));
-    QR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, jacobi_sweep_df_k<NT, RPT>, NT, vsm));
-    if (per_sm < 1) return fail(QR_ECUDA, "double-float sweep kernel cannot be resident");
-    vsm_cached = vsm;
-  }
+  int per_sm = 0, sms = 0;
+  QR_TRY(device_sm_count(&sms));
+  QR_TRY(set_func_attr_once((const void*)jacobi_sweep_df_k<NT, RPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)sizeof(float2) * 4 * 4096));
+  QR_TRY(blocks_per_sm((const void*)jacobi_sweep_df_k<NT, RPT>, NT, vsm, &per_sm));
+  if (per_sm < 1) return fail(QR_ECUDA, "double-float sweep kernel cannot be resident");
   int grid = std::min(per_sm * sms, np / 2);
   if (grid < 1) grid = 1;
   int pr = prof_begin(s, PK_JACOBI_DF, 0.0, 0.0);
@@ -1727,11 +1707,7 @@ int jacobi_df(cudaStream_t s, SvdWork* w, float2* Bh, float2* Bl, long ldb, int 
     const int npairs = np / 2 > 0 ? np / 2 : 1;
     const int cl = npairs < 16 ? npairs : 16;
     const int wpc = std::min(4, (npairs + cl - 1) / cl);
-    static bool nonportable_set = false;
-    if (cl > 8 && !nonportable_set) {
-      QR_CUDA(cudaFuncSetAttribute(jacobi_cluster_df_k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-      nonportable_set = true;
-    }
+    if (cl > 8) QR_TRY(set_func_attr_once((const void*)jacobi_cluster_df_k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(cl);
     cfg.blockDim = dim3(32 * wpc);
