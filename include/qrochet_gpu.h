@@ -52,10 +52,12 @@ typedef struct qr_mpo qr_mpo;     /* one open-boundary MPO resident in device me
 
 /* Precision of a chain's arithmetic (qr_chain_set_precision), a bit mask. */
 #define QR_FP64 0           /* plain: all ComplexF64 */
-#define QR_MIXED 1          /* SVD with more than 128 columns: FP32 Jacobi preconditioner, then
-                               Newton-Schulz, B = A X and Jacobi polish in double-float (FP32 pairs,
-                               ~2^-48) on the FP32 pipes; theta, singular values and vectors and the
-                               truncation cutoff stay FP64.  Smaller SVDs run the FP64 Jacobi. */
+#define QR_MIXED 1          /* two-site gates whose theta has more than 16 columns: theta formed by a
+                               double-float GEMM (FP32 pairs, ~2^-48, on the FP32 pipes; the gate is
+                               applied in FP64), then an SVD with an FP32 Jacobi preconditioner and
+                               double-float Newton-Schulz, B = A X and Jacobi polish; singular values
+                               and vectors and the truncation cutoff stay FP64.  Smaller SVDs run the
+                               FP64 Jacobi. */
 #define QR_SPLIT_CONTRACT 2 /* environment contractions (expect, overlap, norm, MPO expectation) on
                                the BF16 tensor cores with 3-way BF16 splits, FP32 accumulation */
 
