@@ -61,7 +61,6 @@ int ztranspose(cudaStream_t s, const double2* src, long lds, int rows, int cols,
 int zset_identity(cudaStream_t s, double2* A, int rows, int cols, long lda);
 int cset_identity(cudaStream_t s, float2* A, int rows, int cols, long lda);
 int z2c(cudaStream_t s, const double2* src, long lds, float2* dst, long ldd, int rows, int cols);
-int c2z(cudaStream_t s, const float2* src, long lds, double2* dst, long ldd, int rows, int cols);
 // out[0] = || G - I ||_F for the n x n matrix G (ld n); out is device memory
 int zdist_identity(cudaStream_t s, const double2* G, int n, double* out);
 // lam[i] /= norm2(lam) in place (device)

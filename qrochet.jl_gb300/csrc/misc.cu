@@ -176,15 +176,6 @@ __global__ void z2c_k(const double2* __restrict__ s, long lds, float2* __restric
   }
 }
 
-__global__ void c2z_k(const float2* __restrict__ s, long lds, double2* __restrict__ d, long ldd, int rows, int cols) {
-  long total = (long)rows * cols;
-  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
-    long i = t % rows, j = t / rows;
-    float2 v = s[i + j * lds];
-    d[i + j * ldd] = make_double2((double)v.x, (double)v.y);
-  }
-}
-
 __device__ double block_sum(double v) {
   __shared__ double red[32];
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -306,13 +297,6 @@ int z2c(cudaStream_t s, const double2* src, long lds, float2* dst, long ldd, int
   if (rows <= 0 || cols <= 0) return QR_OK;
   z2c_k<<<grid_for((long)rows * cols), TPB, 0, s>>>(src, lds, dst, ldd, rows, cols);
   QR_CHECK_LAUNCH("z2c_k");
-  return QR_OK;
-}
-
-int c2z(cudaStream_t s, const float2* src, long lds, double2* dst, long ldd, int rows, int cols) {
-  if (rows <= 0 || cols <= 0) return QR_OK;
-  c2z_k<<<grid_for((long)rows * cols), TPB, 0, s>>>(src, lds, dst, ldd, rows, cols);
-  QR_CHECK_LAUNCH("c2z_k");
   return QR_OK;
 }
 
