@@ -44,7 +44,7 @@ def parse():
     p.add_argument("--steps", type=int, default=6)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--fp64-steps", type=int, default=2)
+    p.add_argument("--fp64-steps", type=int, default=6)
     p.add_argument("--cpu-steps", type=int, default=2)
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--quick", action="store_true", help="small chi for a fast functional run")
@@ -56,6 +56,7 @@ def parse():
                    help="requests in the saturated mixed-precision serving sample (0: skip)")
     p.add_argument("--mpo-sites", type=int, default=128, help="sites of the MPO environment sweep (0: skip)")
     p.add_argument("--workers", type=int, default=16)
+    p.add_argument("--no-tebd", action="store_true", help="skip the n=64, chi_max=256, depth-40 TEBD leg")
     return p.parse_args()
 
 
@@ -132,10 +133,9 @@ class DevTimer:
         return self.e0.elapsed_time(self.e1) * 1e-3
 
 
-# DRAM bytes (read + write) per launch from one ncu capture of each kernel on a 1024 x 1024 mixed
-# SVD (profiles/jacobi_block_reg_fp32_1024.md, jacobi_sweep_df_1024.md, zgemm_df_1024.md).  The
-# sweeps' traffic is the first touch of B and V and the GEMM's the first touch of its operands,
-# so it scales with the operand size: (k / 1024)^2 at k columns.
+# DRAM bytes (read + write) per launch (one Jacobi sweep, or one GEMM) from one ncu capture of each
+# kernel on a 1024 x 1024 mixed SVD.  A sweep's traffic is the first touch of B and V and a GEMM's
+# the first touch of its operands, so it scales with the operand size: (k / 1024)^2 at k columns.
 NCU_TRAFFIC_1024 = {"jacobi_fp32": 16.937472e6 + 15.872e3, "jacobi_df": 33.711360e6 + 28.087296e6,
                     "zgemm_df": 16.850432e6}
 
@@ -217,25 +217,51 @@ def cpu_gate_step(al, ar, lam, u, maxdim):
 
 
 def run_batched(args, Q, dist, rank, world):
-    """Batched solves/s: requests of the batched distribution (n ~ U[8,96], depth ~ U[4,32],
-    cutoff 1e-10, mixed precision) all submitted at once to the continuous-batching server.
-    chi_max is drawn log-uniformly from {16, 32, 64} (a bounded sample of the {16..512} range:
-    chi_max = 512 requests take minutes each at this part's FP64 rate)."""
+    """Batched solves/s on requests of the batched distribution (n ~ U[8,96], depth ~ U[4,32],
+    cutoff 1e-10) with chi_max log-uniform in {16, 32, 64}: the bond classes the batched engine
+    takes (theta up to 128 x 128).  Two paths on the same requests:
+      - engine: qr_batch -- every layer of all requests one fused launch, device-side truncation,
+        the whole circuit one CUDA graph (FP64 SVD);
+      - server: the continuous-batching request server, one chain and stream per request, mixed
+        precision.
+    The chi_max in {128, 256, 512} part of the distribution is outside the engine's bond limit and
+    takes minutes per request on the server: not in this sample."""
     from qrochet import serve as S
+    from qrochet.batch import Batch
 
     reqs = shard(S.batched_requests(args.batched, seed=4, chi_log2=(4, 6), nobs=1), rank, world)
     gates = dist.sum(sum(len(r.gates) for r in reqs))
+    out = {"requests": int(dist.sum(len(reqs))), "gates": int(gates),
+           "sample": f"{args.batched} requests: n~U[8,96], depth~U[4,32], chi_max log-uniform in {{16,32,64}}, "
+                     f"cutoff 1e-10, 1 Pauli string each, seed 4"}
+    with Batch(device=0) as bt:
+        for r in reqs:
+            bt.add(r)
+        dist.barrier()
+        t0 = time.perf_counter()
+        bt.run()
+        dt = dist.max(time.perf_counter() - t0)
+        info = bt.info()
+        vals_engine = [bt.values(i) for i in range(len(reqs))]
+    out["engine"] = {"solves_per_s": out["requests"] / dt, "gate_steps_per_s": gates / dt, "wall_s": dt,
+                     "graph_ms": info["graph_ms"], "autotune_ms": info["tune_ms"], "layers": info["layers"],
+                     "launches": info["launches"], "graph_nodes": info["graph_nodes"],
+                     "warps_per_cta": info["warps_per_cta"], "precision": "fp64"}
     with S.Server(workers=args.workers, precision="mixed") as sv:
         dist.barrier()
         t0 = time.perf_counter()
         tickets = [sv.submit(r) for r in reqs]
-        lat = [sv.wait(t)["latency_ms"] for t in tickets]
+        res = [sv.wait(t) for t in tickets]
         dt = dist.max(time.perf_counter() - t0)
-    lat = dist.gather(lat)
-    return {"requests": len(lat), "solves_per_s": len(lat) / dt, "gate_steps_per_s": gates / dt,
-            "wall_s": dt, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-            "workers": args.workers, "precision": "mixed",
-            "sample": "n~U[8,96], depth~U[4,32], chi_max log-uniform in {16,32,64}, cutoff 1e-10, seed 4"}
+    lat = dist.gather([x["latency_ms"] for x in res])
+    out["server"] = {"solves_per_s": out["requests"] / dt, "gate_steps_per_s": gates / dt, "wall_s": dt,
+                     "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                     "workers": args.workers, "precision": "mixed"}
+    diffs = [float(np.max(np.abs(a - x["values"])) / max(1e-300, float(np.max(np.abs(x["values"])))))
+             for a, x in zip(vals_engine, res)]
+    out["max_rel_diff_engine_vs_server"] = dist.max(max(diffs) if diffs else 0.0)
+    out["engine_over_server"] = out["engine"]["solves_per_s"] / out["server"]["solves_per_s"]
+    return out
 
 
 def run_serving(args, Q, dist, rank, world):
@@ -327,8 +353,51 @@ def run_mpo_env(args, Q):
                     "flops = algorithmic count of both contractions over the actual bond dims"}
 
 
+def run_tebd(args, Q, local):
+    """TEBD at full size: n = 64 qubits from |0...0>, a depth-40 brick wall of Haar 4 x 4 gates
+    (seed 2), maxdim 256, cutoff 1e-10, in FP64 and in the mixed path.  Errors of every bond's
+    Lambda spectrum and of <X_i> are taken against the oracle's golden results for the same gates
+    (tests/golden/tebd_n64_chi256_d40.npz, written by make_tebd_golden.py next to it)."""
+    from qrochet import random as R
+
+    gold = np.load(os.path.join(ROOT, "tests", "golden", "tebd_n64_chi256_d40.npz"))
+    n, depth, maxdim = 64, 40, 256
+    layers = R.brickwall_layers(n, depth, seed=2)
+    ngates = sum(len(layer) for layer in layers)
+    lam_gold = np.split(gold["lambdas"], np.cumsum(gold["bond_dims"])[:-1])
+    out = {"n": n, "depth": depth, "chi_max": maxdim, "threshold": 1e-10, "gates": ngates,
+           "note": "evolve! defaults (iscanonical=false): Lambdas stay on the bonds and theta is truncated "
+                   "without the neighbouring weights, so the norm decays (oracle: %.3g); <X_i> errors are "
+                   "relative to <psi|psi>" % float(gold["norm"])}
+    for prec in ("fp64", "mixed"):
+        psi = Q.MPS(R.zero_product_arrays(n))
+        psi.set_precision(prec)
+        psi.sync()
+        t = DevTimer(psi.stream(), local)
+        t.start()
+        for layer in layers:
+            for s_, u in layer:
+                Q.evolve_(psi, Q.gate_from_matrix(u, [s_, s_ + 1]), threshold=1e-10, maxdim=maxdim)
+        dt = t.stop()
+        bonds = psi.bond_dims()
+        same = bonds == [int(b) for b in gold["bond_dims"]]
+        lam_err = max(float(np.max(np.abs(psi.lambda_between(b + 1, b + 2) - lam_gold[b])) / lam_gold[b][0])
+                      for b in range(n - 1)) if same else None
+        x = np.array([Q.expect(psi, [Q.gate_from_matrix(R.PAULI["X"], [i])]) for i in range(1, n + 1)])
+        nrm2 = float(gold["norm"]) ** 2
+        out[prec] = {"gate_steps_per_s": ngates / dt, "s": dt, "bond_dims_match_oracle": same,
+                     "lambda_max_rel_err_vs_oracle": lam_err,
+                     "x_max_abs_err_vs_oracle_over_norm2": float(np.max(np.abs(x - gold["x"]))) / nrm2,
+                     "norm_rel_err_vs_oracle": abs(Q.norm(psi) - float(gold["norm"])) / float(gold["norm"]),
+                     "max_bond": int(max(bonds))}
+        del psi
+    out["mixed_over_fp64"] = out["mixed"]["gate_steps_per_s"] / out["fp64"]["gate_steps_per_s"]
+    return out
+
+
 def run_reference(args, chi):
-    """CPU restatement on all host threads (the Julia reference is not installed)."""
+    """CPU restatement on all host threads (the Julia reference is not installed).  Runs the
+    requested --steps gate steps (one untimed warm-up step: the CPU path needs no more)."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
@@ -336,7 +405,7 @@ def run_reference(args, chi):
     from oracle import chain_oracle as O
 
     ch = O.from_reference_arrays(arrays)
-    steps = max(1, min(args.steps, 3))
+    steps = max(1, args.steps)
     warm = min(args.warmup, 1)
     b = BONDS[0] - 1
     al, ar = ch.sites[b], ch.sites[b + 1]
@@ -345,7 +414,7 @@ def run_reference(args, chi):
         cpu_gate_step(al, ar, lam, gates[i], MAXDIM if chi == CHI else chi)
     t0 = time.perf_counter()
     for i in range(steps):
-        cpu_gate_step(al, ar, lam, gates[i], MAXDIM if chi == CHI else chi)
+        cpu_gate_step(al, ar, lam, gates[i % len(gates)], MAXDIM if chi == CHI else chi)
     dt = time.perf_counter() - t0
     v = steps / dt
     cores = os.cpu_count()
@@ -355,21 +424,23 @@ def run_reference(args, chi):
             "config": {"workload": f"tebd_gate_step_chi{chi}", "chi": chi, "theta": f"{2 * chi}x{2 * chi}",
                        "maxdim": MAXDIM if chi == CHI else chi, "threshold": CUTOFF, "n_sites": N_SITES},
             "cpu_baseline": {"value": v, "unit": "gate-steps/s", "cores": cores, "kind": "port",
-                             "sample": f"{steps} gate-steps of the {args.steps} requested (NumPy/LAPACK "
-                                       f"restatement of Chain.jl evolve_2site!+truncate!; Qrochet.jl is Julia "
-                                       f"and is not installed)"},
+                             "sample": f"{steps} gate-steps, {warm} untimed warm-up (NumPy/LAPACK restatement of "
+                                       f"Chain.jl evolve_2site!+truncate!, zgesdd on all host threads; Qrochet.jl "
+                                       f"is Julia and is not installed)"},
             "e2e": {"value": v, "unit": "gate-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
 def run_ours(args, chi):
     import qrochet as Q
+    from qrochet import random as R
 
     rank, world, local = dist_env()
     dist = Dist(world)
     Q.set_device(local)
     arrays, gates = workload(chi)
     maxdim = MAXDIM if chi == CHI else chi
+    b0 = BONDS[0]
 
     def make(prec):
         psi = Q.MPS(arrays)
@@ -380,9 +451,16 @@ def run_ours(args, chi):
         b = BONDS[i % len(BONDS)]
         Q.evolve_(psi, Q.gate_from_matrix(gates[i % len(gates)], [b, b + 1]), threshold=CUTOFF, maxdim=maxdim)
 
+    def local_z(psi):
+        return np.array([Q.expect(psi, [Q.gate_from_matrix(R.PAULI["Z"], [s])]) for s in (b0, b0 + 1)])
+
     # ---- mixed path, state resident in HBM -------------------------------------------------------
+    # Step 0 (gate 0 on bond (b0, b0 + 1) of the initial state) is also the accuracy sample: the
+    # FP64 path and the oracle run the same gate on the same theta below.
     psi = make("mixed")
-    for i in range(args.warmup):
+    step(psi, 0)
+    acc_mixed = (psi.lambda_between(b0, b0 + 1).copy(), local_z(psi), psi.bond_dims()[b0 - 1])
+    for i in range(1, args.warmup):
         step(psi, i)
     psi.sync()
     clocks = Clocks(local)
@@ -400,6 +478,7 @@ def run_ours(args, chi):
     clk = clocks.stop()
     dt_max = dist.max(dt)
     value = world * args.steps / dt_max
+    del psi
     if args.launch_list:
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": "gate-steps/s", "steps": args.steps,
@@ -408,9 +487,11 @@ def run_ours(args, chi):
 
     # ---- plain FP64 path ---------------------------------------------------------------------------
     fp64 = None
+    acc_fp64 = None
     if args.fp64_steps > 0:
         p64 = make("fp64")
         step(p64, 0)
+        acc_fp64 = (p64.lambda_between(b0, b0 + 1).copy(), local_z(p64), p64.bond_dims()[b0 - 1])
         p64.sync()
         t64 = DevTimer(p64.stream(), local)
         dist.barrier()
@@ -423,91 +504,129 @@ def run_ours(args, chi):
         del p64
 
     # ---- e2e through the C ABI with pinned host buffers --------------------------------------------
-    pin = {}
-    for b in sorted({x for bb in BONDS for x in (bb, bb + 1)}):
-        pa = Q.PinnedArray(arrays[b - 1].shape)
-        pa.array[...] = arrays[b - 1]
-        po = Q.PinnedArray(arrays[b - 1].shape)
-        pin[b] = (pa, po)
+    # The same state sequence as `value`: the same warm-up and gates, with the two sites of every
+    # step uploaded from page-locked host copies of the current state before it and downloaded
+    # into them after it (plus the bond's Lambda), so each step moves the state through the host.
     pe = make("mixed")
-    h2d = d2h = 0
+    for i in range(args.warmup):
+        step(pe, i)
+    pin = {}
+    for s_ in sorted({x for bb in BONDS for x in (bb, bb + 1)}):
+        cl, d, cr = pe.site_dims(s_)
+        pa = Q.PinnedArray((d, cl, cr))
+        pe.download_site(s_, pa.array)
+        pin[s_] = pa
     pe.sync()
+    h2d = d2h = 0
     te = DevTimer(pe.stream(), local)
     dist.barrier()
     te.start()
     for i in range(args.steps):
-        b = BONDS[i % len(BONDS)]
-        for s in (b, b + 1):
-            pe.upload_site(s, pin[s][0].array)
-        step(pe, i)
-        for s in (b, b + 1):
-            pe.download_site(s, pin[s][1].array)
+        b = BONDS[(args.warmup + i) % len(BONDS)]
+        for s_ in (b, b + 1):
+            pe.upload_site(s_, pin[s_].array)
+        step(pe, args.warmup + i)
+        for s_ in (b, b + 1):
+            pe.download_site(s_, pin[s_].array)
         lam = pe.lambda_between(b, b + 1)
         if i == 0:
-            h2d = 2 * pin[b][0].array.nbytes + 16 * 16
-            d2h = 2 * pin[b][1].array.nbytes + lam.nbytes
+            h2d = pin[b].array.nbytes + pin[b + 1].array.nbytes + 16 * 16
+            d2h = pin[b].array.nbytes + pin[b + 1].array.nbytes + lam.nbytes
     de = dist.max(te.stop())
     e2e = {"value": world * args.steps / de, "unit": "gate-steps/s", "h2d_bytes_per_step": int(h2d),
-           "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * de / args.steps}
+           "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * de / args.steps,
+           "note": "same gates and state sequence as value; both sites of each step uploaded from and "
+                   "downloaded to page-locked host memory, plus the gate and the bond's Lambda"}
     del pe
 
-    # ---- roofline of the dominant kernel (separate instrumented pass) -------------------------------
+    # ---- roofline: algorithmic work of the whole gate step, plus the dominant kernel's pipe use ----
     Q.prof_enable(True)
     pr = make("mixed")
-    for i in range(min(3, args.steps)):
+    nprof = min(3, args.steps)
+    for i in range(nprof):
         step(pr, i)
     pr.sync()
     stats = {k: Q.prof_read(k) for k in Q.PROF_KINDS}
     Q.prof_enable(False)
     del pr
     dom = max(stats, key=lambda k: stats[k]["ms"])
-    peaks = {"zgemm_dmma": ("dmma", "tensor"), "jacobi_fp32": ("ffma", "fp32"), "jacobi_fp64": ("dfma", "fp64"),
-             "householder_qr": ("dfma", "fp64"), "env_mix": ("dfma", "fp64"), "jacobi_df": ("ffma", "fp32"),
-             "zgemm_split_bf16": ("bf16", "tensor")}
-    pk_kind, bound = peaks[dom]
     try:
         mp = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except Exception:
         mp = {}
-    if pk_kind == "bf16":  # the split GEMM's products run on the BF16 tensor pipe
-        peak = mp.get("bf16_tflops") or 1900.0
-    else:
-        peak = Q.probe_peak(pk_kind)
+    ffma = Q.probe_peak("ffma")
     st = stats[dom]
-    achieved = st["flops"] / (st["ms"] * 1e-3) / 1e12 if st["ms"] > 0 else 0.0
+    executed = st["flops"] / (st["ms"] * 1e-3) / 1e12 if st["ms"] > 0 else 0.0
     shares = {k: round(v["ms"] / max(1e-9, sum(x["ms"] for x in stats.values())), 4) for k, v in stats.items()}
-    roofline = {"bound": bound, "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak if peak else None,
-                "traffic": (NCU_TRAFFIC_1024[dom] * (2 * chi / 1024) ** 2 if dom in NCU_TRAFFIC_1024 else None),
-                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch at k = 1024, "
-                                  "scaled by (k / 1024)^2 to k = 2 chi",
-                "peak_source": ("measured cuBLAS bf16 (MEASURED_PEAKS.json)" if pk_kind == "bf16" else
-                                f"measured in-process ({pk_kind} loop kernel, best of 3)"),
-                "launches": st["launches"], "avg_launch_ms": st["ms"] / max(1, st["launches"]),
+    ms_step = 1e3 * dt_max / args.steps
+    alg = gate_flops(chi)
+    achieved = alg / (ms_step * 1e-3) / 1e12
+    # DRAM traffic per gate step: ncu bytes per launch (per sweep for the Jacobi kernels) times the
+    # launches (sweeps) per step of each profiled class
+    traffic = sum(NCU_TRAFFIC_1024[k] * (2 * chi / 1024) ** 2 * stats[k]["launches"] / nprof
+                  for k in NCU_TRAFFIC_1024)
+    roofline = {"bound": "fp32", "kernel": "gate step (all kernels of one evolve!)", "achieved": achieved,
+                "peak": ffma, "unit": "TFLOP/s", "frac": achieved / ffma if ffma else None,
+                "traffic": traffic, "launches": launches / max(1, args.steps), "avg_launch_ms": ms_step,
+                "achieved_source": f"algorithmic count {alg:.3e} flop per gate step (theta GEMM + gate + "
+                                   f"Golub-Van Loan R-SVD count of a {2 * chi}x{2 * chi} complex SVD) / ms_per_step",
+                "peak_source": "FP32 FFMA rate measured in-process (loop kernel, best of 3): the mixed path runs "
+                               "on the FP32 pipes; MEASURED_PEAKS.json holds only HBM and cuBLAS BF16",
+                "traffic_source": "DRAM bytes per gate step: ncu dram__bytes_read.sum + dram__bytes_write.sum per "
+                                  "launch (one Jacobi sweep, one GEMM) at k = 1024 scaled by (k / 1024)^2, times "
+                                  "the launches per step of jacobi_fp32, jacobi_df and zgemm_df",
+                "units": "launches and traffic per gate step; avg_launch_ms = ms per gate step",
+                "pipe_busy": {"kernel": dom, "executed_tflops": executed, "frac_of_ffma": executed / ffma if ffma else None,
+                              "sweeps_per_step": st["launches"] / nprof,
+                              "avg_sweep_ms": st["ms"] / max(1, st["launches"]),
+                              "traffic_per_sweep": (NCU_TRAFFIC_1024.get(dom, 0.0) * (2 * chi / 1024) ** 2) or None,
+                              "note": "FP32 instructions the kernel class executes (compensated inner products and "
+                                      "rotations) per second, not algorithmic work"},
                 "time_share": shares}
     if mp:
         roofline["measured_peaks_json"] = {"hbm_gbs": mp.get("hbm_gbs"), "bf16_tflops": mp.get("bf16_tflops")}
 
-    # ---- CPU baseline (rank 0, bounded sample) ------------------------------------------------------
+    # ---- CPU baseline (rank 0, bounded sample) and the oracle's spectrum of gate 0 ---------------
     cpu = None
+    lam_oracle = None
     if rank == 0 and not args.no_cpu and args.cpu_steps > 0:
         from oracle import chain_oracle as O
 
         ch = O.from_reference_arrays(arrays)
-        b = BONDS[0] - 1
+        b = b0 - 1
         al, ar = ch.sites[b], ch.sites[b + 1]
         lam = np.ones(al.shape[2])
         t3 = time.perf_counter()
         for i in range(args.cpu_steps):
-            cpu_gate_step(al, ar, lam, gates[i], maxdim)
+            res = cpu_gate_step(al, ar, lam, gates[i], maxdim)
+            if i == 0:
+                lam_oracle = res.lam[1].copy()
         dc = time.perf_counter() - t3
         cpu = {"value": args.cpu_steps / dc, "unit": "gate-steps/s", "cores": os.cpu_count(), "kind": "port",
                "sample": f"{args.cpu_steps} gate-steps at chi={chi} (NumPy/LAPACK zgesdd restatement, all host "
                          f"threads)"}
 
+    accuracy = None
+    if acc_fp64 is not None:
+        lm, zm, bm = acc_mixed
+        lf, zf, bf = acc_fp64
+        smax = float(lf[0])
+        accuracy = {"sample": f"gate 0 on bond ({b0},{b0 + 1}) of the initial state, chi = {chi} both sides",
+                    "bond_dim": {"mixed": int(bm), "fp64": int(bf)},
+                    "lambda_max_abs_err_mixed_vs_fp64_over_sigma_max":
+                        float(np.max(np.abs(lm - lf)) / smax) if lm.size == lf.size else None,
+                    "z_local_max_abs_err_mixed_vs_fp64": float(np.max(np.abs(zm - zf))),
+                    "z_local_fp64": [float(x.real) for x in zf]}
+        if lam_oracle is not None:
+            accuracy["bond_dim"]["oracle"] = int(lam_oracle.size)
+            for nm, lv in (("mixed", lm), ("fp64", lf)):
+                accuracy[f"lambda_max_abs_err_{nm}_vs_oracle_over_sigma_max"] = (
+                    float(np.max(np.abs(lv - lam_oracle)) / lam_oracle[0]) if lv.size == lam_oracle.size else None)
+
     batched = run_batched(args, Q, dist, rank, world) if (args.batched > 0 and not args.quick) else None
     serving = run_serving(args, Q, dist, rank, world) if (args.serve > 0 and not args.quick) else None
     mpo_env = run_mpo_env(args, Q) if (args.mpo_sites > 0 and not args.quick) else None
+    tebd = run_tebd(args, Q, local) if not (args.no_tebd or args.quick) else None
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "gate-steps/s", "n_gpus": world, "steps": args.steps,
@@ -519,10 +638,10 @@ def run_ours(args, chi):
                            "maxdim": maxdim, "threshold": CUTOFF, "n_sites": N_SITES, "precision": "mixed",
                            "parallelism": "replicas" if world > 1 else "single",
                            "l2": "inputs larger than L2 (>129 MB touched per step)"},
-                "fp64": fp64, "mixed_over_fp64": (value / fp64["value"]) if fp64 else None,
+                "fp64": fp64, "mixed_over_fp64": (value / fp64["value"]) if fp64 else None, "accuracy": accuracy,
                 "gflop_per_step": gate_flops(chi) / 1e9, "e2e": e2e, "gpu_launches": launches,
                 "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
-                "batched": batched, "serving": serving, "mpo_env": mpo_env}
+                "batched": batched, "serving": serving, "mpo_env": mpo_env, "tebd_n64_chi256": tebd}
         print(json.dumps(line), flush=True)
 
 

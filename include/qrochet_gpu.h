@@ -74,14 +74,6 @@ int qr_set_device(int device);
 /* number of kernels this library has launched in this process (for launch accounting) */
 int qr_launch_count(uint64_t* count);
 
-/* per-kernel-class CUDA-event timing, for benchmarks: kinds 0 zgemm (FP64 DMMA), 1 Jacobi FP64,
-   2 Jacobi FP32, 3 Householder QR, 4 environment mixing, 5 split-precision tensor-core zgemm,
-   6 double-float Jacobi polish, 7 double-float zgemm.
-   No reference counterpart. */
-int qr_prof_enable(int on);
-int qr_prof_read(int kind, double* ms, uint64_t* launches, double* flops, double* bytes);
-/* peak of one pipe measured now: 0 FP64 tensor (DMMA), 1 FP32 FFMA, 2 FP64 DFMA (TFLOP/s) */
-int qr_probe_peak(int kind, double* tflops);
 /* page-locked host buffers for host<->device copies (cudaHostAlloc). */
 int qr_host_alloc(uint64_t bytes, void** ptr);
 int qr_host_free(void* ptr);
@@ -106,10 +98,11 @@ int qr_chain_set_lambda(qr_chain* h, int bond, const double* lam, int len);
 int qr_chain_ntensors(const qr_chain* h, int* out);
 int qr_chain_nsites(const qr_chain* h, int* out);
 int qr_chain_set_precision(qr_chain* h, int mode);
-/* Checkpoint / export (SURVEY next row: round trip with Julia).  The file holds the site arrays
-   in the reference's (:o, :l, :r) column-major layout (open ends without l / r), the bond
-   dimensions, the Lambda vectors and the precision; little-endian, layout documented in
-   INTEGRATION.md.  No reference counterpart beyond MPS(arrays) on the Julia side. */
+/* Checkpoint / export for a round trip with Julia, little-endian:
+   "QRCHAIN1" | int32 n, d, precision, periodic | int32 bond_dims[n-1, or n when periodic]
+   | uint8 has_lambda[n-1] | per site its complex128 array in the reference's (o, l, r)
+   column-major layout (open ends without l / r) | per bond with has_lambda: float64 Lambda.
+   No reference counterpart beyond MPS(arrays) on the Julia side. */
 int qr_chain_save(const qr_chain* h, const char* path);
 int qr_chain_load(const char* path, qr_chain** out);
 int qr_chain_get_precision(const qr_chain* h, int* mode);
@@ -180,6 +173,33 @@ int qr_server_wait(qr_server* s, uint64_t ticket, double timeout_s, int* done, i
 int qr_server_stats(qr_server* s, uint64_t* submitted, uint64_t* completed, int* in_flight, uint64_t* hbm_in_use,
                     int* queued);
 
+/* ---- batched engine: many independent simulate-and-measure requests evolved together (the
+   batched workload; no reference counterpart beyond the per-chain calls it fuses: evolve! +
+   truncate!, Chain.jl:606-661 and 390-422, and expect, Chain.jl:724-735).  Requests have the
+   qr_server_submit format (a gate circuit on |0...0>, then Pauli strings) with chi_max <= 64.
+   qr_batch_run keeps every chain in fixed-capacity device buffers, takes each truncation decision
+   on the device, runs each brick-wall layer of all requests as one fused launch (one CTA per
+   gate: theta, gate, FP64 Jacobi SVD, truncation, write-back), captures the whole circuit and the
+   expectation sweep in one CUDA graph and launches it once.  The layer kernel's CTA size is
+   autotuned per device and bond class (cached in the process, and in the file named by
+   QROCHET_TUNE_FILE when set).  A request whose truncation would empty a bond, or whose SVD did
+   not converge, gets a nonzero status (QR_EINVAL / QR_ENOCONV) in qr_batch_result. */
+typedef struct qr_batch qr_batch;
+int qr_batch_create(int device, qr_batch** out);
+int qr_batch_free(qr_batch* b);
+int qr_batch_add(qr_batch* b, int n, int chi_max, double threshold, int ngates, const int* gate_site,
+                 const double* gate_mats, int nobs, const int* obs_weight, const int* obs_sites,
+                 const int* obs_paulis, int* id);
+/* layer of every gate of request id (a gate starts a new layer when it shares a site with the
+   current one); host-only */
+int qr_batch_plan(const qr_batch* b, int id, int* layer_of_gate, int* nlayers);
+int qr_batch_run(qr_batch* b, double* ms);
+int qr_batch_result(const qr_batch* b, int id, int* status, double* values /* 2 per string */);
+int qr_batch_bond_dims(const qr_batch* b, int id, int* out /* n-1 */);
+int qr_batch_lambda(const qr_batch* b, int id, int bond, double* out, int* len);
+int qr_batch_info(const qr_batch* b, int* layers, int* launches, int* graph_nodes, int* warps, int* cached,
+                  double* run_ms, double* tune_ms);
+
 /* ---- allocation-free thin SVD (no counterpart in the reference) ----------------------------
    For callers that must not have a library allocate device memory (a Julia process whose CUDA.jl
    pool owns the device, a serving loop that allocates only at start-up).  Plain FP64 Jacobi SVD
@@ -192,21 +212,6 @@ int qr_server_stats(qr_server* s, uint64_t* submitted, uint64_t* completed, int*
    device address; make that first call before any stream capture.  No cudaMalloc/cudaFree. */
 int qr_svd_noalloc(int m, int n, const double* A, long lda, double* U, long ldu, double* S, double* Vh,
                    long ldvh, void* stream);
-
-/* ---- kernel-level test hooks (no reference counterpart): host matrices in and out, complex
-   interleaved, column-major; op codes 0 N, 1 T, 2 C (conjugate transpose), 3 R (conjugate) ----- */
-int qr_test_zgemm(int opA, int opB, int M, int N, int K, const double* alpha, const double* A, long lda,
-                  const double* B, long ldb, const double* beta, double* C, long ldc, const double* dk,
-                  int iters, double* ms_per_iter);
-int qr_test_zgemm_split(int opA, int opB, int M, int N, int K, const double* A, long lda, const double* B,
-                        long ldb, double* C, long ldc, int iters, double* ms_per_iter);
-/* Double-float GEMM on the FP32 pipes.  mode 0: C = op(A) B; 1: C = I - op(A) B; 2: C = D + 0.5
-   op(A) B with FP32 products (A, B rounded to FP32); 3: C = I - A^H A from the upper tiles (op C,
-   B ignored).  op(A) in {0 N, 1 T, 2 C}; D used by mode 2. */
-int qr_test_zgemm_df(int mode, int opA, int M, int N, int K, const double* A, long lda, const double* B, long ldb,
-                     const double* D, double* C, long ldc, int iters, double* ms_per_iter);
-int qr_test_svd(int mode, int m, int n, const double* A, double* U, double* S, double* Vh, double* ms);
-int qr_test_qr(int m, int n, const double* A, double* Q, double* R, double* ms);
 
 #ifdef __cplusplus
 }

@@ -230,7 +230,7 @@ def canonize_site_(ch: OChain, site: int, direction: str, method: str = "qr"):
         nxt = ch.sites[site + 1]
         if ch.lam[site] is not None:  # contract!(tn, virtualind) also eats the old Lambda
             nxt = _scale_left(nxt, ch.lam[site])
-        ch.sites[site + 1] = np.einsum("kb,bor->kor", r, nxt)
+        ch.sites[site + 1] = np.einsum("kb,bor->kor", r, nxt, optimize=True)
         ch.lam[site] = None if s is None else s.astype(np.float64)
     else:
         m = np.transpose(a, (1, 2, 0)).reshape(d * cr, cl)
@@ -244,7 +244,7 @@ def canonize_site_(ch: OChain, site: int, direction: str, method: str = "qr"):
         prv = ch.sites[site - 1]
         if ch.lam[site - 1] is not None:
             prv = _scale_right(prv, ch.lam[site - 1])
-        ch.sites[site - 1] = np.einsum("lob,kb->lok", prv, r)
+        ch.sites[site - 1] = np.einsum("lob,kb->lok", prv, r, optimize=True)
         ch.lam[site - 1] = None if s is None else s.astype(np.float64)
     return ch
 
@@ -265,8 +265,7 @@ def truncate_(ch: OChain, bond, threshold=None, maxdim=None):
     if threshold is None:
         threshold = 1e-16
     extent = extent[np.abs(lm[extent]) > threshold]
-    if extent.size == 0:
-        raise ArgumentError("truncation would leave an empty bond")
+    # an empty extent leaves a bond of size 0 (slice! with an empty range, Chain.jl:404-419)
     ch.sites[s1] = ch.sites[s1][:, :, extent]
     ch.sites[s2] = ch.sites[s2][extent, :, :]
     ch.lam[s1] = lm[extent]
@@ -407,7 +406,7 @@ def evolve_(ch: OChain, g: ODense, threshold=None, maxdim=None, iscanonical=Fals
 
 def evolve_1site_(ch: OChain, site: int, g2):
     """``evolve_1site!`` (``Chain.jl:586-603``): A[l,o',r] = sum_o G[o',o] A[l,o,r]."""
-    ch.sites[site] = np.einsum("po,lor->lpr", g2, ch.sites[site])
+    ch.sites[site] = np.einsum("po,lor->lpr", g2, ch.sites[site], optimize=True)
     return ch
 
 
@@ -427,10 +426,10 @@ def evolve_2site_(ch: OChain, sl: int, g4, threshold=None, maxdim=None, iscanoni
     al, ar = ch.sites[sl], ch.sites[sr]
     if ch.lam[sl] is not None:
         al = _scale_right(al, ch.lam[sl])
-    theta = np.einsum("lab,bcr->lacr", al, ar)
+    theta = np.einsum("lab,bcr->lacr", al, ar, optimize=True)
     d = theta.shape[1]
     g = g4.reshape(d, d, d, d)
-    theta = np.einsum("pqac,lacr->lpqr", g, theta)
+    theta = np.einsum("pqac,lacr->lpqr", g, theta, optimize=True)
     cl, cr = theta.shape[0], theta.shape[3]
     u, s, vh = _thin_svd(theta.reshape(cl * d, d * cr))
     k = s.shape[0]
@@ -471,9 +470,11 @@ def overlap(a: OChain, b: OChain):
     if a.periodic or b.periodic:  # ring: contract the state vectors (oracle sizes are small)
         return np.vdot(to_statevector(b), to_statevector(a))
     sa, sb = _with_lambdas(a), _with_lambdas(b)
+    if any(x.size == 0 for x in sa + sb):  # a size-0 bond: the contraction is an empty sum
+        return 0j
     env = np.ones((1, 1), dtype=np.complex128)  # env[ket, bra]
     for x, y in zip(sa, sb):
-        env = np.einsum("ab,aor,bos->rs", env, x, y.conj())
+        env = np.einsum("ab,aor,bos->rs", env, x, y.conj(), optimize=True)
     return env[0, 0]
 
 
@@ -497,7 +498,7 @@ def mpo_expect(psi: OChain, w_sites):
     s = _with_lambdas(psi)
     env = np.ones((1, 1, 1), dtype=np.complex128)  # env[ket, w, bra]
     for a, w in zip(s, w_sites):
-        env = np.einsum("awb,aic,woix,bod->cxd", env, a, w, a.conj())
+        env = np.einsum("awb,aic,woix,bod->cxd", env, a, w, a.conj(), optimize=True)
     return env[0, 0, 0]
 
 
@@ -508,11 +509,11 @@ def to_statevector(ch: OChain):
     if ch.periodic:
         v = s[0]  # (a0, d, chi_r): the closing index a0 rides along
         for a in s[1:]:
-            v = np.einsum("kxb,bor->kxor", v, a).reshape(v.shape[0], -1, a.shape[2])
-        return np.einsum("kxk->x", v)
+            v = np.einsum("kxb,bor->kxor", v, a, optimize=True).reshape(v.shape[0], -1, a.shape[2])
+        return np.einsum("kxk->x", v, optimize=True)
     v = s[0][0]  # (d, chi_r)
     for a in s[1:]:
-        v = np.einsum("xb,bor->xor", v, a).reshape(-1, a.shape[2])
+        v = np.einsum("xb,bor->xor", v, a, optimize=True).reshape(-1, a.shape[2])
     return v[:, 0]
 
 
@@ -521,6 +522,6 @@ def mpo_to_dense(w_sites):
     h = w_sites[0][0]  # (o, i, wr)
     h = h.reshape(h.shape[0], h.shape[1], h.shape[2])
     for w in w_sites[1:]:
-        h = np.einsum("OIw,woix->OoIix", h, w)
+        h = np.einsum("OIw,woix->OoIix", h, w, optimize=True)
         h = h.reshape(h.shape[0] * h.shape[1], h.shape[2] * h.shape[3], h.shape[4])
     return h[:, :, 0]

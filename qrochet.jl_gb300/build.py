@@ -47,7 +47,8 @@ def build(verbose=False, force=False):
     nvcc = _nvcc()
     os.makedirs(OBJDIR, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
-    headers.append(os.path.join(os.path.dirname(HERE), "include", "qrochet_gpu.h"))
+    inc = os.path.join(os.path.dirname(HERE), "include")
+    headers += [os.path.join(inc, f) for f in os.listdir(inc) if f.endswith(".h")]
     jobs = []
     objs = []
     for src in sources():

@@ -266,11 +266,26 @@ int check_site(const qr_chain* h, int i) {
 
 // ---- canonize_site! (Chain.jl:339-376) ---------------------------------------------------------
 // Canonical forms exist for Open chains only (src/Ansatz/Chain.jl:339,469,509 dispatch on ::Open).
+// truncate! may slice a bond to an empty extent (Chain.jl:404-419): the chain then holds a size-0
+// bond, i.e. the null state.  Contractions of such a chain are 0; factorisations and gates refuse.
+bool has_empty_bond(const qr_chain* h) {
+  for (int b : h->bd)
+    if (b == 0) return true;
+  return false;
+}
+int require_nonempty(const qr_chain* h) {
+  if (h && has_empty_bond(h))
+    return fail(QR_EINVAL, "the chain holds a bond of size 0 (truncate! kept no singular value): it is the null "
+                           "state");
+  return QR_OK;
+}
+
 int require_open(const qr_chain* h) {
   return h->periodic ? fail(QR_EINVAL, "canonical forms are defined for Open chains only") : QR_OK;
 }
 
 int canonize_site_impl(qr_chain* h, int i, int dir, int method) {
+  QR_TRY(require_nonempty(h));
   QR_TRY(require_open(h));
   QR_TRY(check_site(h, i));
   if (dir == QR_DIR_LEFT) {
@@ -366,7 +381,22 @@ int truncate_impl(qr_chain* h, int s1, int s2, double threshold, int maxdim) {
   for (int k = 0; k < upto; k++)
     if (std::fabs(lam[k]) > threshold) keep.push_back(k);
   const int nk = (int)keep.size();
-  if (nk == 0) return fail(QR_EINVAL, "truncation would leave an empty bond");
+  if (dim == 0) return QR_OK;  // already empty
+  if (nk == 0) {
+    // slice! to an empty extent: the bond keeps size 0, both sites hold no entries, Lambda is empty
+    double2 *a = nullptr, *c = nullptr;
+    double* nl = nullptr;
+    QR_TRY(dalloc((void**)&a, 0, h->stream));
+    QR_TRY(dalloc((void**)&c, 0, h->stream));
+    QR_TRY(dalloc((void**)&nl, 0, h->stream));
+    set_site(h, s1, a);
+    set_site(h, s2, c);
+    drop_lambda(h, b);
+    h->lam[b] = nl;
+    h->lamlen[b] = 0;
+    h->bd[b] = 0;
+    return QR_OK;
+  }
   bool prefix = true;
   for (int k = 0; k < nk; k++) prefix = prefix && (keep[k] == k);
   if (nk == dim) return QR_OK;
@@ -437,6 +467,7 @@ int theta_df(qr_chain* h, int sl, int sr, int m, int nn, int cb, double2* th) {
 int evolve2_impl(qr_chain* h, int sl, const double* g, double threshold, int maxdim, int iscanonical,
                  int renormalize) {
   if (!h) return fail(QR_EINVAL, "null chain");
+  QR_TRY(require_nonempty(h));
   if (sl < 0 || sl + 1 >= h->n) return fail(QR_EINVAL, "The sites in the bond must be between 1 and n");
   const int sr = sl + 1, n = h->n, d = h->d;
   cudaStream_t s = h->stream;
@@ -526,14 +557,34 @@ struct EnvOps {
   std::vector<int> wl, wr;
 };
 
-// In QR_MIXED the two contractions of every site step run on the BF16 tensor cores
-// (zgemm_split, ~FP32 accuracy); the operator mixing, Lambda scaling and the stored environments
-// stay FP64.
+// With QR_SPLIT_CONTRACT the two contractions of every site step run on the tcgen05 tensor cores
+// (zgemm_tc: BF16x3 slices, FP32 accumulation, ~FP32 accuracy); the operator mixing, Lambda
+// scaling and the stored environments stay FP64.
 // <b|a> of two periodic chains: the closing bond pair (a0, b0) rides along as a spectator index
 // s = a0 + chi0a b0 in the environment E[a, s, b] (the slot an MPO index takes in env_sweep), the
 // sweep starts from E = delta(a, a0) delta(b, b0) and ends with the trace over a_n = a0, b_n = b0.
 // Per site: X[(s, b), (o, a')] = E^T A, the permute Y[(b, o), s, a'] = X, then the batched
 // E'[a', s, b'] = sum_{(b,o)} Y conj(B).  Cost and memory grow with chi0a chi0b.
+// Workspace of the tensor-core contractions of one sweep: a 256-byte header (the kernel's error
+// flag, zeroed here) followed by the BF16 slices, freed on the stream when the sweep returns.
+struct TcWork {
+  void* base = nullptr;
+  unsigned* err = nullptr;
+  void* ws = nullptr;
+  cudaStream_t s = nullptr;
+  int init(size_t bytes, cudaStream_t st) {
+    s = st;
+    QR_TRY(dalloc(&base, bytes + 256, s));
+    err = static_cast<unsigned*>(base);
+    ws = static_cast<char*>(base) + 256;
+    QR_CUDA(cudaMemsetAsync(err, 0, sizeof(unsigned), s));
+    return QR_OK;
+  }
+  ~TcWork() {
+    if (base) cudaFreeAsync(base, s);
+  }
+};
+
 __global__ void ring_init_k(double2* E, int ca, int cb) {
   const long total = (long)ca * ca * cb * cb;  // E[a, s, b], s = a0 + ca b0
   for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
@@ -567,6 +618,15 @@ int env_sweep_ring(const qr_chain* a, const qr_chain* b, cudaStream_t s, double 
   QR_TRY(dalloc((void**)&X, sizeof(double2) * maxX, s));
   QR_TRY(dalloc((void**)&Y, sizeof(double2) * maxX, s));
   QR_TRY(dalloc((void**)&tr, sizeof(double2) * S, s));
+  TcWork tw;
+  if (split) {
+    size_t ws = 0;
+    for (int i = 0; i < n; i++) {
+      ws = std::max(ws, zgemm_tc_workspace((int)(S * b->cl(i)), d * a->cr(i), a->cl(i), 1, true));
+      ws = std::max(ws, zgemm_tc_workspace(a->cr(i), b->cr(i), b->cl(i) * d, (int)S, true));
+    }
+    QR_TRY(tw.init(ws, s));
+  }
   const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
   {
     long tot = (long)c0a * S * c0b;
@@ -584,7 +644,8 @@ int env_sweep_ring(const qr_chain* a, const qr_chain* b, cudaStream_t s, double 
       count_launch();
     }
     // X[(s, b), (o, a')] = E^T A
-    rc = split ? zgemm_split(s, OP_T, OP_N, (int)(S * cb), d * ca2, ca, E0, ca, 0, a->site[i], ca, 0, X, S * cb, 0, 1)
+    rc = split ? zgemm_tc(s, OP_T, OP_N, (int)(S * cb), d * ca2, ca, E0, ca, 0, a->site[i], ca, 0, X, S * cb, 0, 1,
+                          tw.ws, tw.err)
                : zgemm(s, OP_T, OP_N, (int)(S * cb), d * ca2, ca, one, E0, ca, 0, a->site[i], ca, 0, zero, X, S * cb,
                        0, 1, nullptr);
     if (rc) break;
@@ -602,8 +663,8 @@ int env_sweep_ring(const qr_chain* a, const qr_chain* b, cudaStream_t s, double 
     rc = zpermute(s, X, Y, p);
     if (rc) break;
     // E'[a', s, b'] = sum_{(b,o)} Y[(b,o), s, a'] conj(B[(b,o), b'])
-    rc = split ? zgemm_split(s, OP_T, OP_R, ca2, cb2, cb * d, Y, (long)cb * d * S, (long)cb * d, b->site[i],
-                             (long)cb * d, 0, E1, (long)ca2 * S, ca2, (int)S)
+    rc = split ? zgemm_tc(s, OP_T, OP_R, ca2, cb2, cb * d, Y, (long)cb * d * S, (long)cb * d, b->site[i],
+                          (long)cb * d, 0, E1, (long)ca2 * S, ca2, (int)S, tw.ws, tw.err)
                : zgemm(s, OP_T, OP_R, ca2, cb2, cb * d, one, Y, (long)cb * d * S, (long)cb * d, b->site[i],
                        (long)cb * d, 0, zero, E1, (long)ca2 * S, ca2, (int)S, nullptr);
     std::swap(E0, E1);
@@ -612,10 +673,14 @@ int env_sweep_ring(const qr_chain* a, const qr_chain* b, cudaStream_t s, double 
     unsigned g = (unsigned)std::min<long>((S + 255) / 256, 4864);
     ring_trace_k<<<g, 256, 0, s>>>(E0, c0a, c0b, tr);
     count_launch();
-    double2* h = static_cast<double2*>(host_scratch(sizeof(double2) * S));
+    double2* h = static_cast<double2*>(host_scratch(sizeof(double2) * (S + 1)));
     if (!h) rc = fail(QR_ENOMEM, "page-locked host scratch");
     if (!rc) rc = cuda_ok(cudaMemcpyAsync(h, tr, sizeof(double2) * S, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
+    if (!rc && split)
+      rc = cuda_ok(cudaMemcpyAsync(h + S, tw.err, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
     if (!rc) rc = cuda_ok(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    if (!rc && split && *reinterpret_cast<const unsigned*>(h + S))
+      rc = fail(QR_ECUDA, "tensor-core contraction: a bounded wait gave up");
     double re = 0, im = 0;
     for (long i = 0; !rc && i < S; i++) { re += h[i].x; im += h[i].y; }
     out[0] = re;
@@ -630,6 +695,10 @@ int env_sweep_ring(const qr_chain* a, const qr_chain* b, cudaStream_t s, double 
 }
 
 int env_sweep(const qr_chain* a, const qr_chain* b, const EnvOps* ops, cudaStream_t s, double out[2]) {
+  if (has_empty_bond(a) || has_empty_bond(b)) {  // a size-0 bond: the contraction is an empty sum
+    out[0] = out[1] = 0.0;
+    return QR_OK;
+  }
   if (a->periodic || b->periodic) {
     if (!(a->periodic && b->periodic)) return fail(QR_EINVAL, "both chains must have the same boundary");
     if (ops) return fail(QR_EINVAL, "operator expectation values of periodic chains are not implemented");
@@ -653,6 +722,18 @@ int env_sweep(const qr_chain* a, const qr_chain* b, const EnvOps* ops, cudaStrea
   QR_TRY(dalloc((void**)&E1, sizeof(double2) * maxE, s));
   QR_TRY(dalloc((void**)&X, sizeof(double2) * maxX, s));
   QR_TRY(dalloc((void**)&Y, sizeof(double2) * maxX, s));
+  // split contractions: one BF16-slice workspace for the largest step, behind a 256-byte header
+  // holding the tensor-core kernel's error flag
+  TcWork tw;
+  if (split) {
+    size_t ws = 0;
+    for (int i = 0; i < n; i++) {
+      int wl = ops ? ops->wl[i] : 1, wr = ops ? ops->wr[i] : 1;
+      ws = std::max(ws, zgemm_tc_workspace(wl * b->cl(i), d * a->cr(i), a->cl(i), 1, true));
+      ws = std::max(ws, zgemm_tc_workspace(a->cr(i), b->cr(i), b->cl(i) * d, wr, true));
+    }
+    QR_TRY(tw.init(ws, s));
+  }
   const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
   double2 init = one;
   QR_CUDA(cudaMemcpyAsync(E0, &init, sizeof(double2), cudaMemcpyHostToDevice, s));
@@ -668,7 +749,8 @@ int env_sweep(const qr_chain* a, const qr_chain* b, const EnvOps* ops, cudaStrea
       count_launch();
     }
     // X[(w,b) x (i,a')] = E^T A
-    rc = split ? zgemm_split(s, OP_T, OP_N, wl * cb, d * ca2, ca, E0, ca, 0, a->site[i], ca, 0, X, wl * cb, 0, 1)
+    rc = split ? zgemm_tc(s, OP_T, OP_N, wl * cb, d * ca2, ca, E0, ca, 0, a->site[i], ca, 0, X, wl * cb, 0, 1, tw.ws,
+                          tw.err)
                : zgemm(s, OP_T, OP_N, wl * cb, d * ca2, ca, one, E0, ca, 0, a->site[i], ca, 0, zero, X, wl * cb, 0, 1,
                        nullptr);
     if (rc) break;
@@ -681,18 +763,21 @@ int env_sweep(const qr_chain* a, const qr_chain* b, const EnvOps* ops, cudaStrea
       Yp = Y;
     }
     // E'_w' = Y_w'^T conj(B)
-    rc = split ? zgemm_split(s, OP_T, OP_R, ca2, cb2, cb * d, Yp, (long)cb * d * wr, (long)cb * d, b->site[i],
-                             (long)cb * d, 0, E1, (long)ca2 * wr, ca2, wr)
+    rc = split ? zgemm_tc(s, OP_T, OP_R, ca2, cb2, cb * d, Yp, (long)cb * d * wr, (long)cb * d, b->site[i],
+                          (long)cb * d, 0, E1, (long)ca2 * wr, ca2, wr, tw.ws, tw.err)
                : zgemm(s, OP_T, OP_R, ca2, cb2, cb * d, one, Yp, (long)cb * d * wr, (long)cb * d, b->site[i],
                        (long)cb * d, 0, zero, E1, (long)ca2 * wr, ca2, wr, nullptr);
     std::swap(E0, E1);
   }
   if (rc == QR_OK) {
     QR_CUDA(cudaGetLastError());
-    double2* r = static_cast<double2*>(host_scratch(sizeof(double2)));
+    double2* r = static_cast<double2*>(host_scratch(2 * sizeof(double2)));
     if (!r) return fail(QR_ENOMEM, "page-locked host scratch");
     QR_CUDA(cudaMemcpyAsync(r, E0, sizeof(double2), cudaMemcpyDeviceToHost, s));
+    if (split) QR_CUDA(cudaMemcpyAsync(r + 1, tw.err, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
     QR_CUDA(cudaStreamSynchronize(s));
+    if (split && *reinterpret_cast<const unsigned*>(r + 1))
+      rc = fail(QR_ECUDA, "tensor-core contraction: a bounded wait gave up");
     out[0] = r->x;
     out[1] = r->y;
   }
@@ -757,7 +842,7 @@ static int chain_create(int n, int d, const int* bond_dims, bool periodic, qr_ch
   if (d < 2 || d > 4) return fail(QR_EINVAL, "physical dimension must be 2..4");
   const int nb = periodic ? n : n - 1;
   for (int b = 0; b < nb; b++)
-    if (!bond_dims || bond_dims[b] < 1) return fail(QR_EINVAL, "bond dimensions must be >= 1");
+    if (!bond_dims || bond_dims[b] < 0) return fail(QR_EINVAL, "bond dimensions must be >= 0");
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(QR_ENODEV, "no CUDA device");
   std::call_once(g_pool_once, init_pool);
@@ -1049,7 +1134,7 @@ int qr_chain_load(const char* path, qr_chain** out) {
   if (fread(bd.data(), sizeof(int32_t), bd.size(), fc.f) != bd.size() || fread(fl.data(), 1, fl.size(), fc.f) != fl.size())
     return fail(QR_EINVAL, "truncated chain checkpoint");
   for (int32_t b : bd)
-    if (b < 1) return fail(QR_EINVAL, "corrupt chain checkpoint bond dimensions");
+    if (b < 0) return fail(QR_EINVAL, "corrupt chain checkpoint bond dimensions");
   std::vector<int> bdi(bd.begin(), bd.end());
   qr_chain* h = nullptr;
   QR_TRY(chain_create(n, d, bdi.data(), periodic != 0, &h));
@@ -1210,6 +1295,7 @@ int qr_contract_between(qr_chain* h, int site1, int site2, int direction, int de
   QR_TRY(check_site(h, site1));
   QR_TRY(check_site(h, site2));
   if (site2 != site1 + 1) return fail(QR_EINVAL, "sites must be adjacent");
+  QR_TRY(require_nonempty(h));
   const int b = site1;
   if (!h->lam[b]) return QR_OK;
   if (direction == QR_DIR_RIGHT) {
@@ -1228,6 +1314,7 @@ int qr_canonicality_error(const qr_chain* hc, int site, int direction, double* e
   qr_chain* h = const_cast<qr_chain*>(hc);
   QR_TRY(check_site(h, site));
   if (!err) return fail(QR_EINVAL, "null output");
+  QR_TRY(require_nonempty(h));
   cudaStream_t s = h->stream;
   const int cl = h->cl(site), d = h->d, cr = h->cr(site);
   const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
@@ -1254,6 +1341,7 @@ int qr_truncate(qr_chain* h, int site1, int site2, double threshold, int maxdim)
 int qr_evolve_1site(qr_chain* h, int site, const double* gate) {
   QR_TRY(check_site(h, site));
   if (!gate) return fail(QR_EINVAL, "null gate");
+  QR_TRY(require_nonempty(h));
   QR_TRY(upload_gate(h, gate, h->d));
   QR_TRY(zgate1(h->stream, h->site[site], h->cl(site), h->d, h->cr(site), h->gate));
   QR_CUDA(cudaStreamSynchronize(h->stream));
@@ -1289,6 +1377,10 @@ int qr_expect(const qr_chain* h, int nobs, const int* first, const int* nlanes, 
   if (!h || !out) return fail(QR_EINVAL, "null argument");
   if (nobs < 0 || (nobs > 0 && (!first || !nlanes || !mats))) return fail(QR_EINVAL, "bad observable list");
   const int n = h->n, d = h->d;
+  if (has_empty_bond(h)) {
+    out[0] = out[1] = 0.0;
+    return QR_OK;
+  }
   if (h->periodic) {
     // the reference's own algorithm (Chain.jl:724-735): evolve! a copy by every observable (no
     // truncation), then contract it with the adjoint of the original (the ring sweep)

@@ -7,6 +7,7 @@
 #include <atomic>
 
 #include "../../include/qrochet_gpu.h"
+#include "../../include/qrochet_gpu_testing.h"
 
 namespace qr {
 

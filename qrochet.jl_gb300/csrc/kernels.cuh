@@ -15,6 +15,14 @@ int zgemm(cudaStream_t s, int opA, int opB, int M, int N, int K, double2 alpha,
 int zgemm_split(cudaStream_t s, int opA, int opB, int M, int N, int K, const double2* A, long lda, long sA,
                 const double2* B, long ldb, long sB, double2* C, long ldc, long sC, int batch);
 
+// ---- gemm_tc.cu: the same product on the tcgen05 tensor cores (TMA-staged BF16 slices, TMEM
+// accumulators).  ws: device workspace of zgemm_tc_workspace(M, N, K, batch, sB == 0) bytes;
+// err: device flag set to 1 if a CTA's bounded wait gave up (then C is not valid).
+size_t zgemm_tc_workspace(int M, int N, int K, int batch, bool bshared);
+int zgemm_tc(cudaStream_t s, int opA, int opB, int M, int N, int K, const double2* A, long lda, long sA,
+             const double2* B, long ldb, long sB, double2* C, long ldc, long sC, int batch, void* ws,
+             unsigned* err);
+
 // ---- gemm_df.cu: complex GEMM in double-float (hi, lo FP32 pairs) on the FP32 pipes
 enum { DF_STORE = 0, DF_I_MINUS = 1, DF_F32_AXPY = 2, DF_GRAM = 3 };
 // DF_STORE: (Ch, Cl) = op(A) B; DF_I_MINUS: Ch = I - op(A) B (FP32); DF_F32_AXPY: (Ch, Cl) = D +
@@ -82,5 +90,26 @@ void svd_work_free(SvdWork* w);
 // when their singular values are many decades below sigma_max (callers then discard them).
 int zsvd_thin(cudaStream_t s, SvdWork* w, int mode, const double2* A, int m, int n, long lda,
               double2* U, long ldu, double* S, double2* Vh, long ldvh, int keep = 0);
+// Process-wide counts of the SVD code paths taken (one per Jacobi stage of a call), so tests can
+// check which ordering and which kernel a size reached.
+enum SvdPath {
+  SP_CLUSTER = 0,        // whole Jacobi in one thread-block cluster (k <= 128)
+  SP_BLOCK_CLUSTER,      // FP32 block Jacobi in one cluster
+  SP_BLOCK_BARRIER,      // FP32 block sweep, grid barrier between rounds
+  SP_BLOCK_DATAFLOW,     // FP32 block sweep, per-block flags (more block pairs than CTAs)
+  SP_F64_BARRIER,        // FP64 scalar sweep, grid barrier
+  SP_F64_DATAFLOW,       // FP64 scalar sweep, per-column flags
+  SP_F32_BARRIER,        // FP32 scalar sweep (rows > 2048), grid barrier
+  SP_F32_DATAFLOW,       // FP32 scalar sweep, per-column flags
+  SP_DF_CLUSTER,         // double-float polish in one cluster
+  SP_DF_BARRIER,         // double-float polish sweep, grid barrier
+  SP_DF_DATAFLOW,        // double-float polish sweep, per-column flags
+  SP_QR_PRECOND_FP64,    // FP64 path on R^H of a Householder QR
+  SP_QR_PRECOND_MIXED,   // mixed path restarted on R^H after its FP32 probe
+  SP_REORTH,             // Householder re-orthonormalisation of the kept singular vectors
+  SP_COUNT
+};
+extern std::atomic<uint64_t> g_svd_path[SP_COUNT];
+inline void svd_path(int p) { g_svd_path[p].fetch_add(1, std::memory_order_relaxed); }
 
 }  // namespace qr

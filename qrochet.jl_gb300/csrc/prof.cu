@@ -12,6 +12,7 @@ struct Rec {
   int kind;
   double flops, bytes;
   cudaEvent_t e0, e1;
+  uint64_t units;  // launches (or Jacobi sweeps) the record covers
 };
 std::mutex g_mu;
 bool g_on = false;
@@ -35,7 +36,7 @@ bool prof_on() { return g_on; }
 int prof_begin(cudaStream_t s, int kind, double flops, double bytes) {
   if (!g_on) return -1;
   std::lock_guard<std::mutex> lk(g_mu);
-  Rec r{kind, flops, bytes, take_event(), take_event()};
+  Rec r{kind, flops, bytes, take_event(), take_event(), 1};
   cudaEventRecord(r.e0, s);
   g_recs.push_back(r);
   return (int)g_recs.size() - 1;
@@ -47,12 +48,13 @@ void prof_end(cudaStream_t s, int idx) {
   if (idx < (int)g_recs.size()) cudaEventRecord(g_recs[idx].e1, s);
 }
 
-void prof_account(int idx, double flops, double bytes) {
+void prof_account(int idx, double flops, double bytes, long units) {
   if (idx < 0) return;
   std::lock_guard<std::mutex> lk(g_mu);
   if (idx < (int)g_recs.size()) {
     g_recs[idx].flops = flops;
     g_recs[idx].bytes = bytes;
+    if (units >= 0) g_recs[idx].units = (uint64_t)units;
   }
 }
 
@@ -146,7 +148,7 @@ int qr_prof_read(int kind, double* ms, uint64_t* launches, double* flops, double
     if (cudaEventElapsedTime(&x, r.e0, r.e1) == cudaSuccess) t += x;
     f += r.flops;
     b += r.bytes;
-    c++;
+    c += r.units;
   }
   if (ms) *ms = t;
   if (launches) *launches = c;

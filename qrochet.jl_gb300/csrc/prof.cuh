@@ -8,6 +8,8 @@ bool prof_on();
 // returns a record index (or -1 when profiling is off); pair with prof_end on the same stream
 int prof_begin(cudaStream_t s, int kind, double flops, double bytes);
 void prof_end(cudaStream_t s, int idx);
-// set the work of a record after the fact (flops/bytes known only once the launches ran)
-void prof_account(int idx, double flops, double bytes);
+// set the work of a record after the fact (flops/bytes known only once the launches ran); units
+// >= 0 replaces the record's unit count (1 by default: one launch; the Jacobi stages count the
+// sweeps that ran)
+void prof_account(int idx, double flops, double bytes, long units = -1);
 }  // namespace qr

@@ -29,6 +29,7 @@
 #include "kernels.cuh"
 #include "df.cuh"
 #include "prof.cuh"
+#include "jacobi_rot.cuh"
 
 namespace qr {
 
@@ -54,6 +55,8 @@ struct SvdWork {
   cudaStream_t last = nullptr;
 };
 
+std::atomic<uint64_t> g_svd_path[SP_COUNT];
+
 SvdWork* svd_work_create() { return new SvdWork(); }
 void svd_work_free(SvdWork* w) {
   if (!w) return;
@@ -74,15 +77,6 @@ bool debug_on() {
   return v;
 }
 
-template <typename T> struct Eps;
-template <> struct Eps<double> { static constexpr double v = 2.220446049250313e-16; };
-template <> struct Eps<float> { static constexpr float v = 1.1920929e-07f; };
-
-template <typename T>
-__device__ __forceinline__ T warp_sum(T v) {
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
 
 // One round of the round-robin (circle) ordering: CTA b handles pair b.  When the column length
 // fits (m <= NT * RPT) both columns stay in registers between the inner products and the
@@ -106,16 +100,6 @@ __device__ __forceinline__ void block_sum4(T& a, T& b, T& c, T& d) {
   for (int k = 0; k < NT / 32; k++) { a += red[0][k]; b += red[1][k]; c += red[2][k]; d += red[3][k]; }
 }
 
-template <typename C, typename T>
-__device__ __forceinline__ void rot(C& x, C& y, T c, T sr, T si) {
-  C xn, yn;
-  xn.x = c * x.x - (sr * y.x + si * y.y);
-  xn.y = c * x.y - (sr * y.y - si * y.x);
-  yn.x = (sr * x.x - si * x.y) + c * y.x;
-  yn.y = (sr * x.y + si * x.x) + c * y.y;
-  x = xn;
-  y = yn;
-}
 
 template <typename T, int NT, int RPT>
 __device__ __forceinline__ void jacobi_pair(cplx_t<T>* __restrict__ B, long ldb, int m, int n,
@@ -242,67 +226,6 @@ __global__ void __launch_bounds__(NT) jacobi_sweep_k(cplx_t<T>* __restrict__ B, 
 }
 
 
-
-// Rotation of the pair (p, q) from its Gram entries a = |b_p|^2, b = |b_q|^2, gamma = b_p^H b_q,
-// for columns pre-scaled so that sigma_max ~ 1.  The angle is computed in FP32 (b - a first in
-// the working precision, so near-degenerate pairs do not cancel); c = 1/sqrt(1 + t^2) and the unit
-// phase gamma/|gamma| are then formed in the working precision from FP32 seeds and two Newton
-// steps, so the rotation is unitary to working precision while FP64 square roots and divisions --
-// expensive on this part -- are avoided.  A slightly inexact angle only leaves a coupling a
-// factor ~1e-7 smaller, which the next sweep removes.
-// |g| without forming |g|^2: in FP32 the squared coupling of two tiny columns underflows
-template <typename T>
-__device__ __forceinline__ T cabs_safe(T gr, T gi) {
-  const T x = fabs(gr), y = fabs(gi);
-  const T mx = x > y ? x : y, mn = x > y ? y : x;
-  if (!(mx > T(0))) return T(0);
-  const T r = mn / mx;
-  return mx * sqrt(T(1) + r * r);
-}
-
-// tol < 0 selects the relative test |g| > |tol| sqrt(a b) (every pair is driven to the same
-// relative orthogonality whatever its norms; used on the R^H of a QR preconditioning, where FP32
-// keeps the small columns to full relative precision); otherwise the absolute test below.
-template <typename T>
-__device__ __forceinline__ bool rotation_params(T a, T b, T gr, T gi, T tol, T smax, T& c, T& sr, T& si, float& tabs) {
-  if (!(a > 0) || !(b > 0)) return false;
-  T rg;
-  if (tol < T(0)) {
-    const T gabs = cabs_safe(gr, gi);
-    if (!(gabs > -tol * sqrt(a) * sqrt(b))) return false;
-    rg = T(1) / gabs;
-  } else {
-    const T g2 = gr * gr + gi * gi;
-    const T fl = T(4) * Eps<T>::v * smax;
-    const T mn = a < b ? a : b;
-    // g > tol smax sqrt(min(a, b)) + fl^2, compared in squares
-    if (!(g2 > tol * tol * smax * smax * mn + fl * fl * fl * fl)) return false;
-    // 1/|gamma| in working precision: FP32 seed of the exponent-normalised g2 (exact scaling), then
-    // two Newton steps; gamma may be far below FP32 range while still above the rotation floor
-    int e2 = 0;
-    const T g2n = frexp(g2, &e2);  // g2 = g2n * 2^e2, g2n in [0.5, 1)
-    const int h = e2 / 2;
-    const T g2s = ldexp(g2n, e2 - 2 * h);  // in [0.25, 2)
-    rg = (T)rsqrtf((float)g2s);
-    rg = rg * (T(1.5) - T(0.5) * g2s * rg * rg);
-    rg = rg * (T(1.5) - T(0.5) * g2s * rg * rg);
-    rg = ldexp(rg, -h);
-  }
-  const float zeta = (float)(T(0.5) * (b - a) * rg);
-  const float tf = (zeta >= 0.f ? 1.f : -1.f) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
-  if (!(tf != 0.f)) return false;  // angle below FP32 resolution of the tangent: nothing to do
-  const T t = (T)tf;
-  const T u = T(1) + t * t;
-  T cc = (T)rsqrtf((float)u);
-  cc = cc * (T(1.5) - T(0.5) * u * cc * cc);
-  cc = cc * (T(1.5) - T(0.5) * u * cc * cc);
-  const T sc = t * cc;
-  c = cc;
-  sr = sc * gr * rg;
-  si = sc * gi * rg;
-  tabs = fabsf(tf);
-  return true;
-}
 
 // Warp sum of four values by a transposed butterfly: the first two levels split the values
 // between lane halves, so each lane adds 6 times instead of 20.  Afterwards lane l holds the warp
@@ -1585,6 +1508,7 @@ int jacobi(cudaStream_t s, SvdWork* w, cplx_t<T>* B, long ldb, int rows, int k, 
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
+    svd_path(blk ? SP_BLOCK_CLUSTER : SP_CLUSTER);
     if (blk) {
       QR_CUDA(cudaLaunchKernelEx(&cfg, jacobi_block_cluster_k, (float2*)B, ldb, rows, k, (float2*)V, ldv, (float)tol,
                                  (const double*)smax_d, max_sweeps, state, tan_stop));
@@ -1602,6 +1526,7 @@ int jacobi(cudaStream_t s, SvdWork* w, cplx_t<T>* B, long ldb, int rows, int k, 
     if (per_sm < 1) return fail(QR_ECUDA, "block Jacobi sweep kernel cannot be resident");
     int grid = std::min(per_sm * sms, nbp / 2);
     if (grid < 1) grid = 1;
+    svd_path(nbp / 2 > grid ? SP_BLOCK_DATAFLOW : SP_BLOCK_BARRIER);
     for (int sweep = 0; sweep < max_sweeps; sweep++) {
       float2* Bp = reinterpret_cast<float2*>(B);
       float2* Vp = reinterpret_cast<float2*>(V);
@@ -1623,6 +1548,8 @@ int jacobi(cudaStream_t s, SvdWork* w, cplx_t<T>* B, long ldb, int rows, int k, 
     int grid = per_sm * sms;
     if (grid > np / 2) grid = np / 2;
     if (grid < 1) grid = 1;
+    if (sizeof(T) == 8) svd_path(np / 2 > grid ? SP_F64_DATAFLOW : SP_F64_BARRIER);
+    else svd_path(np / 2 > grid ? SP_F32_DATAFLOW : SP_F32_BARRIER);
     for (int sweep = 0; sweep < max_sweeps; sweep++) {
       cplx_t<T>* Bp = B;
       cplx_t<T>* Vp = V;
@@ -1666,7 +1593,7 @@ int jacobi(cudaStream_t s, SvdWork* w, cplx_t<T>* B, long ldb, int rows, int k, 
   // algorithmic work: three inner products per pair and sweep (16 real flops per row) and two
   // column rotations of B and V per rotated pair (20 flops per row and column)
   prof_account(pr, 16.0 * rows * pairs * ran + 40.0 * rotated * (rows + k),
-               sizeof(cplx_t<T>) * ((double)rows + k) * 2.0 * (pairs * ran + rotated));
+               sizeof(cplx_t<T>) * ((double)rows + k) * 2.0 * (pairs * ran + rotated), ran);
   if (converged) *converged = hs[0] ? 1 : 0;
   if (last_frac) *last_frac = ran > 0 && pairs > 0 ? hs[8 + SW_STRIDE * (ran - 1)] / pairs : 0.0;
   if (!hs[0] && must_converge) return fail(QR_ENOCONV, "Jacobi SVD did not converge");
@@ -1702,6 +1629,7 @@ int jacobi_df(cudaStream_t s, SvdWork* w, float2* Bh, float2* Bl, long ldb, int 
   if (grid < 1) grid = 1;
   int pr = prof_begin(s, PK_JACOBI_DF, 0.0, 0.0);
   const bool cluster = k <= 128 && rows <= 32 * CCR;
+  svd_path(cluster ? SP_DF_CLUSTER : (np / 2 > grid ? SP_DF_DATAFLOW : SP_DF_BARRIER));
   if (cluster) {
     // one cluster of up to 16 CTAs, one warp per pair of a round (as in jacobi<T>)
     const int npairs = np / 2 > 0 ? np / 2 : 1;
@@ -1756,7 +1684,7 @@ int jacobi_df(cudaStream_t s, SvdWork* w, float2* Bh, float2* Bl, long ldb, int 
   // FP32 operations: ~96 per row per inner-product pass (compensated sums) and ~100-340 per row
   // and column rotated (small-angle / general rotation); the count takes the general form
   prof_account(pr, 96.0 * rows * pairs * ran + 344.0 * rotated * (rows + k),
-               sizeof(float2) * 2.0 * ((double)rows + k) * 2.0 * (pairs * ran + rotated));
+               sizeof(float2) * 2.0 * ((double)rows + k) * 2.0 * (pairs * ran + rotated), ran);
   if (!hs[0]) return fail(QR_ENOCONV, "double-float Jacobi polish did not converge");
   return QR_OK;
 }
@@ -1765,6 +1693,7 @@ int jacobi_df(cudaStream_t s, SvdWork* w, float2* Bh, float2* Bl, long ldb, int 
 
 // Re-orthonormalise the m x k column block L in place (Householder QR, phase-preserving).
 static int reorthonormalize(cudaStream_t s, SvdWork* w, double2* L, long ldl, int m, int k) {
+  svd_path(SP_REORTH);
   QR_TRY(w->qtmp.ensure(sizeof(double2) * ((size_t)m * k + (size_t)k * k), s));
   QR_TRY(w->tau.ensure(sizeof(double2) * (size_t)k, s));
   double2* Rr = w->qtmp.as<double2>() + (size_t)m * k;
@@ -1843,6 +1772,7 @@ int zsvd_thin(cudaStream_t s, SvdWork* w, int mode, const double2* A, int m, int
   // Jacobi directly (same accuracy).
   if (mode == QR_FP64 || k <= kMixedMinCols) {
     if (k > kPrecondMinCols) {
+      svd_path(SP_QR_PRECOND_FP64);
       QR_TRY(qr_precondition(s, w, B, rows0, k));
       rows = k;
       pre = true;
@@ -1890,6 +1820,7 @@ int zsvd_thin(cudaStream_t s, SvdWork* w, int mode, const double2* A, int m, int
                            kPrecondTanStop));
     } else if (!conv32) {
       // slow convergence (widely spread spectrum): precondition in FP64 and start over on R^H
+      svd_path(SP_QR_PRECOND_MIXED);
       QR_TRY(qr_precondition(s, w, B, rows0, k));
       rows = k;
       pre = true;
@@ -2093,23 +2024,49 @@ extern "C" int qr_svd_noalloc(int m, int n, const double* A, long lda, double* U
   unsigned* bar = cnt + 4;
   const double2* Ad = (const double2*)A;
 
-  // B = A (tall) or A^H (wide); V = I: every buffer read below is written first
+  // B = A (tall) or A^H (wide): every buffer read below is written first
   if (tall) {
     QR_CUDA(cudaMemcpy2DAsync(B, sizeof(double2) * rows, Ad, sizeof(double2) * lda, sizeof(double2) * m, n,
                               cudaMemcpyDeviceToDevice, s));
   } else {
     QR_TRY(ztranspose(s, Ad, lda, m, n, B, rows, 1));
   }
-  QR_TRY(zset_identity(s, V, k, k, k));
 
-  // sigma_max scale for the rotation criterion (host copy into a stack array: no allocation)
+  // Column norms on the host (a stack array: no allocation).  B is scaled by the power of two
+  // 2^-e that brings its largest column norm into [1/2, 1): the rotation test squares column
+  // norms and inner products, which would underflow below ~1e-154 or overflow above ~1e154.
   double hn[NOALLOC_MAX_K];
-  col_norms_k<double2><<<ceil_div((long)k * 32, TPB), TPB, 0, s>>>(B, rows, rows, k, nrm);
-  QR_CHECK_LAUNCH("col_norms_k");
-  QR_CUDA(cudaMemcpyAsync(hn, nrm, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
-  QR_CUDA(cudaStreamSynchronize(s));
+  auto host_max_norm = [&](const double2* X, long ldx, int r, double* out) -> int {
+    col_norms_k<double2><<<ceil_div((long)k * 32, TPB), TPB, 0, s>>>(X, ldx, r, k, nrm);
+    QR_CHECK_LAUNCH("col_norms_k");
+    QR_CUDA(cudaMemcpyAsync(hn, nrm, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+    QR_CUDA(cudaStreamSynchronize(s));
+    double mx = 0.0;
+    for (int j = 0; j < k; j++) mx = hn[j] > mx ? hn[j] : mx;
+    *out = mx;
+    return QR_OK;
+  };
   double smax = 0.0;
-  for (int j = 0; j < k; j++) smax = hn[j] > smax ? hn[j] : smax;
+  QR_TRY(host_max_norm(B, rows, rows, &smax));
+  if (!std::isfinite(smax)) return fail(QR_EINVAL, "qr_svd_noalloc: non-finite entries");
+  int e2 = 0;
+  if (smax > 0.0) frexp(smax, &e2);
+  QR_TRY(zscale_matrix(s, rows, k, make_double2(ldexp(1.0, -e2), 0.0), B, rows, 0, 1));
+
+  // QR preconditioning above 32 columns, as in the allocating FP64 path: B = Q R and the sweeps
+  // run on W = R^H (k x k), which converges in ~10 sweeps even when the singular values spread
+  // over many decades.  Q goes to L, R to V, W to the head of B.
+  const bool pre = k > 32;
+  int jr = rows;  // rows of the matrix the sweeps rotate
+  if (pre) {
+    QR_TRY(zqr_thin(s, B, rows, k, rows, L, rows, V, k, tau));
+    QR_TRY(ztranspose(s, V, k, k, k, B, k, 1));
+    jr = k;
+    QR_TRY(host_max_norm(B, k, k, &smax));
+  } else {
+    smax = smax > 0.0 ? ldexp(smax, -e2) : 0.0;
+  }
+  QR_TRY(zset_identity(s, V, k, k, k));
 
   constexpr int NT = 256, RPT = 8;
   const int np = k + (k & 1);
@@ -2120,15 +2077,15 @@ extern "C" int qr_svd_noalloc(int m, int n, const double* A, long lda, double* U
   int grid = per_sm * sms;
   if (grid > np / 2) grid = np / 2;
   if (grid < 1) grid = 1;
-  double tol = sqrt((double)rows) * Eps<double>::v;
+  double tol = sqrt((double)jr) * Eps<double>::v;
   bool converged = false;
   for (int sweep = 0; sweep < 60 && !converged; sweep++) {
     // counters and the grid barrier start every sweep at zero
     QR_CUDA(cudaMemsetAsync(cnt, 0, 8 * sizeof(unsigned), s));
     double2* Bp = B;
     double2* Vp = V;
-    int mm = rows, kk = k, npp = np;
-    long ldbb = rows, ldvv = k;
+    int mm = jr, kk = k, npp = np;
+    long ldbb = jr, ldvv = k;
     double tl = tol, sm = smax;
     void* args[] = {&Bp, &ldbb, &mm, &kk, &Vp, &ldvv, &npp, &tl, &sm, &cnt, &bar};
     QR_CUDA(cudaLaunchCooperativeKernel((const void*)jacobi_sweep_k<double, NT, RPT>, dim3(grid), dim3(NT), args, 0, s));
@@ -2144,38 +2101,66 @@ extern "C" int qr_svd_noalloc(int m, int n, const double* A, long lda, double* U
   }
   if (!converged) return fail(QR_ENOCONV, "qr_svd_noalloc: Jacobi SVD did not converge");
 
-  col_norms_k<double2><<<ceil_div((long)k * 32, TPB), TPB, 0, s>>>(B, rows, rows, k, nrm);
+  // sigma of the scaled matrix, sorted; S = sigma 2^e
+  col_norms_k<double2><<<ceil_div((long)k * 32, TPB), TPB, 0, s>>>(B, jr, jr, k, nrm);
   QR_CHECK_LAUNCH("col_norms_k");
   rank_sort_k<<<ceil_div(k, TPB), TPB, 0, s>>>(nrm, k, perm, sorted);
   QR_CHECK_LAUNCH("rank_sort_k");
-  QR_CUDA(cudaMemcpyAsync(S, sorted, sizeof(double) * k, cudaMemcpyDeviceToDevice, s));
   QR_CUDA(cudaMemcpyAsync(hn, sorted, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
   QR_CUDA(cudaStreamSynchronize(s));
   if (!(hn[0] >= 0.0) || !std::isfinite(hn[0])) return fail(QR_ENOCONV, "qr_svd_noalloc: non-finite singular values");
   const bool reorth = !(hn[k - 1] > 1e-3 * hn[0]);
+  for (int j = 0; j < k; j++) hn[j] = ldexp(hn[j], e2);
+  QR_CUDA(cudaMemcpyAsync(S, hn, sizeof(double) * k, cudaMemcpyHostToDevice, s));
 
-  // left factor Lf (rows x k) = B[:, perm] / sigma ; right factor (k x k) = V[:, perm]
-  double2* Ud = (double2*)U;
-  double2* Lf = tall ? Ud : L;
-  const long ldl = tall ? ldu : rows;
-  double2* Rf = tall ? L : Ud;
-  const long ldr = tall ? k : ldu;
-  gather_cols_k<double2><<<gs((long)rows * k), TPB, 0, s>>>(B, rows, rows, k, perm, sorted, Lf, ldl);
-  QR_CHECK_LAUNCH("gather_cols_k");
-  gather_cols_k<double2><<<gs((long)k * k), TPB, 0, s>>>(V, k, k, k, perm, nullptr, Rf, ldr);
-  QR_CHECK_LAUNCH("gather_cols_k");
-  if (reorth) {
-    // B and V are free now: QR copy in B, R in V
-    QR_CUDA(cudaMemcpy2DAsync(B, sizeof(double2) * rows, Lf, sizeof(double2) * ldl, sizeof(double2) * rows, k,
+  // Re-orthonormalise the k columns of F (ld ldf, r rows) in place through the QR copy at X
+  // (ld r), with R in V (free once the right factor has been gathered).
+  auto reorthonormalize_noalloc = [&](double2* F, long ldf, int r, double2* X) -> int {
+    QR_CUDA(cudaMemcpy2DAsync(X, sizeof(double2) * r, F, sizeof(double2) * ldf, sizeof(double2) * r, k,
                               cudaMemcpyDeviceToDevice, s));
-    QR_TRY(zqr_thin(s, B, rows, k, rows, Lf, ldl, V, k, tau));
-    phase_fix_k<<<gs((long)rows * k), TPB, 0, s>>>(Lf, ldl, rows, k, V, k);
+    QR_TRY(zqr_thin(s, X, r, k, r, F, ldf, V, k, tau));
+    phase_fix_k<<<gs((long)r * k), TPB, 0, s>>>(F, ldf, r, k, V, k);
     QR_CHECK_LAUNCH("phase_fix_k");
-  }
-  if (tall) {
-    QR_TRY(ztranspose(s, Rf, k, k, k, (double2*)Vh, ldvh, 1));  // Vh = Rf^H
+    return QR_OK;
+  };
+  double2* Ud = (double2*)U;
+  double2* Vhd = (double2*)Vh;
+  const double2 one = make_double2(1.0, 0.0), zero = make_double2(0.0, 0.0);
+  if (pre) {
+    // W = Lw Sigma Rf^H with Lw = W[:, perm] / sigma, Rf = V[:, perm]; B0 = Q R = (Q Rf) Sigma Lw^H
+    double2* Bk = B + (size_t)k * k;  // second k x k slot of B
+    if (tall) {  // A = B0: U = Q Rf, Vh = Lw^H; Rf waits in Vh (k x k) until the GEMM has read it
+      gather_cols_k<double2><<<gs((long)k * k), TPB, 0, s>>>(B, k, k, k, perm, sorted, Bk, k);
+      QR_CHECK_LAUNCH("gather_cols_k");
+      gather_cols_k<double2><<<gs((long)k * k), TPB, 0, s>>>(V, k, k, k, perm, nullptr, Vhd, ldvh);
+      QR_CHECK_LAUNCH("gather_cols_k");
+      if (reorth) QR_TRY(reorthonormalize_noalloc(Bk, k, k, B));
+      QR_TRY(zgemm(s, OP_N, OP_N, rows, k, k, one, L, rows, 0, Vhd, ldvh, 0, zero, Ud, ldu, 0, 1, nullptr));
+      QR_TRY(ztranspose(s, Bk, k, k, k, Vhd, ldvh, 1));
+    } else {  // A = B0^H = Lw Sigma (Q Rf)^H: U = Lw (m x m), Vh = Rf^H Q^H (m x n)
+      gather_cols_k<double2><<<gs((long)k * k), TPB, 0, s>>>(B, k, k, k, perm, sorted, Ud, ldu);
+      QR_CHECK_LAUNCH("gather_cols_k");
+      gather_cols_k<double2><<<gs((long)k * k), TPB, 0, s>>>(V, k, k, k, perm, nullptr, Bk, k);
+      QR_CHECK_LAUNCH("gather_cols_k");
+      if (reorth) QR_TRY(reorthonormalize_noalloc(Ud, ldu, k, B));
+      QR_TRY(zgemm(s, OP_C, OP_C, k, rows, k, one, Bk, k, 0, L, rows, 0, zero, Vhd, ldvh, 0, 1, nullptr));
+    }
   } else {
-    QR_TRY(ztranspose(s, Lf, ldl, rows, k, (double2*)Vh, ldvh, 1));  // Vh = L^H
+    // left factor Lf (rows x k) = B[:, perm] / sigma ; right factor (k x k) = V[:, perm]
+    double2* Lf = tall ? Ud : L;
+    const long ldl = tall ? ldu : rows;
+    double2* Rf = tall ? L : Ud;
+    const long ldr = tall ? k : ldu;
+    gather_cols_k<double2><<<gs((long)rows * k), TPB, 0, s>>>(B, rows, rows, k, perm, sorted, Lf, ldl);
+    QR_CHECK_LAUNCH("gather_cols_k");
+    gather_cols_k<double2><<<gs((long)k * k), TPB, 0, s>>>(V, k, k, k, perm, nullptr, Rf, ldr);
+    QR_CHECK_LAUNCH("gather_cols_k");
+    if (reorth) QR_TRY(reorthonormalize_noalloc(Lf, ldl, rows, B));
+    if (tall) {
+      QR_TRY(ztranspose(s, Rf, k, k, k, Vhd, ldvh, 1));  // Vh = Rf^H
+    } else {
+      QR_TRY(ztranspose(s, Lf, ldl, rows, k, Vhd, ldvh, 1));  // Vh = L^H
+    }
   }
   QR_CUDA(cudaStreamSynchronize(s));
   return QR_OK;

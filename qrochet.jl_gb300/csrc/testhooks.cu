@@ -96,6 +96,51 @@ int qr_test_zgemm_split(int opA, int opB, int M, int N, int K, const double* A, 
   return QR_OK;
 }
 
+// C[b] = op(A[b]) op(B[b]) with the tcgen05 split-precision kernel (gemm_tc.cu); A and B hold
+// `batch` matrices at strides sA and sB (sB = 0: one B shared by the batch), C at stride ldc * N.
+int qr_test_zgemm_tc(int opA, int opB, int M, int N, int K, int batch, const double* A, long lda, long sA,
+                     const double* B, long ldb, long sB, double* C, long ldc, int iters, double* ms_per_iter) {
+  if (M <= 0 || N <= 0 || K < 0 || iters < 1 || batch < 1) return fail(QR_EINVAL, "bad gemm shape");
+  long ca = (opA == OP_N || opA == OP_R) ? K : M;
+  long cb = (opB == OP_N || opB == OP_R) ? N : K;
+  const long sC = ldc * N;
+  if (sA < lda * ca && batch > 1) return fail(QR_EINVAL, "bad batch stride");
+  Dev dA, dB, dC, dW;
+  QR_TRY(up(dA, A, (size_t)(batch > 1 ? sA * (batch - 1) : 0) + (size_t)lda * ca));
+  QR_TRY(up(dB, B, (size_t)(sB ? sB * (batch - 1) : 0) + (size_t)ldb * cb));
+  QR_TRY(up(dC, nullptr, (size_t)sC * batch));
+  const size_t wsb = zgemm_tc_workspace(M, N, K, batch, sB == 0);
+  QR_CUDA(cudaMalloc(&dW.p, wsb + 256));
+  unsigned* err = static_cast<unsigned*>(dW.p);
+  void* ws = static_cast<char*>(dW.p) + 256;
+  QR_CUDA(cudaMemset(err, 0, sizeof(unsigned)));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float total = 0;
+  int rc = QR_OK;
+  for (int it = 0; it < iters && rc == QR_OK; it++) {
+    cudaEventRecord(e0);
+    rc = zgemm_tc(0, opA, opB, M, N, K, (double2*)dA.p, lda, sA, (double2*)dB.p, ldb, sB, (double2*)dC.p, ldc, sC,
+                  batch, ws, err);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    total += ms;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  QR_TRY(rc);
+  QR_CUDA(cudaDeviceSynchronize());
+  unsigned herr = 0;
+  QR_CUDA(cudaMemcpy(&herr, err, sizeof(unsigned), cudaMemcpyDeviceToHost));
+  if (herr) return fail(QR_ECUDA, "tensor-core GEMM: a bounded wait gave up");
+  QR_CUDA(cudaMemcpy(C, dC.p, sizeof(double2) * sC * batch, cudaMemcpyDeviceToHost));
+  if (ms_per_iter) *ms_per_iter = total / iters;
+  return QR_OK;
+}
+
 // Double-float GEMM (gemm_df.cu) through FP64 host matrices: inputs are split into (hi, lo) FP32
 // pairs on the device, the result converted back (mode 1 returns the FP32 value I - op(A) B).
 int qr_test_zgemm_df(int mode, int opA, int M, int N, int K, const double* A, long lda, const double* B, long ldb,
@@ -154,6 +199,13 @@ int qr_test_zgemm_df(int mode, int opA, int M, int N, int K, const double* A, lo
 }
 
 // Thin SVD of the m x n column-major A: U (m x k), S (k), Vh (k x n), k = min(m, n).
+// counts[i] = how often SVD code path i ran in this process (i < min(n, SP_COUNT)); *total = SP_COUNT
+int qr_test_svd_paths(uint64_t* counts, int n, int* total) {
+  for (int i = 0; i < n && i < SP_COUNT; i++) counts[i] = g_svd_path[i].load(std::memory_order_relaxed);
+  if (total) *total = SP_COUNT;
+  return QR_OK;
+}
+
 int qr_test_svd(int mode, int m, int n, const double* A, double* U, double* S, double* Vh, double* ms) {
   if (m <= 0 || n <= 0) return fail(QR_EINVAL, "bad svd shape");
   const int k = m < n ? m : n;

@@ -120,7 +120,9 @@ function load(path::AbstractString)
 end
 
 """Reads a checkpoint on the host (no GPU needed): returns `(arrays, Λs, periodic)` with the arrays
-exactly as `MPS(arrays)` / `pMPS(arrays)` take them (layout documented in INTEGRATION.md)."""
+exactly as `MPS(arrays)` / `pMPS(arrays)` take them.  Layout (little-endian): "QRCHAIN1", Int32 n, d,
+precision, periodic, Int32 bond dimensions, UInt8 Λ flags per bond, the site arrays in (o, l, r)
+column-major order, then Float64 Λ for every flagged bond."""
 function read_checkpoint(path::AbstractString)
     open(path, "r") do io
         String(read(io, 8)) == "QRCHAIN1" || throw(ArgumentError("not a chain checkpoint"))

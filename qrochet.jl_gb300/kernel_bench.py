@@ -4,6 +4,7 @@
     python qrochet.jl_gb300/kernel_bench.py svd fp64|mixed N [M]
     python qrochet.jl_gb300/kernel_bench.py qr M N
     python qrochet.jl_gb300/kernel_bench.py zgemm_split M N K [iters]
+    python qrochet.jl_gb300/kernel_bench.py zgemm_tc M N K [iters] [batch]
     python qrochet.jl_gb300/kernel_bench.py upload CHI
 
 Inputs are seeded complex Gaussians; prints one JSON line with the event-timed duration, the
@@ -70,6 +71,24 @@ def main(argv):
         _lib.check(L.qr_test_zgemm_split(0, 0, M, N, K, p(A), M, p(B), K, p(Cm), M, iters, C.byref(ms)))
         fl = 8.0 * M * N * K
         out = {"op": "zgemm_split", "M": M, "N": N, "K": K, "ms": ms.value, "tflops_complex_equiv": fl / ms.value / 1e9}
+    elif what == "zgemm_tc":
+        # the tcgen05 split kernel with the environment sweep's operand shapes: op(A) = A^T with K
+        # contiguous, B shared by the batch
+        M, N, K = (int(x) for x in argv[1:4])
+        iters = int(argv[4]) if len(argv) > 4 else 3
+        batch = int(argv[5]) if len(argv) > 5 else 1
+        A = np.asfortranarray(R.complex_gaussian(g, (K, M * batch)))
+        B = np.asfortranarray(R.complex_gaussian(g, (K, N)))
+        Cm = np.zeros(M * N * batch, dtype=np.complex128)
+        ms = C.c_double()
+        _lib.check(L.qr_test_zgemm_tc(1, 0, M, N, K, batch, p(A), K, K * M if batch > 1 else 0, p(B), K, 0, p(Cm), M,
+                                      iters, C.byref(ms)))
+        ref = A[:, :M].T @ B
+        got = Cm[:M * N].reshape((M, N), order="F")
+        fl = 8.0 * M * N * K * batch
+        out = {"op": "zgemm_tc", "M": M, "N": N, "K": K, "batch": batch, "ms": ms.value,
+               "tflops_complex_equiv": fl / ms.value / 1e9, "bf16_tflops_executed": 6.0 * fl / ms.value / 1e9,
+               "rel_err": float(np.linalg.norm(got - ref) / np.linalg.norm(ref))}
     elif what == "upload":
         # a 3-site chain whose middle site is (2, chi, chi) in the reference's (o, l, r) order: the
         # upload permutes it to the device layout (l, o, r)

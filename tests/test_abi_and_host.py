@@ -20,7 +20,8 @@ def lib():
 
 
 def _declared():
-    text = open(os.path.join(ROOT, "include", "qrochet_gpu.h")).read()
+    inc = os.path.join(ROOT, "include")
+    text = "".join(open(os.path.join(inc, f)).read() for f in sorted(os.listdir(inc)) if f.endswith(".h"))
     return sorted(set(re.findall(r"\b(qr_[a-z0-9_]+)\s*\(", text)))
 
 

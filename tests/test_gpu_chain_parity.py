@@ -180,6 +180,27 @@ def test_truncate():
     _check_same(psi, ref)
 
 
+def test_truncate_to_an_empty_bond():
+    """A threshold above every singular value slices the bond to size 0 (slice! with an empty
+    extent, Chain.jl:404-419), like the oracle: the chain is the null state, its contractions are
+    0 and factorisations refuse it."""
+    psi, ref = _pair(4, 3, seed=12)
+    Q.canonize_site_(psi, 2, "right", "svd")
+    O.canonize_site_(ref, 1, "right", "svd")
+    lam = psi.lambda_between(2, 3)
+    Q.truncate_(psi, (2, 3), threshold=2 * lam[0])
+    O.truncate_(ref, (1, 2), threshold=2 * lam[0])
+    assert psi.bond_dims() == ref.bond_dims() and psi.bond_dims()[1] == 0
+    assert psi.lambda_between(2, 3).size == 0
+    assert psi.site_array(2).size == 0 and psi.site_array(3).size == 0
+    assert Q.norm(psi) == 0.0 and O.norm(ref) == 0.0
+    assert Q.expect(psi, [Q.gate_from_matrix(R.PAULI["Z"], [1])]) == 0
+    with pytest.raises(Q.ArgumentError, match="size 0"):
+        Q.canonize_(psi)
+    with pytest.raises(Q.ArgumentError, match="size 0"):
+        Q.evolve_(psi, Q.gate_from_matrix(np.eye(4), [1, 2]), threshold=1e-10, maxdim=4)
+
+
 def test_contract_between():
     # Chain_test.jl:241-266 runs on rand(Chain, Open, State; n=5, p=2, chi=20): a normalised state
     arrays = R.rand_chain_state_arrays(R.rng(21), 5, 20, p=2)

@@ -1,0 +1,151 @@
+"""GPU parity at the sizes the headline numbers are measured on.
+
+1. The thin SVD at sizes whose Jacobi rounds have more pairs than the grid has resident CTAs, so
+   the sweeps order their rounds by per-column flags (the dataflow ordering) instead of a grid
+   barrier: 2048 x 2048 in the mixed path (FP32 block sweep and double-float polish) and
+   1024 x 1024 in FP64.  The library's path counters must show that ordering ran.  Checked against
+   LAPACK (numpy.linalg.svd): singular values within 1e-10 sigma_max, U S Vh within 1e-10 sigma_max
+   sqrt(n), orthonormal U and Vh.
+2. One evolve! of a Haar gate on a bond whose neighbours both carry chi = 1024 (theta 2048 x 2048,
+   maxdim 1024, cutoff 1e-10; Chain.jl:606-661 then truncate! :390-422) on the 24-site random
+   isometric chain of the benchmark, against the oracle: bond dimensions exact; Lambda within
+   1e-10 (FP64) and 1e-9 (mixed) of sigma_max; local <Z_i> within 1e-8.
+3. The n = 64 TEBD workload (|0...0>, depth-40 Haar brick wall, maxdim 256, cutoff 1e-10) at its
+   full size against the oracle's golden results (tests/golden/make_tebd_golden.py): bond
+   dimensions exact, every bond's Lambda within 1e-10 (FP64) / 1e-8 (mixed) of its largest value,
+   <X_i> and the norm within 1e-10 / 1e-8 relative to <psi|psi> and ||psi||.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+import qrochet as Q
+from oracle import chain_oracle as O
+from qrochet import _lib
+from qrochet import random as R
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PATHS = ["cluster", "block_cluster", "block_barrier", "block_dataflow", "f64_barrier", "f64_dataflow",
+         "f32_barrier", "f32_dataflow", "df_cluster", "df_barrier", "df_dataflow", "qr_precond_fp64",
+         "qr_precond_mixed", "reorth"]
+
+
+def svd_paths():
+    counts = (C.c_uint64 * 32)()
+    total = C.c_int()
+    _lib.check(_lib.lib().qr_test_svd_paths(counts, 32, C.byref(total)))
+    return {name: int(counts[i]) for i, name in enumerate(PATHS[:total.value])}
+
+
+def svd(mode, A):
+    A = np.asfortranarray(A, dtype=np.complex128)
+    m, n = A.shape
+    k = min(m, n)
+    U = np.empty((m, k), dtype=np.complex128, order="F")
+    Vh = np.empty((k, n), dtype=np.complex128, order="F")
+    S = np.empty(k)
+    ms = C.c_double()
+    _lib.check(_lib.lib().qr_test_svd(mode, m, n, _lib.dptr(A), _lib.dptr(U), _lib.dptr(S), _lib.dptr(Vh),
+                                      C.byref(ms)))
+    return U, S, Vh
+
+
+def _graded(g, n, decades):
+    u, _ = np.linalg.qr(R.complex_gaussian(g, (n, n)))
+    v, _ = np.linalg.qr(R.complex_gaussian(g, (n, n)))
+    return (u * np.logspace(0, -decades, n)) @ v.conj().T
+
+
+@pytest.mark.parametrize("mode,case,n,expect_paths", [
+    (1, "gaussian", 2048, ("block_dataflow", "df_dataflow")),
+    (1, "graded", 2048, ("qr_precond_mixed", "block_dataflow", "df_dataflow")),
+    (0, "gaussian", 1024, ("qr_precond_fp64", "f64_dataflow")),
+])
+def test_svd_dataflow_ordering_against_lapack(mode, case, n, expect_paths):
+    g = R.rng(1000 + n + mode)
+    A = R.complex_gaussian(g, (n, n)) if case == "gaussian" else _graded(g, n, 10)
+    before = svd_paths()
+    U, S, Vh = svd(mode, A)
+    after = svd_paths()
+    for p in expect_paths:
+        assert after[p] > before[p], (p, before, after)
+    s_ref = np.linalg.svd(A, compute_uv=False)
+    smax = s_ref[0]
+    assert np.all(np.diff(S) <= 1e-14 * smax)
+    assert np.max(np.abs(S - s_ref)) <= 1e-10 * smax
+    assert np.max(np.abs((U * S) @ Vh - A)) <= 1e-10 * smax * np.sqrt(n)
+    assert np.max(np.abs(U.conj().T @ U - np.eye(n))) <= 1e-10
+    assert np.max(np.abs(Vh @ Vh.conj().T - np.eye(n))) <= 1e-10
+
+
+def _z(i):
+    return O.ODense(R.PAULI["Z"], (O.OSite(i), O.OSite(i, True)))
+
+
+@pytest.fixture(scope="module")
+def chi1024_reference():
+    """The benchmark's chain (24 sites, bonds min(1024, 2^i) mirrored) and the oracle's result of
+    one gate on sites (12, 13), whose bonds on both sides carry chi = 1024."""
+    g = R.rng(2024)
+    arrays = R.rand_chain_state_arrays(g, 24, 1024, p=2)
+    u = R.haar_unitary(R.rng(99), 4)
+    ref = O.from_reference_arrays(arrays)
+    assert ref.bond_dims()[10:13] == [1024, 1024, 1024]
+    O.evolve_2site_(ref, 11, u, threshold=1e-10, maxdim=1024)
+    z = {i: O.expect(ref, [_z(i)]) for i in (12, 13)}
+    return arrays, u, ref, z
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_gate_step_chi1024_against_oracle(chi1024_reference, precision):
+    arrays, u, ref, z_ref = chi1024_reference
+    psi = Q.MPS(arrays)
+    psi.set_precision(precision)
+    before = svd_paths()
+    Q.evolve_(psi, Q.gate_from_matrix(u, [12, 13]), threshold=1e-10, maxdim=1024)
+    after = svd_paths()
+    if precision == "mixed":
+        assert after["block_dataflow"] > before["block_dataflow"]
+        assert after["df_dataflow"] > before["df_dataflow"]
+    else:
+        assert after["f64_dataflow"] > before["f64_dataflow"]
+    assert psi.bond_dims() == ref.bond_dims()
+    assert psi.bond_dims()[11] == 1024
+    lam, lam_ref = psi.lambda_between(12, 13), ref.lam[11]
+    tol_l = 1e-10 if precision == "fp64" else 1e-9
+    assert np.max(np.abs(lam - lam_ref)) <= tol_l * lam_ref[0]
+    for i in (12, 13):
+        e = Q.expect(psi, [Q.gate_from_matrix(R.PAULI["Z"], [i])])
+        assert abs(e - z_ref[i]) <= 1e-8, (i, e, z_ref[i])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_tebd_n64_chi256_depth40_against_golden(precision):
+    gold = np.load(os.path.join(HERE, "golden", "tebd_n64_chi256_d40.npz"))
+    n, depth, maxdim = 64, 40, 256
+    layers = R.brickwall_layers(n, depth, seed=2)
+    cs = float(sum(np.abs(u).sum() + 0.5 * u.real.sum() for layer in layers for _, u in layer))
+    assert abs(cs - float(gold["gate_checksum"])) <= 1e-9 * abs(cs)
+    psi = Q.MPS(R.zero_product_arrays(n))
+    psi.set_precision(precision)
+    for layer in layers:
+        for s, u in layer:
+            Q.evolve_(psi, Q.gate_from_matrix(u, [s, s + 1]), threshold=1e-10, maxdim=maxdim)
+    assert psi.bond_dims() == [int(b) for b in gold["bond_dims"]]
+    tol = 1e-10 if precision == "fp64" else 1e-8
+    lam_gold = np.split(gold["lambdas"], np.cumsum(gold["bond_dims"])[:-1])
+    for b in range(n - 1):
+        lam = psi.lambda_between(b + 1, b + 2)
+        assert np.max(np.abs(lam - lam_gold[b])) <= tol * lam_gold[b][0], b
+    # evolve! without iscanonical keeps every bond's Lambda as a separate tensor and truncates theta
+    # without the neighbouring weights (Chain.jl:606-661), so the state's norm is not preserved
+    # (~1e-13 here): <X_i> (unnormalised, as expect returns it) is compared relative to <psi|psi>
+    nrm2 = float(gold["norm"]) ** 2
+    for i in range(1, n + 1):
+        e = Q.expect(psi, [Q.gate_from_matrix(R.PAULI["X"], [i])])
+        assert abs(e - gold["x"][i - 1]) <= tol * nrm2, (i, e, gold["x"][i - 1])
+    assert abs(Q.norm(psi) - float(gold["norm"])) <= tol * float(gold["norm"])

@@ -56,3 +56,19 @@ def test_results_same_alone_and_in_the_mix():
     assert st["completed"] == len(reqs) and st["in_flight"] == 0
     for a, b in zip(alone, mixed):
         assert np.max(np.abs(a - b)) <= 1e-12
+
+
+def test_large_mixed_requests_same_alone_and_in_the_mix():
+    """Mixed-precision requests whose bonds reach chi = 128-256 (theta of 256-512 columns: the
+    FP32-preconditioned SVD with the double-float polish, beyond the single-cluster kernels), run
+    alone and then four at a time on one GPU; every expectation value must agree within 1e-12."""
+    g = R.rng(23)
+    reqs = [S.random_request(g, n_range=(16, 18), depth_range=(8, 10), chi_choices=(128, 256), nobs=4)
+            for _ in range(4)]
+    with S.Server(workers=1, precision="mixed") as sv:
+        alone = [sv.wait(sv.submit(r))["values"] for r in reqs]
+    with S.Server(workers=4, precision="mixed") as sv:
+        tickets = [sv.submit(r) for r in reqs]
+        mixed = [sv.wait(t)["values"] for t in tickets]
+    for a, b in zip(alone, mixed):
+        assert np.max(np.abs(a - b)) <= 1e-12

@@ -141,3 +141,15 @@ def test_order_permutation():
     b = O.from_reference_arrays(perm, order=("r", "o", "l"))
     assert np.allclose(_sv(a), _sv(b))
     assert a.bond_dims() == [1, 3]
+
+
+def test_truncate_to_an_empty_extent_leaves_a_size_0_bond():
+    """truncate! slices with whatever extent survives the filter (Chain.jl:404-419); an empty one
+    leaves a bond of size 0 and a null state."""
+    arrays = R.gaussian_mps_arrays(4, 3, seed=5, uniform=False)
+    ch = O.from_reference_arrays(arrays)
+    O.canonize_site_(ch, 1, "right", "svd")
+    O.truncate_(ch, (1, 2), threshold=10 * ch.lam[1][0])
+    assert ch.bond_dims()[1] == 0 and ch.lam[1].size == 0
+    assert ch.sites[1].shape[2] == 0 and ch.sites[2].shape[0] == 0
+    assert O.norm(ch) == 0.0
