@@ -51,9 +51,11 @@ def parse():
     p.add_argument("--launch-list", action="store_true",
                    help="only the warm-up and timed steps of the mixed path (for ncu launch lists)")
     p.add_argument("--batched", type=int, default=128, help="requests in the batched sample (0: skip)")
-    p.add_argument("--serve", type=int, default=32, help="requests in the serving sample (0: skip)")
-    p.add_argument("--serve-sat", type=int, default=96,
+    p.add_argument("--serve", type=int, default=24, help="requests in the serving sample (0: skip)")
+    p.add_argument("--serve-sat", type=int, default=64,
                    help="requests in the saturated mixed-precision serving sample (0: skip)")
+    p.add_argument("--serve-full", type=int, default=16,
+                   help="requests in the mixed-precision sample over every chi_max class (0: skip)")
     p.add_argument("--mpo-sites", type=int, default=128, help="sites of the MPO environment sweep (0: skip)")
     p.add_argument("--workers", type=int, default=16)
     p.add_argument("--no-tebd", action="store_true", help="skip the n=64, chi_max=256, depth-40 TEBD leg")
@@ -266,23 +268,29 @@ def run_batched(args, Q, dist, rank, world):
 
 def run_serving(args, Q, dist, rank, world):
     """Serving: Poisson arrivals at 200 req/s of random brick-wall circuits with 8 Pauli strings of
-    weight 1-4; p50/p99 latency and solves/s for the FP64 and mixed forms.  Bounded sample:
-    n ~ U[16,64], depth ~ U[4,16], chi_max in {32, 128}.  With `--serve` requests (2x the
-    workers by default) half the requests start at once, so p99/p50 mostly shows the spread of the
-    requests' own service times; the `mixed_saturated` sample (`--serve-sat`, 6x the workers)
-    keeps a queue in front of every worker for most of the run, the regime in which a serving loop
-    is judged at saturation."""
+    weight 1-4; p50/p99 latency and solves/s.  Bounded samples:
+      - fp64 / mixed: `--serve` requests, n ~ U[16,64], depth ~ U[4,16], chi_max in {32, 128}; the
+        two forms' expectation values are compared;
+      - mixed_saturated: `--serve-sat` requests of the same distribution (~4x the workers), so a
+        queue stands in front of every worker for most of the run;
+      - mixed_full_chi: `--serve-full` requests over every chi_max class {32, 128, 512, 1024} of the
+        serving distribution, on n ~ U[16,32], depth ~ U[4,10]."""
     from qrochet import serve as S
     from qrochet import random as R
 
     out = {}
-    runs = [("fp64", "fp64", args.serve), ("mixed", "mixed", args.serve)]
+    small = dict(n_range=(16, 64), depth_range=(4, 16), chi_choices=(32, 128))
+    runs = [("fp64", "fp64", args.serve, small), ("mixed", "mixed", args.serve, small)]
     if args.serve_sat > 0:
-        runs.append(("mixed_saturated", "mixed", args.serve_sat))
-    for name, prec, nreq in runs:
+        runs.append(("mixed_saturated", "mixed", args.serve_sat, small))
+    if args.serve_full > 0:
+        # every chi_max class of the serving distribution, on shorter and shallower circuits so the
+        # chi_max = 512 / 1024 requests take seconds, not minutes
+        runs.append(("mixed_full_chi", "mixed", args.serve_full,
+                     dict(n_range=(16, 32), depth_range=(4, 10), chi_choices=(32, 128, 512, 1024))))
+    for name, prec, nreq, dist_kw in runs:
         g = R.rng(5)
-        reqs = [S.random_request(g, n_range=(16, 64), depth_range=(4, 16), chi_choices=(32, 128), nobs=8)
-                for _ in range(nreq)]
+        reqs = [S.random_request(g, nobs=8, **dist_kw) for _ in range(nreq)]
         # arrivals at 200 req/s in total: each replica sees its share of the Poisson stream
         gaps = shard(g.exponential(1.0 / 200.0, size=len(reqs)).cumsum(), rank, world)
         reqs = shard(reqs, rank, world)
@@ -305,10 +313,14 @@ def run_serving(args, Q, dist, rank, world):
     err = max(float(np.max(np.abs(a - b))) for a, b in zip(out["fp64"]["values"], out["mixed"]["values"]))
     for prec in out:
         del out[prec]["values"]
+    if "mixed_full_chi" in out:
+        out["mixed_full_chi"]["sample"] = (f"{args.serve_full} requests: n~U[16,32], depth~U[4,10], "
+                                           f"chi_max in {{32,128,512,1024}}, 8 Pauli strings of weight 1-4, seed 5")
     out["max_abs_expectation_diff_mixed_vs_fp64"] = err
     out["arrival_rate_per_s"] = 200
     out["workers"] = args.workers
-    out["sample"] = "n~U[16,64], depth~U[4,16], chi_max in {32,128}, 8 Pauli strings of weight 1-4, seed 5"
+    out["sample"] = ("fp64 / mixed / mixed_saturated: n~U[16,64], depth~U[4,16], chi_max in {32,128}, 8 Pauli "
+                     "strings of weight 1-4, seed 5")
     return out
 
 
@@ -355,43 +367,67 @@ def run_mpo_env(args, Q):
 
 def run_tebd(args, Q, local):
     """TEBD at full size: n = 64 qubits from |0...0>, a depth-40 brick wall of Haar 4 x 4 gates
-    (seed 2), maxdim 256, cutoff 1e-10, in FP64 and in the mixed path.  Errors of every bond's
-    Lambda spectrum and of <X_i> are taken against the oracle's golden results for the same gates
-    (tests/golden/tebd_n64_chi256_d40.npz, written by make_tebd_golden.py next to it)."""
+    (seed 2), maxdim 256, cutoff 1e-10.
+      - mixed: all 40 layers; every bond's Lambda spectrum and <X_i> against the oracle's golden
+        results for the same gates (tests/golden/tebd_n64_chi256_d40.npz, made by
+        make_tebd_golden.py next to it);
+      - fp64 vs mixed: from the mixed state after layer 30 (bonds saturated at chi = 256), the last
+        10 layers in both precisions: gate-steps/s of each and the mixed path's error against the
+        FP64 path on the same start state.  (The FP64 path's full 40 layers take ~160 s; the
+        GPU test suite runs them against the golden results.)"""
     from qrochet import random as R
 
     gold = np.load(os.path.join(ROOT, "tests", "golden", "tebd_n64_chi256_d40.npz"))
-    n, depth, maxdim = 64, 40, 256
+    n, depth, maxdim, split_at = 64, 40, 256, 30
     layers = R.brickwall_layers(n, depth, seed=2)
-    ngates = sum(len(layer) for layer in layers)
     lam_gold = np.split(gold["lambdas"], np.cumsum(gold["bond_dims"])[:-1])
-    out = {"n": n, "depth": depth, "chi_max": maxdim, "threshold": 1e-10, "gates": ngates,
+    nrm2 = float(gold["norm"]) ** 2
+    out = {"n": n, "depth": depth, "chi_max": maxdim, "threshold": 1e-10, "gates": sum(len(x) for x in layers),
            "note": "evolve! defaults (iscanonical=false): Lambdas stay on the bonds and theta is truncated "
-                   "without the neighbouring weights, so the norm decays (oracle: %.3g); <X_i> errors are "
-                   "relative to <psi|psi>" % float(gold["norm"])}
-    for prec in ("fp64", "mixed"):
-        psi = Q.MPS(R.zero_product_arrays(n))
-        psi.set_precision(prec)
+                   "without the neighbouring weights, so the norm decays (oracle: %.3g) and the maxdim "
+                   "truncation amplifies rounding differences over the 40 layers; <X_i> errors are relative to "
+                   "<psi|psi>" % float(gold["norm"])}
+
+    def run_layers(psi, ls):
         psi.sync()
         t = DevTimer(psi.stream(), local)
         t.start()
-        for layer in layers:
+        for layer in ls:
             for s_, u in layer:
                 Q.evolve_(psi, Q.gate_from_matrix(u, [s_, s_ + 1]), threshold=1e-10, maxdim=maxdim)
-        dt = t.stop()
-        bonds = psi.bond_dims()
-        same = bonds == [int(b) for b in gold["bond_dims"]]
-        lam_err = max(float(np.max(np.abs(psi.lambda_between(b + 1, b + 2) - lam_gold[b])) / lam_gold[b][0])
-                      for b in range(n - 1)) if same else None
-        x = np.array([Q.expect(psi, [Q.gate_from_matrix(R.PAULI["X"], [i])]) for i in range(1, n + 1)])
-        nrm2 = float(gold["norm"]) ** 2
-        out[prec] = {"gate_steps_per_s": ngates / dt, "s": dt, "bond_dims_match_oracle": same,
-                     "lambda_max_rel_err_vs_oracle": lam_err,
-                     "x_max_abs_err_vs_oracle_over_norm2": float(np.max(np.abs(x - gold["x"]))) / nrm2,
-                     "norm_rel_err_vs_oracle": abs(Q.norm(psi) - float(gold["norm"])) / float(gold["norm"]),
-                     "max_bond": int(max(bonds))}
-        del psi
-    out["mixed_over_fp64"] = out["mixed"]["gate_steps_per_s"] / out["fp64"]["gate_steps_per_s"]
+        return t.stop(), sum(len(x) for x in ls)
+
+    def xs(psi):
+        return np.array([Q.expect(psi, [Q.gate_from_matrix(R.PAULI["X"], [i])]) for i in range(1, n + 1)])
+
+    psi = Q.MPS(R.zero_product_arrays(n))
+    psi.set_precision("mixed")
+    t1, g1 = run_layers(psi, layers[:split_at])
+    mid = psi.copy()
+    t2, g2 = run_layers(psi, layers[split_at:])
+    bonds = psi.bond_dims()
+    same = bonds == [int(b) for b in gold["bond_dims"]]
+    xm = xs(psi)
+    out["mixed"] = {"gate_steps_per_s": (g1 + g2) / (t1 + t2), "s": t1 + t2, "bond_dims_match_oracle": same,
+                    "lambda_max_rel_err_vs_oracle": (max(
+                        float(np.max(np.abs(psi.lambda_between(b + 1, b + 2) - lam_gold[b])) / lam_gold[b][0])
+                        for b in range(n - 1)) if same else None),
+                    "x_max_abs_err_vs_oracle_over_norm2": float(np.max(np.abs(xm - gold["x"]))) / nrm2,
+                    "norm_rel_err_vs_oracle": abs(Q.norm(psi) - float(gold["norm"])) / float(gold["norm"])}
+    mid.set_precision("fp64")
+    t3, g3 = run_layers(mid, layers[split_at:])
+    xf = xs(mid)
+    nf2 = Q.norm(mid) ** 2
+    same2 = mid.bond_dims() == bonds
+    out["last_layers_fp64_vs_mixed"] = {
+        "layers": f"{split_at + 1}-{depth}", "gates": g3,
+        "fp64_gate_steps_per_s": g3 / t3, "mixed_gate_steps_per_s": g2 / t2, "mixed_over_fp64": (g2 / t2) / (g3 / t3),
+        "bond_dims_match": same2,
+        "lambda_max_rel_err_mixed_vs_fp64": (max(
+            float(np.max(np.abs(psi.lambda_between(b + 1, b + 2) - mid.lambda_between(b + 1, b + 2))) /
+                  mid.lambda_between(b + 1, b + 2)[0]) for b in range(n - 1)) if same2 else None),
+        "x_max_abs_err_mixed_vs_fp64_over_norm2": float(np.max(np.abs(xm - xf))) / nf2}
+    del psi, mid
     return out
 
 

@@ -17,11 +17,12 @@
 //     a k-block (64 k' columns: 128-byte rows, 128-byte swizzle) of all three slices of A and B
 //     into one of two shared-memory stages; warp 1 issues, per k-block, the six slice products
 //     (l h, h l, m m, m h, h m, h h) as tcgen05.mma kind::f16 (BF16 in, FP32 accumulate,
-//     M = 128, N = 128, K = 16 per instruction) into a TMEM accumulator; warps 2-9 drain the
-//     accumulator every TC_CHUNK k-blocks with tcgen05.ld and add it to FP32 registers with
-//     round-to-nearest adds, so the tensor cores' own accumulation only ever spans 2 TC_CHUNK
-//     64-wide k-blocks.  Two TMEM accumulators alternate so the drain overlaps the next chunk's
-//     MMAs.  Every wait on an mbarrier is bounded; a timeout sets an error flag, the CTA drains its
+//     M = 128, N = 128, K = 16 per instruction): the five correction products into one TMEM
+//     accumulator, the h h product into another; warps 2-9 drain both after every k-block with
+//     tcgen05.ld and add them to FP32 registers with round-to-nearest adds.  The tensor cores' own
+//     accumulation of the leading term thus spans 4 instructions (64 k'), which keeps the bias of
+//     their FP32 accumulation at the level of one add per 64 products.  Two pairs of TMEM
+//     accumulators alternate so the drain overlaps the next k-block's MMAs.  Every wait on an mbarrier is bounded; a timeout sets an error flag, the CTA drains its
 //     own copies and MMAs in flight, frees its TMEM and returns.
 //
 // Result accuracy ~FP32 (relative error ~sqrt(K) 2^-24), at (BF16 rate) / 6 real-product
@@ -42,10 +43,10 @@ constexpr int TC_BK = 64;   // k' columns of a k-block (128-byte bf16 rows)
 constexpr int TC_STAGES = 2;
 constexpr int TC_TILE = TC_BM * TC_BK * 2;  // bytes of one slice tile (A and B alike: 16 KiB)
 constexpr int TC_STAGE = 6 * TC_TILE;        // A h/m/l + B h/m/l
-constexpr int TC_CHUNK = 2;                  // k-blocks per TMEM accumulation
+constexpr int TC_CHUNK = 1;                  // k-blocks per TMEM accumulation
 constexpr int TC_THREADS = 320;              // warp 0 TMA, warp 1 MMA + TMEM, warps 2-9 epilogue
 constexpr int TC_EPI_WARPS = 8;              // two per TMEM lane quarter, 64 columns each
-constexpr int TC_TMEM_COLS = 2 * TC_BN;      // two FP32 accumulators of 128 columns
+constexpr int TC_TMEM_COLS = 4 * TC_BN;      // two buffers x (corrections, leading term), FP32
 constexpr int TC_SMEM = TC_STAGES * TC_STAGE + 1024 /* alignment */ + 256 /* barriers */;
 constexpr unsigned TC_SPIN = 1u << 24;       // polls before a wait gives up (seconds)
 
@@ -288,7 +289,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         const uint32_t aph = (uint32_t)(c >> 1) & 1u;
         if (*abort_flag || !mbar_wait(aempty + buf, aph ^ 1u, abort_flag)) { ok = false; break; }
         tc_fence_after();
-        const uint32_t dt = tmem + (uint32_t)(buf * TC_BN);
+        const uint32_t dt = tmem + (uint32_t)(buf * 2 * TC_BN);  // corrections; + TC_BN: h h
         const int kb1 = min(nk, (c + 1) * TC_CHUNK);
         for (int kb = c * TC_CHUNK; kb < kb1; kb++) {
           const int s = kb % TC_STAGES;
@@ -299,10 +300,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
           for (int p = 0; p < 6; p++) {
             const uint32_t a0 = st + kPairA[p] * TC_TILE, b0 = st + (3 + kPairB[p]) * TC_TILE;
+            const bool lead = p == 5;  // h h
+            const uint32_t d = lead ? dt + TC_BN : dt;
 #pragma unroll
             for (int j = 0; j < TC_BK / 16; j++) {
-              const uint32_t acc = (kb > c * TC_CHUNK || p > 0 || j > 0) ? 1u : 0u;
-              tc_mma(dt, smem_desc(a0 + 32 * j), smem_desc(b0 + 32 * j), acc);
+              const uint32_t acc = (kb > c * TC_CHUNK || (!lead && p > 0) || j > 0) ? 1u : 0u;
+              tc_mma(d, smem_desc(a0 + 32 * j), smem_desc(b0 + 32 * j), acc);
             }
           }
           tc_commit(empty + s);  // the stage is free once these MMAs have read it
@@ -334,13 +337,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       got = __shfl_sync(0xffffffffu, got, 0);
       if (!got) { ok = false; break; }
       tc_fence_after();
-      const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(buf * TC_BN + half * EC);
+      const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(buf * 2 * TC_BN + half * EC);
 #pragma unroll
       for (int j = 0; j < EC / 32; j++) {
-        float v[32];
-        tmem_ld32(ta + 32 * j, v);
+        float v[32], w[32];
+        tmem_ld32(ta + 32 * j, v);          // corrections
+        tmem_ld32(ta + TC_BN + 32 * j, w);  // leading term
 #pragma unroll
-        for (int i = 0; i < 32; i++) acc[32 * j + i] = __fadd_rn(acc[32 * j + i], v[i]);
+        for (int i = 0; i < 32; i++) acc[32 * j + i] = __fadd_rn(acc[32 * j + i], __fadd_rn(w[i], v[i]));
       }
       tc_fence_before();
       __syncwarp();

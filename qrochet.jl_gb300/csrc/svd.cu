@@ -1384,6 +1384,25 @@ __global__ void max_reduce_k(const double* __restrict__ nrm, int k, double* __re
   }
 }
 
+// out = max over the rows x k entries of max(|re|, |im|), as the bits of a non-negative double
+// (their unsigned order is the numeric order); NaN entries propagate as NaN
+__global__ void max_abs_k(const double2* __restrict__ B, long ldb, int rows, int k, unsigned long long* out) {
+  double m = 0.0;
+  const long total = (long)rows * k;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+    const double2 v = B[t % rows + (t / rows) * ldb];
+    double a = fabs(v.x);
+    const double b = fabs(v.y);
+    a = (b > a || b != b) ? b : a;  // fmax would drop a NaN
+    m = (a > m || a != a) ? a : m;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const double x = __shfl_xor_sync(0xffffffffu, m, o);
+    m = (x > m || x != x) ? x : m;
+  }
+  if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
+}
+
 // nrm[j] = |col_j| in FP64 (one warp per column)
 template <typename C>
 __global__ void col_norms_k(const C* __restrict__ B, long ldb, int m, int n, double* __restrict__ nrm) {
@@ -2032,9 +2051,9 @@ extern "C" int qr_svd_noalloc(int m, int n, const double* A, long lda, double* U
     QR_TRY(ztranspose(s, Ad, lda, m, n, B, rows, 1));
   }
 
-  // Column norms on the host (a stack array: no allocation).  B is scaled by the power of two
-  // 2^-e that brings its largest column norm into [1/2, 1): the rotation test squares column
-  // norms and inner products, which would underflow below ~1e-154 or overflow above ~1e154.
+  // Column norms on the host (a stack array: no allocation).  B is first scaled by the power of
+  // two 2^-e that brings its largest entry into [1/2, 1): the rotation test squares column norms
+  // and inner products, which would underflow below ~1e-154 or overflow above ~1e154.
   double hn[NOALLOC_MAX_K];
   auto host_max_norm = [&](const double2* X, long ldx, int r, double* out) -> int {
     col_norms_k<double2><<<ceil_div((long)k * 32, TPB), TPB, 0, s>>>(X, ldx, r, k, nrm);
@@ -2046,12 +2065,20 @@ extern "C" int qr_svd_noalloc(int m, int n, const double* A, long lda, double* U
     *out = mx;
     return QR_OK;
   };
+  // the exponent comes from the largest |re| or |im| (squares of entries near the ends of the
+  // range would under- or overflow); after the scaling every column norm is finite and O(1)
+  QR_CUDA(cudaMemsetAsync(nrm, 0, sizeof(double), s));
+  max_abs_k<<<gs((long)rows * k), TPB, 0, s>>>(B, rows, rows, k, reinterpret_cast<unsigned long long*>(nrm));
+  QR_CHECK_LAUNCH("max_abs_k");
+  QR_CUDA(cudaMemcpyAsync(hn, nrm, sizeof(double), cudaMemcpyDeviceToHost, s));
+  QR_CUDA(cudaStreamSynchronize(s));
+  const double amax = hn[0];
+  if (!std::isfinite(amax)) return fail(QR_EINVAL, "qr_svd_noalloc: non-finite entries");
+  int e2 = 0;
+  if (amax > 0.0) frexp(amax, &e2);
+  QR_TRY(zscale_matrix(s, rows, k, make_double2(ldexp(1.0, -e2), 0.0), B, rows, 0, 1));
   double smax = 0.0;
   QR_TRY(host_max_norm(B, rows, rows, &smax));
-  if (!std::isfinite(smax)) return fail(QR_EINVAL, "qr_svd_noalloc: non-finite entries");
-  int e2 = 0;
-  if (smax > 0.0) frexp(smax, &e2);
-  QR_TRY(zscale_matrix(s, rows, k, make_double2(ldexp(1.0, -e2), 0.0), B, rows, 0, 1));
 
   // QR preconditioning above 32 columns, as in the allocating FP64 path: B = Q R and the sweeps
   // run on W = R^H (k x k), which converges in ~10 sweeps even when the singular values spread
@@ -2063,8 +2090,6 @@ extern "C" int qr_svd_noalloc(int m, int n, const double* A, long lda, double* U
     QR_TRY(ztranspose(s, V, k, k, k, B, k, 1));
     jr = k;
     QR_TRY(host_max_norm(B, k, k, &smax));
-  } else {
-    smax = smax > 0.0 ? ldexp(smax, -e2) : 0.0;
   }
   QR_TRY(zset_identity(s, V, k, k, k));
 
