@@ -223,7 +223,7 @@ def run_batched(args, Q, dist, rank, world):
     cutoff 1e-10) with chi_max log-uniform in {16, 32, 64}: the bond classes the batched engine
     takes (theta up to 128 x 128).  Two paths on the same requests:
       - engine: qr_batch -- every layer of all requests one fused launch, device-side truncation,
-        the whole circuit one CUDA graph (FP64 SVD);
+        the whole circuit one CUDA graph; mixed (FP32-preconditioned SVD, FP64 finish) and FP64;
       - server: the continuous-batching request server, one chain and stream per request, mixed
         precision.
     The chi_max in {128, 256, 512} part of the distribution is outside the engine's bond limit and
@@ -236,19 +236,23 @@ def run_batched(args, Q, dist, rank, world):
     out = {"requests": int(dist.sum(len(reqs))), "gates": int(gates),
            "sample": f"{args.batched} requests: n~U[8,96], depth~U[4,32], chi_max log-uniform in {{16,32,64}}, "
                      f"cutoff 1e-10, 1 Pauli string each, seed 4"}
-    with Batch(device=0) as bt:
-        for r in reqs:
-            bt.add(r)
-        dist.barrier()
-        t0 = time.perf_counter()
-        bt.run()
-        dt = dist.max(time.perf_counter() - t0)
-        info = bt.info()
-        vals_engine = [bt.values(i) for i in range(len(reqs))]
-    out["engine"] = {"solves_per_s": out["requests"] / dt, "gate_steps_per_s": gates / dt, "wall_s": dt,
-                     "graph_ms": info["graph_ms"], "autotune_ms": info["tune_ms"], "layers": info["layers"],
-                     "launches": info["launches"], "graph_nodes": info["graph_nodes"],
-                     "warps_per_cta": info["warps_per_cta"], "precision": "fp64"}
+    vals_engine = None
+    for prec in ("mixed", "fp64"):
+        with Batch(device=0, precision=prec) as bt:
+            for r in reqs:
+                bt.add(r)
+            dist.barrier()
+            t0 = time.perf_counter()
+            bt.run()
+            dt = dist.max(time.perf_counter() - t0)
+            info = bt.info()
+            if prec == "mixed":
+                vals_engine = [bt.values(i) for i in range(len(reqs))]
+        out["engine" if prec == "mixed" else "engine_fp64"] = {
+            "solves_per_s": out["requests"] / dt, "gate_steps_per_s": gates / dt, "wall_s": dt,
+            "graph_ms": info["graph_ms"], "autotune_ms": info["tune_ms"], "layers": info["layers"],
+            "launches": info["launches"], "graph_nodes": info["graph_nodes"],
+            "warps_per_cta": info["warps_per_cta"], "precision": prec}
     with S.Server(workers=args.workers, precision="mixed") as sv:
         dist.barrier()
         t0 = time.perf_counter()

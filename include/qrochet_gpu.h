@@ -179,7 +179,7 @@ int qr_server_stats(qr_server* s, uint64_t* submitted, uint64_t* completed, int*
    qr_server_submit format (a gate circuit on |0...0>, then Pauli strings) with chi_max <= 64.
    qr_batch_run keeps every chain in fixed-capacity device buffers, takes each truncation decision
    on the device, runs each brick-wall layer of all requests as one fused launch (one CTA per
-   gate: theta, gate, FP64 Jacobi SVD, truncation, write-back), captures the whole circuit and the
+   gate: theta, gate, Jacobi SVD, truncation, write-back), captures the whole circuit and the
    expectation sweep in one CUDA graph and launches it once.  The layer kernel's CTA size is
    autotuned per device and bond class (cached in the process, and in the file named by
    QROCHET_TUNE_FILE when set).  A request whose truncation would empty a bond, or whose SVD did
@@ -187,6 +187,10 @@ int qr_server_stats(qr_server* s, uint64_t* submitted, uint64_t* completed, int*
 typedef struct qr_batch qr_batch;
 int qr_batch_create(int device, qr_batch** out);
 int qr_batch_free(qr_batch* b);
+/* QR_FP64 (default): every gate's SVD in FP64.  QR_MIXED: SVDs of more than 32 columns run FP32
+   Jacobi sweeps first, one FP64 Newton-Schulz step on their rotations, then FP64 sweeps to the
+   FP64 tolerance; singular values, vectors and truncation decisions stay FP64.  Before run. */
+int qr_batch_set_precision(qr_batch* b, int mode);
 int qr_batch_add(qr_batch* b, int n, int chi_max, double threshold, int ngates, const int* gate_site,
                  const double* gate_mats, int nobs, const int* obs_weight, const int* obs_sites,
                  const int* obs_paulis, int* id);

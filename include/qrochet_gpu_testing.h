@@ -28,8 +28,6 @@ int qr_probe_peak(int kind, double* tflops);
 int qr_test_zgemm(int opA, int opB, int M, int N, int K, const double* alpha, const double* A, long lda,
                   const double* B, long ldb, const double* beta, double* C, long ldc, const double* dk,
                   int iters, double* ms_per_iter);
-int qr_test_zgemm_split(int opA, int opB, int M, int N, int K, const double* A, long lda, const double* B,
-                        long ldb, double* C, long ldc, int iters, double* ms_per_iter);
 /* C[b] = op(A[b]) op(B[b]) on the tcgen05 tensor cores (TMA-staged BF16x3 slices, TMEM
    accumulators); `batch` matrices at strides sA / sB (sB = 0: B shared), C[b] at b * ldc * N. */
 int qr_test_zgemm_tc(int opA, int opB, int M, int N, int K, int batch, const double* A, long lda, long sA,

@@ -11,7 +11,8 @@
 //     and rewrite: the truncation decision (the first min(k, maxdim) singular values above the
 //     threshold) is taken on the device, so no layer waits for the host;
 //   - one CTA runs one whole gate step: theta = A_l diag(Lambda) A_r, the gate, a one-sided
-//     Jacobi SVD in FP64 (theta of at most 128 x 128: chi_max <= 64), the sort, the truncation,
+//     Jacobi SVD (theta of at most 128 x 128: chi_max <= 64; FP64, or with QR_MIXED FP32 sweeps
+//     first and FP64 sweeps to finish), the sort, the truncation,
 //     re-orthonormalisation of the kept vectors when their singular values fall below 1e-3
 //     sigma_max (classical Gram-Schmidt twice), and the write-back of U, Vh and Lambda.  A
 //     layer's gates sit on disjoint bonds, so the CTAs of one launch never touch the same site;
@@ -36,7 +37,8 @@ namespace {
 constexpr int BT_MAXK = 128;         // largest theta side: chi_max <= 64
 constexpr int BT_MAXCHI = BT_MAXK / 2;
 constexpr int BT_MAX_SWEEPS = 60;
-constexpr size_t BT_SLOT = 3 * (size_t)BT_MAXK * BT_MAXK;  // B, V, W (double2) per CTA slot
+constexpr size_t BT_SLOT = 4 * (size_t)BT_MAXK * BT_MAXK;  // B, V, W, Tm (double2) per CTA slot
+constexpr int BT_MIXED_MIN = 32;  // the mixed SVD precondition in FP32 above this many columns
 
 struct BTask {
   double2* sl;          // left site buffer
@@ -63,8 +65,74 @@ struct BObs {
 // ---- the fused gate step ------------------------------------------------------------------------
 __device__ __forceinline__ double2 zmul(double2 a, double2 b) { return cmul(a, b); }
 
+// Hestenes sweeps of one CTA on B (rows x k, ld rows) accumulating V (k x k, ld k) in precision
+// T: round-robin pairs, one warp per pair, a CTA barrier between rounds.  Stops after a sweep that
+// rotates nothing or whose largest rotation tangent is below tan_stop; returns that verdict.
+template <typename T>
+__device__ bool cta_sweeps(cplx_t<T>* __restrict__ B, cplx_t<T>* __restrict__ V, int rows, int k, T tol, T smax,
+                           int max_sweeps, float tan_stop, unsigned* rot_count, unsigned* tmax_bits) {
+  using Cx = cplx_t<T>;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int np = k + (k & 1), npairs = np / 2;
+  bool converged = false;
+  for (int sweep = 0; sweep < max_sweeps && !converged; sweep++) {
+    if (threadIdx.x == 0) { *rot_count = 0u; *tmax_bits = 0u; }
+    __syncthreads();
+    for (int round = 0; round < np - 1; round++) {
+      for (int pair = warp; pair < npairs; pair += nw) {
+        int p, q;
+        if (pair == 0) { p = round; q = np - 1; }
+        else { p = (round + pair) % (np - 1); q = (round - pair + np - 1) % (np - 1); }
+        if (p > q) { const int x = p; p = q; q = x; }
+        if (q >= k) continue;
+        Cx* bp = B + (long)rows * p;
+        Cx* bq = B + (long)rows * q;
+        T a = 0, bb = 0, gr = 0, gi = 0;
+        for (int r = lane; r < rows; r += 32) {
+          const Cx x = bp[r], y = bq[r];
+          a += x.x * x.x + x.y * x.y;
+          bb += y.x * y.x + y.y * y.y;
+          gr += x.x * y.x + x.y * y.y;
+          gi += x.x * y.y - x.y * y.x;
+        }
+        a = warp_sum(a); bb = warp_sum(bb); gr = warp_sum(gr); gi = warp_sum(gi);
+        T c, sr, si;
+        float tabs;
+        if (!rotation_params<T>(a, bb, gr, gi, tol, smax, c, sr, si, tabs)) continue;
+        for (int r = lane; r < rows; r += 32) {
+          Cx x = bp[r], y = bq[r];
+          rot(x, y, c, sr, si);
+          bp[r] = x;
+          bq[r] = y;
+        }
+        Cx* vp = V + (long)k * p;
+        Cx* vq = V + (long)k * q;
+        for (int r = lane; r < k; r += 32) {
+          Cx x = vp[r], y = vq[r];
+          rot(x, y, c, sr, si);
+          vp[r] = x;
+          vq[r] = y;
+        }
+        if (lane == 0) {
+          atomicAdd(rot_count, 1u);
+          atomicMax(tmax_bits, __float_as_uint(tabs));
+        }
+      }
+      __syncthreads();
+    }
+    converged = *rot_count == 0u || __uint_as_float(*tmax_bits) < tan_stop;
+    __syncthreads();
+  }
+  return converged;
+}
+
 // One CTA per task (strided over the layer's tasks).  ws: BT_SLOT double2 per CTA.  dry = 1 runs
-// the arithmetic without writing the chain (the autotuner's timing runs).
+// the arithmetic without writing the chain (the autotuner's timing runs).  MIXED: above
+// BT_MIXED_MIN columns the SVD first runs FP32 sweeps on a copy of theta (64x the FP64 rate on
+// this part), makes their rotations unitary to ~1e-12 with one FP64 Newton-Schulz step
+// X <- X + X (I - X^H X) / 2, forms B = theta X in FP64 and lets the FP64 sweeps finish from
+// couplings of ~1e-6 (two or three sweeps instead of eight to ten).
+template <bool MIXED>
 __global__ void __launch_bounds__(512, 1)
     batch_gate_k(const BTask* __restrict__ tasks, int ntasks, double2* __restrict__ ws, int dry) {
   __shared__ BTask T;
@@ -80,6 +148,7 @@ __global__ void __launch_bounds__(512, 1)
   double2* B = ws + (size_t)blockIdx.x * BT_SLOT;
   double2* V = B + (size_t)BT_MAXK * BT_MAXK;
   double2* W = V + (size_t)BT_MAXK * BT_MAXK;
+  double2* Tm = W + (size_t)BT_MAXK * BT_MAXK;
 
   for (int ti = blockIdx.x; ti < ntasks; ti += gridDim.x) {
     if (tid == 0) T = tasks[ti];
@@ -150,59 +219,48 @@ __global__ void __launch_bounds__(512, 1)
     }
     __syncthreads();
 
-    // ---- Hestenes sweeps, round-robin pairs, one warp per pair
-    const int np = k + (k & 1), npairs = np / 2;
+    // ---- Hestenes sweeps (optionally preconditioned in FP32)
     const double tol = sqrt((double)rows) * Eps<double>::v;
     const double smax = smax_s;
-    bool converged = false;
-    for (int sweep = 0; sweep < BT_MAX_SWEEPS && !converged; sweep++) {
-      if (tid == 0) { rot_count = 0u; tmax_bits = 0u; }
+    if (MIXED && k > BT_MIXED_MIN) {
+      float2* B32 = reinterpret_cast<float2*>(W);
+      float2* V32 = B32 + (size_t)rows * k;
+      for (int t = tid; t < rows * k; t += blockDim.x) B32[t] = make_float2((float)B[t].x, (float)B[t].y);
+      for (int t = tid; t < k * k; t += blockDim.x) V32[t] = make_float2((t % k) == (t / k) ? 1.f : 0.f, 0.f);
       __syncthreads();
-      for (int round = 0; round < np - 1; round++) {
-        for (int pair = warp; pair < npairs; pair += nw) {
-          int p, q;
-          if (pair == 0) { p = round; q = np - 1; }
-          else { p = (round + pair) % (np - 1); q = (round - pair + np - 1) % (np - 1); }
-          if (p > q) { const int x = p; p = q; q = x; }
-          if (q >= k) continue;
-          double2* bp = B + (long)rows * p;
-          double2* bq = B + (long)rows * q;
-          double a = 0.0, bb = 0.0, gr = 0.0, gi = 0.0;
-          for (int r = lane; r < rows; r += 32) {
-            const double2 x = bp[r], y = bq[r];
-            a += x.x * x.x + x.y * x.y;
-            bb += y.x * y.x + y.y * y.y;
-            gr += x.x * y.x + x.y * y.y;
-            gi += x.x * y.y - x.y * y.x;
-          }
-          a = warp_sum(a); bb = warp_sum(bb); gr = warp_sum(gr); gi = warp_sum(gi);
-          double c, sr, si;
-          float tabs;
-          if (!rotation_params<double>(a, bb, gr, gi, tol, smax, c, sr, si, tabs)) continue;
-          for (int r = lane; r < rows; r += 32) {
-            double2 x = bp[r], y = bq[r];
-            rot(x, y, c, sr, si);
-            bp[r] = x;
-            bq[r] = y;
-          }
-          double2* vp = V + (long)k * p;
-          double2* vq = V + (long)k * q;
-          for (int r = lane; r < k; r += 32) {
-            double2 x = vp[r], y = vq[r];
-            rot(x, y, c, sr, si);
-            vp[r] = x;
-            vq[r] = y;
-          }
-          if (lane == 0) {
-            atomicAdd(&rot_count, 1u);
-            atomicMax(&tmax_bits, __float_as_uint(tabs));
-          }
-        }
-        __syncthreads();
+      const float tol32 = fmaxf(4e-6f, 2.f * sqrtf((float)rows) * Eps<float>::v);
+      cta_sweeps<float>(B32, V32, rows, k, tol32, (float)smax, 20, 0.15f, &rot_count, &tmax_bits);
+      for (int t = tid; t < k * k; t += blockDim.x) V[t] = make_double2((double)V32[t].x, (double)V32[t].y);
+      __syncthreads();
+      // Tm = I - X^H X, then W = X + X Tm / 2 -> V
+      for (int t = tid; t < k * k; t += blockDim.x) {
+        const int i = t % k, j = t / k;
+        double2 acc = make_double2(i == j ? 1.0 : 0.0, 0.0);
+        for (int x = 0; x < k; x++) acc = csub(acc, cmulc(V[x + (long)k * i], V[x + (long)k * j]));
+        Tm[t] = acc;
       }
-      converged = rot_count == 0u || __uint_as_float(tmax_bits) < 1e-8f;
+      __syncthreads();
+      for (int t = tid; t < k * k; t += blockDim.x) {
+        const int i = t % k, j = t / k;
+        double2 acc = make_double2(0.0, 0.0);
+        for (int x = 0; x < k; x++) acc = cadd(acc, zmul(V[i + (long)k * x], Tm[x + (long)k * j]));
+        W[t] = cadd(V[t], cscale(acc, 0.5));
+      }
+      __syncthreads();
+      for (int t = tid; t < k * k; t += blockDim.x) V[t] = W[t];
+      __syncthreads();
+      // B <- B X
+      for (int t = tid; t < rows * k; t += blockDim.x) {
+        const int i = t % rows, j = t / rows;
+        double2 acc = make_double2(0.0, 0.0);
+        for (int x = 0; x < k; x++) acc = cadd(acc, zmul(B[i + (long)rows * x], V[x + (long)k * j]));
+        Tm[t] = acc;
+      }
+      __syncthreads();
+      for (int t = tid; t < rows * k; t += blockDim.x) B[t] = Tm[t];
       __syncthreads();
     }
+    const bool converged = cta_sweeps<double>(B, V, rows, k, tol, smax, BT_MAX_SWEEPS, 1e-8f, &rot_count, &tmax_bits);
     if (!converged && tid == 0) atomicExch(T.status, (int)QR_ENOCONV);
 
     // ---- sigma, descending order (ties by index), truncation on the device
@@ -451,6 +509,7 @@ using namespace qr;
 
 struct qr_batch {
   int device = 0;
+  int precision = QR_FP64;
   std::vector<BReq> reqs;
   bool ran = false;
   int warps = 0, layers = 0, launches = 0, tuned_from_cache = 0;
@@ -465,7 +524,8 @@ namespace {
 int autotune(qr_batch* bt, cudaStream_t s, int chi, int slots, double2* ws) {
   cudaDeviceProp prop;
   QR_CUDA(cudaGetDeviceProperties(&prop, bt->device));
-  std::string key = std::string(prop.name).substr(0, 40) + "/chi" + std::to_string(chi);
+  const bool mixed = (bt->precision & QR_MIXED) != 0;
+  std::string key = std::string(prop.name).substr(0, 40) + "/chi" + std::to_string(chi) + (mixed ? "/mixed" : "/fp64");
   for (char& ch : key)
     if (ch == ' ') ch = '_';
   {
@@ -517,10 +577,11 @@ int autotune(qr_batch* bt, cudaStream_t s, int chi, int slots, double2* ws) {
   int bw = 8;
   bt->tune_candidates_ms.clear();
   for (int w : cand) {
-    batch_gate_k<<<ntask, 32 * w, 0, s>>>(dt, ntask, ws, 1);  // warm-up
+    auto kern = mixed ? batch_gate_k<true> : batch_gate_k<false>;
+    kern<<<ntask, 32 * w, 0, s>>>(dt, ntask, ws, 1);  // warm-up
     count_launch();
     QR_CUDA(cudaEventRecord(e0, s));
-    batch_gate_k<<<ntask, 32 * w, 0, s>>>(dt, ntask, ws, 1);
+    kern<<<ntask, 32 * w, 0, s>>>(dt, ntask, ws, 1);
     count_launch();
     QR_CUDA(cudaEventRecord(e1, s));
     QR_CUDA(cudaEventSynchronize(e1));
@@ -552,6 +613,14 @@ int qr_batch_create(int device, qr_batch** out) {
   qr_batch* b = new qr_batch();
   b->device = device;
   *out = b;
+  return QR_OK;
+}
+
+int qr_batch_set_precision(qr_batch* b, int mode) {
+  if (!b) return fail(QR_EINVAL, "null batch");
+  if (b->ran) return fail(QR_EINVAL, "the batch has already run");
+  if (mode < 0 || mode > 3) return fail(QR_EINVAL, "bad precision");
+  b->precision = mode;
   return QR_OK;
 }
 
@@ -768,7 +837,8 @@ int qr_batch_run(qr_batch* bt, double* ms) {
 
   double2* ws = reinterpret_cast<double2*>(base + o_ws);
   QR_TRY(autotune(bt, s, std::min(maxchi, BT_MAXCHI), slots, ws));
-  QR_TRY(blocks_per_sm((const void*)batch_gate_k, 32 * bt->warps, 0, &per_sm));
+  auto gate_kernel = (bt->precision & QR_MIXED) ? batch_gate_k<true> : batch_gate_k<false>;
+  QR_TRY(blocks_per_sm((const void*)gate_kernel, 32 * bt->warps, 0, &per_sm));
   const int grid_cap = std::min(slots, std::max(1, per_sm) * sms);
 
   // ---- one CUDA graph: init, every layer, the expectation sweep
@@ -783,7 +853,7 @@ int qr_batch_run(qr_batch* bt, double* ms) {
   for (int L = 0; L < nlayers; L++) {
     const int nt = (int)(layer_start[L + 1] - layer_start[L]);
     if (nt == 0) continue;
-    batch_gate_k<<<std::min(nt, grid_cap), 32 * bt->warps, 0, s>>>(dtasks + layer_start[L], nt, ws, 0);
+    gate_kernel<<<std::min(nt, grid_cap), 32 * bt->warps, 0, s>>>(dtasks + layer_start[L], nt, ws, 0);
     launches++;
   }
   if (!obs.empty()) {

@@ -4,8 +4,8 @@
 //   C[b] = op(A[b]) * op(B[b])        (assignment; FP64 complex in and out)
 //
 // Two passes:
-//  1. split (memory-bound): every FP64 operand element x is split into three BF16 slices
-//     x = h + m + l (about 24 significant bits) and the complex product is real-ified,
+//  1. split (memory-bound): every FP64 operand element x is rounded to FP32 and split into three
+//     BF16 slices x = h + m + l (the 24 bits of fl32(x)), and the complex product is real-ified,
 //         [Cr; Ci] = [[Ar, -Ai], [Ai, Ar]] [Br; Bi],
 //     so one real GEMM with doubled M and K covers it.  The slices are written once, K-major
 //     (K contiguous), as bf16 planes [batch][slice][row][k'] with k' in [0, 2 Kh): the first Kh
@@ -145,16 +145,39 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
 }
 
 // ---- pass 1: BF16 slices of the real-ified operands --------------------------------------------
-__device__ __forceinline__ void split3(double x, __nv_bfloat16& h, __nv_bfloat16& m, __nv_bfloat16& l) {
-  h = __double2bfloat16(x);
-  const double r1 = x - (double)__bfloat162float(h);
-  m = __double2bfloat16(r1);
-  const double r2 = r1 - (double)__bfloat162float(m);
-  l = __double2bfloat16(r2);
+// x is rounded once to FP32 (the only FP64-pipe operation: this part's FP64 rate is 1/64 of FP32)
+// and split exactly in FP32: h = bf16(x), m = bf16(x - h), l = bf16(x - h - m); h + m + l carries
+// the 24 bits of fl32(x).  Two consecutive k of a row are handled together, so every store is a
+// 4-byte bf16 pair.
+struct Slices2 {
+  __nv_bfloat162 h, m, l;
+};
+__device__ __forceinline__ Slices2 split3x2(double x0, double x1) {
+  const float f0 = __double2float_rn(x0), f1 = __double2float_rn(x1);
+  Slices2 r;
+  r.h = __floats2bfloat162_rn(f0, f1);
+  const float2 hf = __bfloat1622float2(r.h);
+  const float a0 = __fsub_rn(f0, hf.x), a1 = __fsub_rn(f1, hf.y);
+  r.m = __floats2bfloat162_rn(a0, a1);
+  const float2 mf = __bfloat1622float2(r.m);
+  r.l = __floats2bfloat162_rn(__fsub_rn(a0, mf.x), __fsub_rn(a1, mf.y));
+  return r;
+}
+__device__ __forceinline__ Slices2 neg(Slices2 v) {
+  v.h = __hneg2(v.h);
+  v.m = __hneg2(v.m);
+  v.l = __hneg2(v.l);
+  return v;
+}
+// the three slices of a bf16 pair at element offset e of plane 0 (planes `plane` elements apart)
+__device__ __forceinline__ void put3(__nv_bfloat16* o, long plane, long e, const Slices2& v) {
+  *reinterpret_cast<__nv_bfloat162*>(o + e) = v.h;
+  *reinterpret_cast<__nv_bfloat162*>(o + plane + e) = v.m;
+  *reinterpret_cast<__nv_bfloat162*>(o + 2 * plane + e) = v.l;
 }
 
-// A side: element (i, k) of op(A) (M x K) of batch b goes to the four real-ified positions of
-// its 128-row tile.  One thread per (k, i) pair, k fastest.
+// A side: elements (i, k), (i, k + 1) of op(A) (M x K) of batch b go to the four real-ified
+// positions of their 128-row tile.  One thread per (k pair, i), k fastest.
 template <int OPA>
 __global__ void split_a_k(const double2* __restrict__ A, long lda, long sA, int M, int K, int Mp, int Kh,
                           __nv_bfloat16* __restrict__ out) {
@@ -163,29 +186,30 @@ __global__ void split_a_k(const double2* __restrict__ A, long lda, long sA, int 
   const long plane = rows * Kp;
   __nv_bfloat16* o = out + (long)b * 3 * plane;
   A += (long)b * sA;
-  const long total = (long)Mp * Kh;
+  const int Kh2 = Kh / 2;
+  const long total = (long)Mp * Kh2;
   for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
-    const int k = (int)(t % Kh), i = (int)(t / Kh);
-    double ar = 0.0, ai = 0.0;
-    if (i < M && k < K) {
-      const double2 v = (OPA == OP_N || OPA == OP_R) ? A[i + (long)k * lda] : A[k + (long)i * lda];
-      ar = v.x;
-      ai = (OPA == OP_C || OPA == OP_R) ? -v.y : v.y;
+    const int k = 2 * (int)(t % Kh2), i = (int)(t / Kh2);
+    double ar[2] = {0.0, 0.0}, ai[2] = {0.0, 0.0};
+#pragma unroll
+    for (int u = 0; u < 2; u++) {
+      if (i < M && k + u < K) {
+        const double2 v = (OPA == OP_N || OPA == OP_R) ? A[i + (long)(k + u) * lda] : A[k + u + (long)i * lda];
+        ar[u] = v.x;
+        ai[u] = (OPA == OP_C || OPA == OP_R) ? -v.y : v.y;
+      }
     }
     const long rre = (long)(i / 64) * 128 + (i % 64), rim = rre + 64;
-    __nv_bfloat16 h, m, l;
-    split3(ar, h, m, l);  // Re row, real block; Im row, imaginary block
-    o[rre * Kp + k] = h; o[plane + rre * Kp + k] = m; o[2 * plane + rre * Kp + k] = l;
-    o[rim * Kp + Kh + k] = h; o[plane + rim * Kp + Kh + k] = m; o[2 * plane + rim * Kp + Kh + k] = l;
-    split3(-ai, h, m, l);  // Re row, imaginary block
-    o[rre * Kp + Kh + k] = h; o[plane + rre * Kp + Kh + k] = m; o[2 * plane + rre * Kp + Kh + k] = l;
-    split3(ai, h, m, l);  // Im row, real block
-    o[rim * Kp + k] = h; o[plane + rim * Kp + k] = m; o[2 * plane + rim * Kp + k] = l;
+    const Slices2 re = split3x2(ar[0], ar[1]), im = split3x2(ai[0], ai[1]);
+    put3(o, plane, rre * Kp + k, re);            // Re row, real block:  Ar
+    put3(o, plane, rre * Kp + Kh + k, neg(im));  // Re row, imag block: -Ai
+    put3(o, plane, rim * Kp + k, im);            // Im row, real block:  Ai
+    put3(o, plane, rim * Kp + Kh + k, re);       // Im row, imag block:  Ar
   }
 }
 
-// B side: element (k, n) of op(B) (K x N) goes to row n, columns k (real part) and Kh + k
-// (imaginary part).
+// B side: elements (k, n), (k + 1, n) of op(B) (K x N) go to row n, columns k (real parts) and
+// Kh + k (imaginary parts).
 template <int OPB>
 __global__ void split_b_k(const double2* __restrict__ B, long ldb, long sB, int K, int N, int Np, int Kh,
                           __nv_bfloat16* __restrict__ out) {
@@ -194,20 +218,21 @@ __global__ void split_b_k(const double2* __restrict__ B, long ldb, long sB, int 
   const long plane = (long)Np * Kp;
   __nv_bfloat16* o = out + (long)b * 3 * plane;
   B += (long)b * sB;
-  const long total = (long)Np * Kh;
+  const int Kh2 = Kh / 2;
+  const long total = (long)Np * Kh2;
   for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
-    const int k = (int)(t % Kh), n = (int)(t / Kh);
-    double br = 0.0, bi = 0.0;
-    if (n < N && k < K) {
-      const double2 v = (OPB == OP_N || OPB == OP_R) ? B[k + (long)n * ldb] : B[n + (long)k * ldb];
-      br = v.x;
-      bi = (OPB == OP_C || OPB == OP_R) ? -v.y : v.y;
+    const int k = 2 * (int)(t % Kh2), n = (int)(t / Kh2);
+    double br[2] = {0.0, 0.0}, bi[2] = {0.0, 0.0};
+#pragma unroll
+    for (int u = 0; u < 2; u++) {
+      if (n < N && k + u < K) {
+        const double2 v = (OPB == OP_N || OPB == OP_R) ? B[k + u + (long)n * ldb] : B[n + (long)(k + u) * ldb];
+        br[u] = v.x;
+        bi[u] = (OPB == OP_C || OPB == OP_R) ? -v.y : v.y;
+      }
     }
-    __nv_bfloat16 h, m, l;
-    split3(br, h, m, l);
-    o[(long)n * Kp + k] = h; o[plane + (long)n * Kp + k] = m; o[2 * plane + (long)n * Kp + k] = l;
-    split3(bi, h, m, l);
-    o[(long)n * Kp + Kh + k] = h; o[plane + (long)n * Kp + Kh + k] = m; o[2 * plane + (long)n * Kp + Kh + k] = l;
+    put3(o, plane, (long)n * Kp + k, split3x2(br[0], br[1]));
+    put3(o, plane, (long)n * Kp + Kh + k, split3x2(bi[0], bi[1]));
   }
 }
 
@@ -436,8 +461,8 @@ int zgemm_tc(cudaStream_t s, int opA, int opB, int M, int N, int K, const double
   const double by = 16.0 * ((double)M * K + (double)K * N + (double)M * N) * batch;
   int pr = prof_begin(s, PK_ZGEMM_SPLIT, fl, by);
   {
-    const long ta = (long)Mp * Kh;
-    dim3 g((unsigned)std::min<long>((ta + 255) / 256, 2048), 1, batch);
+    const long ta = (long)Mp * (Kh / 2);
+    dim3 g((unsigned)std::min<long>((ta + 255) / 256, 152 * 16), 1, batch);
     switch (opA) {
       case OP_N: split_a_k<OP_N><<<g, 256, 0, s>>>(A, lda, sA, M, K, Mp, Kh, as); break;
       case OP_T: split_a_k<OP_T><<<g, 256, 0, s>>>(A, lda, sA, M, K, Mp, Kh, as); break;
@@ -446,8 +471,8 @@ int zgemm_tc(cudaStream_t s, int opA, int opB, int M, int N, int K, const double
       default: return fail(QR_EINVAL, "zgemm_tc: bad opA");
     }
     QR_CHECK_LAUNCH("split_a_k");
-    const long tb = (long)Np * Kh;
-    dim3 gb((unsigned)std::min<long>((tb + 255) / 256, 2048), 1, bshared ? 1 : batch);
+    const long tb = (long)Np * (Kh / 2);
+    dim3 gb((unsigned)std::min<long>((tb + 255) / 256, 152 * 16), 1, bshared ? 1 : batch);
     switch (opB) {
       case OP_N: split_b_k<OP_N><<<gb, 256, 0, s>>>(B, ldb, sB, K, N, Np, Kh, bs); break;
       case OP_T: split_b_k<OP_T><<<gb, 256, 0, s>>>(B, ldb, sB, K, N, Np, Kh, bs); break;

@@ -11,13 +11,9 @@ int zgemm(cudaStream_t s, int opA, int opB, int M, int N, int K, double2 alpha,
           const double2* A, long lda, long sA, const double2* B, long ldb, long sB,
           double2 beta, double2* C, long ldc, long sC, int batch, const double* dk);
 
-// ---- gemm_split.cu: C = op(A) op(B) on the BF16 tensor cores, 3-way BF16 split, FP32 accumulate
-int zgemm_split(cudaStream_t s, int opA, int opB, int M, int N, int K, const double2* A, long lda, long sA,
-                const double2* B, long ldb, long sB, double2* C, long ldc, long sC, int batch);
-
-// ---- gemm_tc.cu: the same product on the tcgen05 tensor cores (TMA-staged BF16 slices, TMEM
-// accumulators).  ws: device workspace of zgemm_tc_workspace(M, N, K, batch, sB == 0) bytes;
-// err: device flag set to 1 if a CTA's bounded wait gave up (then C is not valid).
+// ---- gemm_tc.cu: C = op(A) op(B) on the tcgen05 tensor cores: operands rounded to FP32 and split
+// into three BF16 slices, six slice products, FP32 accumulation in TMEM, TMA-staged tiles.
+// ws: device workspace of zgemm_tc_workspace(M, N, K, batch, sB == 0) bytes; err: device flag set to 1 if a CTA's bounded wait gave up (then C is not valid).
 size_t zgemm_tc_workspace(int M, int N, int K, int batch, bool bshared);
 int zgemm_tc(cudaStream_t s, int opA, int opB, int M, int N, int K, const double2* A, long lda, long sA,
              const double2* B, long ldb, long sB, double2* C, long ldc, long sC, int batch, void* ws,

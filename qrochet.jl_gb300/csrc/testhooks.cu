@@ -64,38 +64,6 @@ int qr_test_zgemm(int opA, int opB, int M, int N, int K, const double* alpha, co
   return QR_OK;
 }
 
-// C = op(A) op(B) with the split-precision tensor-core kernel (mixed-precision contractions).
-int qr_test_zgemm_split(int opA, int opB, int M, int N, int K, const double* A, long lda, const double* B, long ldb,
-                        double* C, long ldc, int iters, double* ms_per_iter) {
-  if (M <= 0 || N <= 0 || K < 0 || iters < 1) return fail(QR_EINVAL, "bad gemm shape");
-  long ca = (opA == OP_N || opA == OP_R) ? K : M;
-  long cb = (opB == OP_N || opB == OP_R) ? N : K;
-  Dev dA, dB, dC;
-  QR_TRY(up(dA, A, (size_t)lda * ca));
-  QR_TRY(up(dB, B, (size_t)ldb * cb));
-  QR_TRY(up(dC, nullptr, (size_t)ldc * N));
-  cudaEvent_t e0, e1;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
-  float total = 0;
-  int rc = QR_OK;
-  for (int it = 0; it < iters && rc == QR_OK; it++) {
-    cudaEventRecord(e0);
-    rc = zgemm_split(0, opA, opB, M, N, K, (double2*)dA.p, lda, 0, (double2*)dB.p, ldb, 0, (double2*)dC.p, ldc, 0, 1);
-    cudaEventRecord(e1);
-    cudaEventSynchronize(e1);
-    float ms = 0;
-    cudaEventElapsedTime(&ms, e0, e1);
-    total += ms;
-  }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  QR_TRY(rc);
-  QR_CUDA(cudaMemcpy(C, dC.p, sizeof(double2) * ldc * N, cudaMemcpyDeviceToHost));
-  if (ms_per_iter) *ms_per_iter = total / iters;
-  return QR_OK;
-}
-
 // C[b] = op(A[b]) op(B[b]) with the tcgen05 split-precision kernel (gemm_tc.cu); A and B hold
 // `batch` matrices at strides sA and sB (sB = 0: one B shared by the batch), C at stride ldc * N.
 int qr_test_zgemm_tc(int opA, int opB, int M, int N, int K, int batch, const double* A, long lda, long sA,

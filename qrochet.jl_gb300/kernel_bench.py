@@ -3,7 +3,6 @@
     python qrochet.jl_gb300/kernel_bench.py zgemm M N K [iters]
     python qrochet.jl_gb300/kernel_bench.py svd fp64|mixed N [M]
     python qrochet.jl_gb300/kernel_bench.py qr M N
-    python qrochet.jl_gb300/kernel_bench.py zgemm_split M N K [iters]
     python qrochet.jl_gb300/kernel_bench.py zgemm_tc M N K [iters] [batch]
     python qrochet.jl_gb300/kernel_bench.py upload CHI
 
@@ -61,16 +60,6 @@ def main(argv):
         ms = C.c_double()
         _lib.check(L.qr_test_qr(m, n, p(A), p(Q), p(Rm), C.byref(ms)))
         out = {"op": "qr", "m": m, "n": n, "ms": ms.value}
-    elif what == "zgemm_split":
-        M, N, K = (int(x) for x in argv[1:4])
-        iters = int(argv[4]) if len(argv) > 4 else 3
-        A = np.asfortranarray(R.complex_gaussian(g, (M, K)))
-        B = np.asfortranarray(R.complex_gaussian(g, (K, N)))
-        Cm = np.zeros((M, N), dtype=np.complex128, order="F")
-        ms = C.c_double()
-        _lib.check(L.qr_test_zgemm_split(0, 0, M, N, K, p(A), M, p(B), K, p(Cm), M, iters, C.byref(ms)))
-        fl = 8.0 * M * N * K
-        out = {"op": "zgemm_split", "M": M, "N": N, "K": K, "ms": ms.value, "tflops_complex_equiv": fl / ms.value / 1e9}
     elif what == "zgemm_tc":
         # the tcgen05 split kernel with the environment sweep's operand shapes: op(A) = A^T with K
         # contiguous, B shared by the batch

@@ -103,6 +103,7 @@ SIGNATURES = {
     "qr_server_stats": [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), _PI, C.POINTER(C.c_uint64), _PI],
     "qr_batch_create": [_I, C.POINTER(_P)],
     "qr_batch_free": [_P],
+    "qr_batch_set_precision": [_P, _I],
     "qr_batch_add": [_P, _I, _I, _D, _I, _PI, _PD, _I, _PI, _PI, _PI, _PI],
     "qr_batch_plan": [_P, _I, _PI, _PI],
     "qr_batch_run": [_P, _PD],
@@ -112,7 +113,6 @@ SIGNATURES = {
     "qr_batch_info": [_P, _PI, _PI, _PI, _PI, _PI, _PD, _PD],
     "qr_svd_noalloc": [_I, _I, _P, C.c_long, _P, C.c_long, _P, _P, C.c_long, _P],
     "qr_test_zgemm": [_I, _I, _I, _I, _I, _PD, _PD, C.c_long, _PD, C.c_long, _PD, _PD, C.c_long, _PD, _I, _PD],
-    "qr_test_zgemm_split": [_I, _I, _I, _I, _I, _PD, C.c_long, _PD, C.c_long, _PD, C.c_long, _I, _PD],
     "qr_test_zgemm_tc": [_I, _I, _I, _I, _I, _I, _PD, C.c_long, C.c_long, _PD, C.c_long, C.c_long, _PD, C.c_long,
                          _I, _PD],
     "qr_test_zgemm_df": [_I, _I, _I, _I, _I, _PD, C.c_long, _PD, C.c_long, _PD, _PD, C.c_long, _I, _PD],

@@ -13,9 +13,10 @@ from .serve import PAULI_CODE, Request
 
 
 class Batch:
-    def __init__(self, device=0):
+    def __init__(self, device=0, precision="fp64"):
         self._h = C.c_void_p()
         check(lib().qr_batch_create(device, C.byref(self._h)))
+        check(lib().qr_batch_set_precision(self._h, {"fp64": 0, "mixed": 1}[precision]))
         self._reqs = []
 
     def close(self):

@@ -611,7 +611,7 @@ def probe_peak(kind):
 
 
 PROF_KINDS = {"zgemm_dmma": 0, "jacobi_fp64": 1, "jacobi_fp32": 2, "householder_qr": 3, "env_mix": 4,
-              "zgemm_split_bf16": 5, "jacobi_df": 6,
+              "zgemm_tc_bf16x3": 5, "jacobi_df": 6,
               "zgemm_df": 7}
 
 

@@ -135,47 +135,6 @@ def test_qr_against_lapack():
         assert np.allclose(np.abs(np.diag(Rm)), np.abs(np.diag(np.linalg.qr(A)[1])), rtol=1e-10)
 
 
-def zgemm_split(opA, opB, A, B, M, N):
-    K = OPS[opA](A).shape[1]
-    A = np.asfortranarray(A, dtype=np.complex128)
-    B = np.asfortranarray(B, dtype=np.complex128)
-    out = np.zeros((M, N), dtype=np.complex128, order="F")
-    ms = C.c_double()
-    _lib.check(_lib.lib().qr_test_zgemm_split(opA, opB, M, N, K, _p(A), A.shape[0], _p(B), B.shape[0], _p(out), M,
-                                              1, C.byref(ms)))
-    return out
-
-
-# split-precision contraction: 3-way BF16 split, FP32 accumulation; error bound ~sqrt(K) 2^-24
-SPLIT_TOL = 2e-6
-
-
-@pytest.mark.parametrize("opA", [0, 1, 2, 3])
-@pytest.mark.parametrize("opB", [0, 1, 2, 3])
-def test_zgemm_split_ops(opA, opB):
-    g = R.rng(300 + 4 * opA + opB)
-    M, N, K = 90, 70, 200
-    A0 = R.complex_gaussian(g, (M, K))
-    B0 = R.complex_gaussian(g, (K, N))
-    A = {0: A0, 1: A0.T.copy(), 2: A0.conj().T.copy(), 3: A0.conj()}[opA]
-    B = {0: B0, 1: B0.T.copy(), 2: B0.conj().T.copy(), 3: B0.conj()}[opB]
-    got = zgemm_split(opA, opB, A, B, M, N)
-    ref = A0 @ B0
-    # entries of a random product are ~sqrt(K); compare against the magnitude scale |A||B|
-    scale = np.sqrt(K)
-    assert np.max(np.abs(got - ref)) <= SPLIT_TOL * scale * 4
-
-
-def test_zgemm_split_large_k():
-    g = R.rng(9)
-    A = R.complex_gaussian(g, (256, 2048))
-    B = R.complex_gaussian(g, (2048, 128))
-    got = zgemm_split(0, 0, A, B, 256, 128)
-    ref = A @ B
-    rel = np.linalg.norm(got - ref) / np.linalg.norm(ref)
-    assert rel <= 5e-7, rel
-
-
 def zgemm_df(mode, opA, A, B, M, N, D=None):
     K = OPS[opA](A).shape[1]
     A = np.asfortranarray(A, dtype=np.complex128)
