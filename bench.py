@@ -54,7 +54,7 @@ def parse():
     p.add_argument("--serve", type=int, default=24, help="requests in the serving sample (0: skip)")
     p.add_argument("--serve-sat", type=int, default=64,
                    help="requests in the saturated mixed-precision serving sample (0: skip)")
-    p.add_argument("--serve-full", type=int, default=16,
+    p.add_argument("--serve-full", type=int, default=64,
                    help="requests in the mixed-precision sample over every chi_max class (0: skip)")
     p.add_argument("--mpo-sites", type=int, default=128, help="sites of the MPO environment sweep (0: skip)")
     p.add_argument("--workers", type=int, default=16)
@@ -358,11 +358,31 @@ def run_mpo_env(args, Q):
         e = Q.mpo_expect(psi, H)
         res[prec] = (time.perf_counter() - t0, e)
     (ts, es), (td, ed) = res["mixed+split"], res["fp64"]
+    # canonize! of this chain is 127 QR steps and 127 SVD steps of up to 2048 x 1024 (Chain.jl:469-497);
+    # one of each on a middle site (chi = 1024 on both sides), per precision, on a copy
+    mid = n // 2 + 1
+    canon = {}
+    for prec in ("fp64", "mixed"):
+        c = psi.copy()
+        c.set_precision(prec)
+        c.sync()
+        t0 = time.perf_counter()
+        Q.canonize_site_(c, mid, "left", "qr")
+        c.sync()
+        t1 = time.perf_counter()
+        Q.canonize_site_(c, mid, "left", "svd")
+        c.sync()
+        t2 = time.perf_counter()
+        canon[prec] = {"qr_step_ms": 1e3 * (t1 - t0), "svd_step_ms": 1e3 * (t2 - t1)}
+        del c
     bonds = [1] + [min(chi, 2 ** (i + 1), 2 ** (n - i - 1)) for i in range(n - 1)] + [1]
     wdim = [1] + [5] * (n - 1) + [1]
     flops = sum(8.0 * (wdim[i] * bonds[i] * 2 * bonds[i + 1] * bonds[i] + bonds[i + 1] * bonds[i + 1] * 2 * bonds[i] *
                        wdim[i + 1]) for i in range(n))
     return {"n": n, "chi": chi, "w": 5, "split_ms_per_sweep": 1e3 * ts, "fp64_ms_per_sweep": 1e3 * td,
+            "canonize_site_at_chi1024": canon,
+            "canonize_note": "one canonize_site!(; direction=:left) step of each method on site n/2+1 "
+                             "(a 2048 x 1024 factorisation); canonize! runs 127 of each, most at this size",
             "split_over_fp64": td / ts, "rel_err_split_vs_fp64": abs(es - ed) / abs(ed),
             "energy_fp64": [ed.real, ed.imag], "split_tflops_complex_equiv": flops / ts / 1e12,
             "note": "sites complex Gaussian / sqrt(2 chi_l); bond dims min(1024, 2^i) mirrored; "
