@@ -75,6 +75,10 @@ int dnormalize(cudaStream_t s, double* lam, int len);
 // R: k x n (ld ldr), k = min(m, n).  tau: device workspace of k entries.
 int zqr_thin(cudaStream_t s, double2* A, int m, int n, long lda, double2* Q, long ldq,
              double2* R, long ldr, double2* tau);
+// The same factorisation with one launch per column and no scratch beyond tau (for callers that
+// must not allocate).
+int zqr_thin_steps(cudaStream_t s, double2* A, int m, int n, long lda, double2* Q, long ldq,
+                   double2* R, long ldr, double2* tau);
 
 // ---- svd.cu ------------------------------------------------------------------------------------
 struct SvdWork;  // opaque, grows on demand

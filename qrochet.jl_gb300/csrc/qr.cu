@@ -6,9 +6,18 @@
 // A <- H^H A during the factorisation, Q = H_0 H_1 ... H_{k-1} [I; 0]), so R has a real diagonal
 // like the R that Julia's qr returns.
 //
-// Step j needs the updated column j, so the factorisation is one reflector launch plus one
-// trailing-update launch per column; each trailing column is owned by one CTA.
+// Two schedules of the same arithmetic:
+//  - zqr_thin: the whole factorisation in one cooperative launch.  CTA b owns the columns
+//    c = b (mod grid).  At step j every CTA reads column j (final after step j - 1), forms the
+//    reflector's scalars itself (the same reduction order in every CTA gives the same bits), and
+//    applies H_j^H to its own columns c > j; the owner of column j writes beta and the scaled
+//    reflector into it at the start of step j + 1, once no CTA reads it any more.  One bounded grid
+//    barrier per step.  Q needs no barrier at all: applying H_{k-1} .. H_0 to a column of [I; 0]
+//    touches that column only, so each CTA runs all steps for its own columns in one launch.
+//  - zqr_thin_steps: one reflector launch and one trailing-update launch per column (and one
+//    Q launch per column), no scratch beyond tau; the allocation-free SVD uses it.
 #include "kernels.cuh"
+#include "grid_sync.cuh"
 
 namespace qr {
 
@@ -124,6 +133,118 @@ __global__ void extract_r_k(const double2* A, long lda, int k, int n, double2* R
   }
 }
 
+// zlarfg scalars of x = A[j:m, j] (len = m - j), computed by every CTA alike: returns skip (tau = 0)
+// or beta, tau and scal = 1 / (alpha - beta) through shared memory.
+struct Reflector {
+  double2 tau, scal;
+  double beta;
+  int skip;
+};
+__device__ void reflector_of(const double2* x, int len, double* red, Reflector* out) {
+  double acc = 0.0;
+  for (int t = 1 + threadIdx.x; t < len; t += blockDim.x) acc += x[t].x * x[t].x + x[t].y * x[t].y;
+  const double xnorm2 = block_sum_d(acc, red);
+  if (threadIdx.x == 0) {
+    const double2 alpha = x[0];
+    Reflector r;
+    if (xnorm2 == 0.0 && alpha.y == 0.0) {
+      r.tau = make_double2(0.0, 0.0);
+      r.scal = make_double2(0.0, 0.0);
+      r.beta = alpha.x;
+      r.skip = 1;
+    } else {
+      const double beta = -copysign(sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xnorm2), alpha.x);
+      r.tau = make_double2((beta - alpha.x) / beta, -alpha.y / beta);
+      const double2 den = make_double2(alpha.x - beta, alpha.y);
+      const double dd = den.x * den.x + den.y * den.y;
+      r.scal = make_double2(den.x / dd, -den.y / dd);
+      r.beta = beta;
+      r.skip = 0;
+    }
+    *out = r;
+  }
+  __syncthreads();
+}
+
+// the pivot column j after its step: beta on the diagonal, the reflector scaled below it
+__device__ void store_reflector(double2* x, int len, const Reflector& r) {
+  if (r.skip) return;
+  for (int t = 1 + threadIdx.x; t < len; t += blockDim.x) x[t] = cmul(x[t], r.scal);
+  if (threadIdx.x == 0) x[0] = make_double2(r.beta, 0.0);
+}
+
+__global__ void house_qr_coop_k(double2* A, int m, int n, long lda, double2* tau, unsigned* bar) {
+  __shared__ double red[32];
+  __shared__ Reflector cur;
+  Reflector prev;
+  prev.skip = 1;
+  const int k = m < n ? m : n;
+  for (int j = 0; j < k; j++) {
+    if (j > 0 && (int)((j - 1) % gridDim.x) == (int)blockIdx.x)
+      store_reflector(A + (j - 1) + (long)(j - 1) * lda, m - (j - 1), prev);
+    const double2* x = A + j + (long)j * lda;
+    const int len = m - j;
+    reflector_of(x, len, red, &cur);
+    const Reflector r = cur;
+    if ((int)(j % gridDim.x) == (int)blockIdx.x) {
+      if (threadIdx.x == 0) tau[j] = r.tau;
+      prev = r;
+    }
+    if (!r.skip) {
+      const double2 tc = make_double2(r.tau.x, -r.tau.y);
+      // own columns c > j: the first is the smallest c = blockIdx.x (mod grid) above j
+      int c0 = j + 1 + (int)(((long)blockIdx.x - (j + 1)) % (long)gridDim.x + gridDim.x) % (int)gridDim.x;
+      for (int c = c0; c < n; c += gridDim.x) {
+        double2* col = A + j + (long)c * lda;
+        double2 acc = make_double2(0.0, 0.0);
+        for (int t = threadIdx.x; t < len; t += blockDim.x) {
+          const double2 v = t == 0 ? make_double2(1.0, 0.0) : cmul(x[t], r.scal);
+          acc = cadd(acc, cmulc(v, col[t]));
+        }
+        const double2 w = cmul(tc, block_sum_z(acc, red));
+        for (int t = threadIdx.x; t < len; t += blockDim.x) {
+          const double2 v = t == 0 ? make_double2(1.0, 0.0) : cmul(x[t], r.scal);
+          col[t] = csub(col[t], cmul(v, w));
+        }
+        __syncthreads();
+      }
+    }
+    if (!grid_barrier(bar)) return;
+  }
+  if (k > 0 && (int)((k - 1) % gridDim.x) == (int)blockIdx.x)
+    store_reflector(A + (k - 1) + (long)(k - 1) * lda, m - (k - 1), prev);
+}
+
+// Q (m x k) = H_0 .. H_{k-1} [I; 0]: CTA b forms the columns c = b (mod grid), each from e_c
+// through H_{k-1}, ..., H_0 (H_j touches rows j.. of the columns c >= j only)
+__global__ void house_q_cols_k(double2* Q, int m, int k, long ldq, const double2* V, long ldv, const double2* tau) {
+  __shared__ double red[32];
+  for (int c = blockIdx.x; c < k; c += gridDim.x) {
+    double2* col = Q + (long)c * ldq;
+    for (int t = threadIdx.x; t < m; t += blockDim.x) col[t] = make_double2(t == c ? 1.0 : 0.0, 0.0);
+    __syncthreads();
+    for (int j = c; j >= 0; j--) {
+      const double2 tj = tau[j];
+      if (tj.x == 0.0 && tj.y == 0.0) continue;
+      const double2* v = V + j + (long)j * ldv;
+      const int len = m - j;
+      double2 acc = make_double2(0.0, 0.0);
+      for (int t = threadIdx.x; t < len; t += blockDim.x) {
+        const double2 vr = t == 0 ? make_double2(1.0, 0.0) : v[t];
+        acc = cadd(acc, cmulc(vr, col[j + t]));
+      }
+      const double2 w = cmul(tj, block_sum_z(acc, red));
+      for (int t = threadIdx.x; t < len; t += blockDim.x) {
+        const double2 vr = t == 0 ? make_double2(1.0, 0.0) : v[t];
+        col[j + t] = csub(col[j + t], cmul(vr, w));
+      }
+      __syncthreads();
+    }
+  }
+}
+
+inline int cuda_ok_qr(cudaError_t e) { return e == cudaSuccess ? QR_OK : cuda_fail(e, "Householder QR"); }
+
 inline unsigned cols_grid(int ncols) {
   int g = ncols < 1 ? 1 : ncols;
   return (unsigned)(g > 152 * 8 ? 152 * 8 : g);
@@ -131,8 +252,8 @@ inline unsigned cols_grid(int ncols) {
 
 }  // namespace
 
-int zqr_thin(cudaStream_t s, double2* A, int m, int n, long lda, double2* Q, long ldq, double2* R,
-             long ldr, double2* tau) {
+int zqr_thin_steps(cudaStream_t s, double2* A, int m, int n, long lda, double2* Q, long ldq, double2* R,
+                   long ldr, double2* tau) {
   if (m <= 0 || n <= 0) return QR_OK;
   const int k = m < n ? m : n;
   for (int j = 0; j < k; j++) {
@@ -155,6 +276,49 @@ int zqr_thin(cudaStream_t s, double2* A, int m, int n, long lda, double2* Q, lon
       house_apply_q_k<<<cols_grid(k - j), TPB, 0, s>>>(Q, m, k, ldq, A, lda, j, tau);
       QR_CHECK_LAUNCH("house_apply_q_k");
     }
+  }
+  return QR_OK;
+}
+
+int zqr_thin(cudaStream_t s, double2* A, int m, int n, long lda, double2* Q, long ldq, double2* R,
+             long ldr, double2* tau) {
+  if (m <= 0 || n <= 0) return QR_OK;
+  const int k = m < n ? m : n;
+  int sms = 0, per_sm = 0;
+  QR_TRY(device_sm_count(&sms));
+  QR_TRY(blocks_per_sm((const void*)house_qr_coop_k, TPB, 0, &per_sm));
+  if (per_sm < 1) return zqr_thin_steps(s, A, m, n, lda, Q, ldq, R, ldr, tau);
+  // one CTA per trailing column while they last; more CTAs only add barrier arrivals
+  int grid = std::min(per_sm * sms, std::max(1, n - 1));
+  unsigned* bar = nullptr;
+  cudaError_t e = cudaMallocAsync((void**)&bar, 4 * sizeof(unsigned), s);
+  if (e != cudaSuccess) return fail(QR_ENOMEM, std::string("QR barrier: ") + cudaGetErrorString(e));
+  int rc = cuda_ok_qr(cudaMemsetAsync(bar, 0, 4 * sizeof(unsigned), s));
+  if (!rc) {
+    double2* Ap = A;
+    int mm = m, nn = n;
+    long ld = lda;
+    double2* tp = tau;
+    unsigned* bp = bar;
+    void* args[] = {&Ap, &mm, &nn, &ld, &tp, &bp};
+    rc = cuda_ok_qr(cudaLaunchCooperativeKernel((const void*)house_qr_coop_k, dim3(grid), dim3(TPB), args, 0, s));
+    count_launch();
+  }
+  unsigned hb[3] = {0, 0, 0};
+  if (!rc) rc = cuda_ok_qr(cudaMemcpyAsync(hb, bar, 3 * sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  if (!rc) rc = cuda_ok_qr(cudaStreamSynchronize(s));
+  cudaFreeAsync(bar, s);
+  if (rc) return rc;
+  if (hb[2]) return fail(QR_ECUDA, "Householder QR: a grid barrier timed out");
+  if (R) {
+    long total = (long)k * n;
+    unsigned g = (unsigned)((total + TPB - 1) / TPB);
+    extract_r_k<<<g > 4864 ? 4864 : g, TPB, 0, s>>>(A, lda, k, n, R, ldr);
+    QR_CHECK_LAUNCH("extract_r_k");
+  }
+  if (Q) {
+    house_q_cols_k<<<cols_grid(k), TPB, 0, s>>>(Q, m, k, ldq, A, lda, tau);
+    QR_CHECK_LAUNCH("house_q_cols_k");
   }
   return QR_OK;
 }

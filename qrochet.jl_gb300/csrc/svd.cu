@@ -30,6 +30,7 @@
 #include "df.cuh"
 #include "prof.cuh"
 #include "jacobi_rot.cuh"
+#include "grid_sync.cuh"
 
 namespace qr {
 
@@ -179,36 +180,6 @@ __device__ __forceinline__ void jacobi_pair(cplx_t<T>* __restrict__ B, long ldb,
     atomicAdd(count, 1u);
     atomicMax(count + 1, __float_as_uint((float)fabs(t)));  // largest rotation tangent of the sweep
   }
-}
-
-// Grid-wide barrier for a cooperative launch (all CTAs resident).  The wait is bounded: after
-// ~2^22 polls (about a second) the CTA records a timeout in bar[2] and proceeds; every CTA checks
-// bar[2] after the barrier and leaves the sweep, so the kernel always returns.
-__device__ __forceinline__ bool grid_barrier(unsigned* bar) {
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    volatile unsigned* vb = bar;
-    const unsigned gen = vb[1];
-    __threadfence();
-    const unsigned arrived = atomicAdd(&bar[0], 1u) + 1u;
-    if (arrived == gridDim.x) {
-      atomicExch(&bar[0], 0u);
-      __threadfence();
-      atomicAdd(&bar[1], 1u);
-    } else {
-      unsigned polls = 0;
-      while (vb[1] == gen) {
-        if (++polls > (1u << 22)) {
-          atomicExch(&bar[2], 1u);
-          break;
-        }
-        __nanosleep(200);
-      }
-    }
-    __threadfence();
-  }
-  __syncthreads();
-  return ((volatile unsigned*)bar)[2] == 0u;
 }
 
 // One full sweep (np-1 rounds) in one cooperative launch: CTAs stride over the round's pairs.
@@ -2086,7 +2057,7 @@ extern "C" int qr_svd_noalloc(int m, int n, const double* A, long lda, double* U
   const bool pre = k > 32;
   int jr = rows;  // rows of the matrix the sweeps rotate
   if (pre) {
-    QR_TRY(zqr_thin(s, B, rows, k, rows, L, rows, V, k, tau));
+    QR_TRY(zqr_thin_steps(s, B, rows, k, rows, L, rows, V, k, tau));
     QR_TRY(ztranspose(s, V, k, k, k, B, k, 1));
     jr = k;
     QR_TRY(host_max_norm(B, k, k, &smax));
@@ -2143,7 +2114,7 @@ extern "C" int qr_svd_noalloc(int m, int n, const double* A, long lda, double* U
   auto reorthonormalize_noalloc = [&](double2* F, long ldf, int r, double2* X) -> int {
     QR_CUDA(cudaMemcpy2DAsync(X, sizeof(double2) * r, F, sizeof(double2) * ldf, sizeof(double2) * r, k,
                               cudaMemcpyDeviceToDevice, s));
-    QR_TRY(zqr_thin(s, X, r, k, r, F, ldf, V, k, tau));
+    QR_TRY(zqr_thin_steps(s, X, r, k, r, F, ldf, V, k, tau));
     phase_fix_k<<<gs((long)r * k), TPB, 0, s>>>(F, ldf, r, k, V, k);
     QR_CHECK_LAUNCH("phase_fix_k");
     return QR_OK;

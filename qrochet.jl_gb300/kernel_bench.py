@@ -4,6 +4,7 @@
     python qrochet.jl_gb300/kernel_bench.py svd fp64|mixed N [M]
     python qrochet.jl_gb300/kernel_bench.py qr M N
     python qrochet.jl_gb300/kernel_bench.py zgemm_tc M N K [iters] [batch]
+    python qrochet.jl_gb300/kernel_bench.py batch CHI_MAX REQUESTS fp64|mixed
     python qrochet.jl_gb300/kernel_bench.py upload CHI
 
 Inputs are seeded complex Gaussians; prints one JSON line with the event-timed duration, the
@@ -78,6 +79,22 @@ def main(argv):
         out = {"op": "zgemm_tc", "M": M, "N": N, "K": K, "batch": batch, "ms": ms.value,
                "tflops_complex_equiv": fl / ms.value / 1e9, "bf16_tflops_executed": 6.0 * fl / ms.value / 1e9,
                "rel_err": float(np.linalg.norm(got - ref) / np.linalg.norm(ref))}
+    elif what == "batch":
+        # the batched engine on requests of the batched distribution with one chi_max class
+        import time
+        from qrochet import serve as S
+        from qrochet.batch import Batch
+        chi, nreq, prec = int(argv[1]), int(argv[2]), argv[3]
+        e = int(round(np.log2(chi)))
+        reqs = S.batched_requests(nreq, seed=4, chi_log2=(e, e), nobs=1)
+        with Batch(precision=prec) as b:
+            for r in reqs:
+                b.add(r)
+            t0 = time.perf_counter()
+            b.run()
+            dt = time.perf_counter() - t0
+            out = {"op": "batch", "chi_max": chi, "requests": nreq, "precision": prec,
+                   "gates": sum(len(r.gates) for r in reqs), "wall_s": dt, **b.info()}
     elif what == "upload":
         # a 3-site chain whose middle site is (2, chi, chi) in the reference's (o, l, r) order: the
         # upload permutes it to the device layout (l, o, r)

@@ -122,7 +122,8 @@ def test_svd_against_lapack(mode, case):
 
 def test_qr_against_lapack():
     g = R.rng(5)
-    for m, n in [(64, 32), (32, 64), (50, 50), (2, 1)]:
+    # up to the canonize_site! factorisation of a chi = 1024 site (2048 x 1024), wide and odd shapes
+    for m, n in [(64, 32), (32, 64), (50, 50), (2, 1), (1, 3), (257, 300), (2048, 1024)]:
         A = np.asfortranarray(R.complex_gaussian(g, (m, n)))
         k = min(m, n)
         Q = np.empty((m, k), dtype=np.complex128, order="F")
