@@ -152,6 +152,10 @@ struct qr_mpo {
   int n = 0, d = 0;
   std::vector<int> bd;
   std::vector<double2*> site;  // (wl, o, i, wr), wl fastest
+  // host copies of the site tensors, read back once for the sparse mixing tables (see env_sweep)
+  // and dropped by every upload
+  mutable std::vector<std::vector<double2>> host_w;
+  mutable bool host_ok = false;
   int wl(int i) const { return i == 0 ? 1 : bd[i - 1]; }
   int wr(int i) const { return i == n - 1 ? 1 : bd[i]; }
 };
@@ -552,9 +556,62 @@ __global__ void mix_k(const double2* __restrict__ X, double2* __restrict__ Y, co
   }
 }
 
+// The nonzero entries of one site's W, grouped by output (o, w'): MPOs of local Hamiltonians and
+// products of few-site observables are sparse (the XXZ MPO has 12 nonzeros among its 100 entries),
+// so the mixing step does only their multiply-adds.  Passed to the kernel by value.
+constexpr int MIX_MAX_TERMS = 96, MIX_MAX_OUT = 16;
+struct MixTable {
+  int nout;
+  int start[MIX_MAX_OUT + 1];
+  short w[MIX_MAX_TERMS], i[MIX_MAX_TERMS];
+  double2 v[MIX_MAX_TERMS];
+};
+
+// false when W (host, (wl, o, i, wr) wl fastest) has too many outputs or nonzeros for a table
+bool build_mix_table(const double2* W, int wl, int d, int wr, MixTable* t) {
+  if (d * wr > MIX_MAX_OUT) return false;
+  int nt = 0;
+  t->nout = d * wr;
+  for (int w2 = 0; w2 < wr; w2++)
+    for (int o = 0; o < d; o++) {
+      const int out = o + d * w2;
+      t->start[out] = nt;
+      for (int i = 0; i < d; i++)
+        for (int w = 0; w < wl; w++) {
+          const double2 v = W[w + wl * (o + d * (i + d * w2))];
+          if (v.x == 0.0 && v.y == 0.0) continue;
+          if (nt == MIX_MAX_TERMS) return false;
+          t->w[nt] = (short)w;
+          t->i[nt] = (short)i;
+          t->v[nt] = v;
+          nt++;
+        }
+    }
+  t->start[d * wr] = nt;
+  return true;
+}
+
+// mix_k over the nonzeros only: Y[b,o,w',a'] = sum over the table's (w, i) of W X[w,b,i,a']
+__global__ void mix_sparse_k(const double2* __restrict__ X, double2* __restrict__ Y, const MixTable tab, int wl,
+                             int d, int cb, int ca2) {
+  const long pairs = (long)cb * ca2;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < pairs; t += (long)gridDim.x * blockDim.x) {
+    const long b = t % cb, a2 = t / cb;
+    for (int out = 0; out < tab.nout; out++) {
+      double2 acc = make_double2(0, 0);
+      for (int e = tab.start[out]; e < tab.start[out + 1]; e++)
+        acc = cadd(acc, cmul(tab.v[e], X[tab.w[e] + wl * (b + (long)cb * (tab.i[e] + (long)d * a2))]));
+      const int o = out % d, w2 = out / d;
+      Y[b + (long)cb * (o + (long)d * (w2 + (long)(tab.nout / d) * a2))] = acc;
+    }
+  }
+}
+
 struct EnvOps {
   std::vector<const double2*> W;  // per site, device (wl,o,i,wr) or nullptr for identity
   std::vector<int> wl, wr;
+  std::vector<MixTable> tab;      // per site, used where has_tab[i]
+  std::vector<char> has_tab;
 };
 
 // With QR_SPLIT_CONTRACT the two contractions of every site step run on the tcgen05 tensor cores
@@ -758,7 +815,10 @@ int env_sweep(const qr_chain* a, const qr_chain* b, const EnvOps* ops, cudaStrea
     if (W) {
       long pairs = (long)cb * ca2;
       unsigned g = (unsigned)((pairs + 255) / 256);
-      mix_k<<<g > 4864 ? 4864 : g, 256, sizeof(double2) * wl * d * d * wr, s>>>(X, Y, W, wl, wr, d, cb, ca2);
+      if (!ops->has_tab.empty() && ops->has_tab[i])
+        mix_sparse_k<<<g > 4864 ? 4864 : g, 256, 0, s>>>(X, Y, ops->tab[i], wl, d, cb, ca2);
+      else
+        mix_k<<<g > 4864 ? 4864 : g, 256, sizeof(double2) * wl * d * d * wr, s>>>(X, Y, W, wl, wr, d, cb, ca2);
       count_launch();
       Yp = Y;
     }
@@ -1467,6 +1527,14 @@ int qr_expect(const qr_chain* h, int nobs, const int* first, const int* nlanes, 
   ops.W.assign(n, nullptr);
   ops.wl = wl;
   ops.wr = wr;
+  ops.tab.resize(n);
+  ops.has_tab.assign(n, 0);
+  for (int i = 0; i < n; i++) {
+    if (!touched[i]) continue;
+    std::vector<double2> wh(W[i].size());
+    for (size_t e = 0; e < wh.size(); e++) wh[e] = make_double2(W[i][e].real(), W[i][e].imag());
+    ops.has_tab[i] = build_mix_table(wh.data(), wl[i], d, wr[i], &ops.tab[i]) ? 1 : 0;
+  }
   std::vector<double2*> dev(n, nullptr);
   int rc = QR_OK;
   for (int i = 0; i < n && !rc; i++) {
@@ -1508,6 +1576,7 @@ int qr_mpo_free(qr_mpo* w) {
 
 int qr_mpo_upload_site(qr_mpo* w, int site, const double* host, const char* order) {
   if (!w || site < 0 || site >= w->n || !host) return fail(QR_EINVAL, "bad MPO site");
+  w->host_ok = false;
   if (!is_perm(order ? order : "", "oilr")) return fail(QR_EINVAL, "order must be a permutation of (o, i, l, r)");
   std::string ho = filtered(order, site == 0, site == w->n - 1);
   long idims[4] = {w->wl(site), w->d, w->d, w->wr(site)};
@@ -1557,6 +1626,19 @@ int qr_mpo_expect(const qr_chain* h, const qr_mpo* w, double* out) {
   ops.wl.resize(h->n);
   ops.wr.resize(h->n);
   for (int i = 0; i < h->n; i++) { ops.wl[i] = w->wl(i); ops.wr[i] = w->wr(i); }
+  if (!w->host_ok) {  // one read-back of the (small) site tensors, kept until the next upload
+    w->host_w.resize(w->n);
+    for (int i = 0; i < w->n; i++) {
+      w->host_w[i].resize((size_t)w->wl(i) * w->d * w->d * w->wr(i));
+      QR_CUDA(cudaMemcpy(w->host_w[i].data(), w->site[i], sizeof(double2) * w->host_w[i].size(),
+                         cudaMemcpyDeviceToHost));
+    }
+    w->host_ok = true;
+  }
+  ops.tab.resize(h->n);
+  ops.has_tab.assign(h->n, 0);
+  for (int i = 0; i < h->n; i++)
+    ops.has_tab[i] = build_mix_table(w->host_w[i].data(), ops.wl[i], h->d, ops.wr[i], &ops.tab[i]) ? 1 : 0;
   return env_sweep(h, h, &ops, h->stream, out);
 }
 

@@ -13,17 +13,19 @@
 //     (Kh = K rounded up to 32, zero padded).  A row tile of 128 real rows holds the real rows
 //     of 64 complex rows followed by their imaginary rows, so the accumulator tile maps to one
 //     64 x 128 complex output tile.
-//  2. GEMM (tensor-bound): one CTA per 128 x 128 real output tile.  Warp 0 issues TMA loads of
-//     a k-block (64 k' columns: 128-byte rows, 128-byte swizzle) of all three slices of A and B
-//     into one of two shared-memory stages; warp 1 issues, per k-block, the six slice products
-//     (l h, h l, m m, m h, h m, h h) as tcgen05.mma kind::f16 (BF16 in, FP32 accumulate,
-//     M = 128, N = 128, K = 16 per instruction): the five correction products into one TMEM
-//     accumulator, the h h product into another; warps 2-9 drain both after every k-block with
-//     tcgen05.ld and add them to FP32 registers with round-to-nearest adds.  The tensor cores' own
-//     accumulation of the leading term thus spans 4 instructions (64 k'), which keeps the bias of
-//     their FP32 accumulation at the level of one add per 64 products.  Two pairs of TMEM
-//     accumulators alternate so the drain overlaps the next k-block's MMAs.  Every wait on an mbarrier is bounded; a timeout sets an error flag, the CTA drains its
-//     own copies and MMAs in flight, frees its TMEM and returns.
+//  2. GEMM (tensor-bound): a persistent grid, one CTA per SM walking 128 x 128 real output tiles.
+//     Warp 0 issues TMA loads of a k-block (64 k' columns: 128-byte rows, 128-byte swizzle) of all
+//     three slices of A and B into one of two shared-memory stages; warp 1 issues, per k-block,
+//     the six slice products (l h, h l, m m, m h, h m, h h) as tcgen05.mma kind::f16 (BF16 in,
+//     FP32 accumulate, M = 128, N = 128, K = 16 per instruction): the five correction products into
+//     one TMEM accumulator, the h h product into another; warps 2-9 drain both after every k-block
+//     with tcgen05.ld and add them to FP32 registers with round-to-nearest adds.  The tensor
+//     cores' own accumulation of the leading term thus spans 4 instructions (64 k'), which keeps
+//     the bias of their FP32 accumulation at the level of one add per 64 products.  Two pairs of
+//     TMEM accumulators alternate so the drain overlaps the next k-block's MMAs, and the next
+//     tile's loads and MMAs run while the epilogue writes the previous tile.  Every wait on an
+//     mbarrier is bounded; a timeout sets an error flag, the CTA drains its own copies and MMAs in
+//     flight, frees its TMEM and returns.
 //
 // Result accuracy ~FP32 (relative error ~sqrt(K) 2^-24), at (BF16 rate) / 6 real-product
 // throughput: 48 BF16 flops per complex multiply-add.
@@ -43,7 +45,6 @@ constexpr int TC_BK = 64;   // k' columns of a k-block (128-byte bf16 rows)
 constexpr int TC_STAGES = 2;
 constexpr int TC_TILE = TC_BM * TC_BK * 2;  // bytes of one slice tile (A and B alike: 16 KiB)
 constexpr int TC_STAGE = 6 * TC_TILE;        // A h/m/l + B h/m/l
-constexpr int TC_CHUNK = 1;                  // k-blocks per TMEM accumulation
 constexpr int TC_THREADS = 320;              // warp 0 TMA, warp 1 MMA + TMEM, warps 2-9 epilogue
 constexpr int TC_EPI_WARPS = 8;              // two per TMEM lane quarter, 64 columns each
 constexpr int TC_TMEM_COLS = 4 * TC_BN;      // two buffers x (corrections, leading term), FP32
@@ -239,22 +240,27 @@ __global__ void split_b_k(const double2* __restrict__ B, long ldb, long sB, int 
 // ---- pass 2: the tcgen05 GEMM ------------------------------------------------------------------
 // Grid (N tiles, M tiles, batch).  nk = k-blocks of 64 k' columns; bplanes = 1 when B is shared by
 // the batch (its planes are 0..2), else B's planes of batch b are 3b..3b+2.
+// Persistent: CTA b takes the output tiles t = b, b + grid, ... (tile t: column tile t % ntn, row
+// tile (t / ntn) % ntm, batch t / (ntn ntm)); the three roles keep one running k-block count g over
+// all its tiles, which selects the shared-memory stage (g % 2) and the TMEM accumulator pair
+// (g & 1) with their mbarrier phases, so the loads and MMAs of the next tile start while the
+// epilogue warps still write the previous tile's C.
 __global__ void __launch_bounds__(TC_THREADS, 1)
     zgemm_tc_k(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, double2* __restrict__ C,
-               long ldc, long sC, int M, int N, int nk, int bshared, unsigned* __restrict__ err) {
+               long ldc, long sC, int M, int N, int nk, int bshared, int ntm, int ntn, int batch,
+               unsigned* __restrict__ err) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + TC_STAGES * TC_STAGE);
   uint64_t* full = bars;        // [2] stage loaded
   uint64_t* empty = bars + 2;   // [2] stage consumed by the MMAs
-  uint64_t* afull = bars + 4;   // [2] accumulator chunk complete
-  uint64_t* aempty = bars + 6;  // [2] accumulator drained by the epilogue
+  uint64_t* afull = bars + 4;   // [2] accumulator pair complete for a k-block
+  uint64_t* aempty = bars + 6;  // [2] accumulator pair drained by the epilogue
   uint64_t* done = bars + 8;    // all MMAs of the CTA complete
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 9);
   volatile uint32_t* abort_flag = reinterpret_cast<volatile uint32_t*>(bars + 10);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int b = blockIdx.z;
-  const int nchunks = (nk + TC_CHUNK - 1) / TC_CHUNK;
+  const int ntiles = ntm * ntn * batch;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < TC_STAGES; s++) {
@@ -284,23 +290,29 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     if (lane == 0) {
       // ---- producer: TMA loads of the three slices of A and of B per k-block
       int issued[TC_STAGES] = {0, 0};
-      const int arow = blockIdx.y * TC_BM, brow = blockIdx.x * TC_BN;
-      const int aplane = 3 * b, bplane = bshared ? 0 : 3 * b;
-      for (int kb = 0; kb < nk; kb++) {
-        const int s = kb % TC_STAGES;
-        const uint32_t ph = (uint32_t)(kb / TC_STAGES) & 1u;
-        if (*abort_flag || !mbar_wait(empty + s, ph ^ 1u, abort_flag)) {
-          *abort_flag = 1;
-          break;
+      unsigned g = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+        const int tn = t % ntn, tm = (t / ntn) % ntm, b = t / (ntn * ntm);
+        const int arow = tm * TC_BM, brow = tn * TC_BN;
+        const int aplane = 3 * b, bplane = bshared ? 0 : 3 * b;
+        for (int kb = 0; kb < nk; kb++, g++) {
+          const int s = g % TC_STAGES;
+          const uint32_t ph = (g / TC_STAGES) & 1u;
+          if (*abort_flag || !mbar_wait(empty + s, ph ^ 1u, abort_flag)) {
+            ok = false;
+            break;
+          }
+          uint8_t* st = smem + s * TC_STAGE;
+          mbar_expect_tx(full + s, TC_STAGE);
+          for (int sl = 0; sl < 3; sl++) {
+            tma_load_3d(st + sl * TC_TILE, &tmA, kb * TC_BK, arow, aplane + sl, full + s);
+            tma_load_3d(st + (3 + sl) * TC_TILE, &tmB, kb * TC_BK, brow, bplane + sl, full + s);
+          }
+          issued[s]++;
         }
-        uint8_t* st = smem + s * TC_STAGE;
-        mbar_expect_tx(full + s, TC_STAGE);
-        for (int sl = 0; sl < 3; sl++) {
-          tma_load_3d(st + sl * TC_TILE, &tmA, kb * TC_BK, arow, aplane + sl, full + s);
-          tma_load_3d(st + (3 + sl) * TC_TILE, &tmB, kb * TC_BK, brow, bplane + sl, full + s);
-        }
-        issued[s]++;
       }
+      if (!ok) *abort_flag = 1;
       // every copy this thread started has landed before the CTA may exit
       for (int s = 0; s < TC_STAGES; s++)
         if (issued[s] > 0 && !mbar_wait(full + s, (uint32_t)(issued[s] - 1) & 1u, &kNever)) *abort_flag = 1;
@@ -309,16 +321,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     if (lane == 0) {
       // ---- MMA issuer
       bool ok = true;
-      for (int c = 0; c < nchunks && ok; c++) {
-        const int buf = c & 1;
-        const uint32_t aph = (uint32_t)(c >> 1) & 1u;
-        if (*abort_flag || !mbar_wait(aempty + buf, aph ^ 1u, abort_flag)) { ok = false; break; }
-        tc_fence_after();
-        const uint32_t dt = tmem + (uint32_t)(buf * 2 * TC_BN);  // corrections; + TC_BN: h h
-        const int kb1 = min(nk, (c + 1) * TC_CHUNK);
-        for (int kb = c * TC_CHUNK; kb < kb1; kb++) {
-          const int s = kb % TC_STAGES;
-          const uint32_t ph = (uint32_t)(kb / TC_STAGES) & 1u;
+      unsigned g = 0;
+      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+        for (int kb = 0; kb < nk; kb++, g++) {
+          const int buf = g & 1u;
+          const uint32_t aph = (g >> 1) & 1u;
+          if (*abort_flag || !mbar_wait(aempty + buf, aph ^ 1u, abort_flag)) { ok = false; break; }
+          tc_fence_after();
+          const uint32_t dt = tmem + (uint32_t)(buf * 2 * TC_BN);  // corrections; + TC_BN: h h
+          const int s = g % TC_STAGES;
+          const uint32_t ph = (g / TC_STAGES) & 1u;
           if (*abort_flag || !mbar_wait(full + s, ph, abort_flag)) { ok = false; break; }
           tc_fence_after();
           const uint32_t st = smem_u32(smem + s * TC_STAGE);
@@ -329,14 +341,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const uint32_t d = lead ? dt + TC_BN : dt;
 #pragma unroll
             for (int j = 0; j < TC_BK / 16; j++) {
-              const uint32_t acc = (kb > c * TC_CHUNK || (!lead && p > 0) || j > 0) ? 1u : 0u;
+              const uint32_t acc = ((!lead && p > 0) || j > 0) ? 1u : 0u;
               tc_mma(d, smem_desc(a0 + 32 * j), smem_desc(b0 + 32 * j), acc);
             }
           }
-          tc_commit(empty + s);  // the stage is free once these MMAs have read it
+          tc_commit(empty + s);   // the stage is free once these MMAs have read it
+          tc_commit(afull + buf);  // and the accumulator pair holds this k-block's products
         }
-        if (!ok) break;
-        tc_commit(afull + buf);
       }
       if (!ok) *abort_flag = 1;
       // all MMAs issued by this thread complete before the TMEM is released
@@ -349,47 +360,49 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int q = warp & 3, half = (warp - 2) >> 2;
     constexpr int EC = TC_BN / 2;
     const int r = 32 * q + lane;
-    float acc[EC];
-#pragma unroll
-    for (int j = 0; j < EC; j++) acc[j] = 0.f;
     bool ok = true;
-    for (int c = 0; c < nchunks; c++) {
-      const int buf = c & 1;
-      const uint32_t aph = (uint32_t)(c >> 1) & 1u;
-      // lane 0 waits and the warp follows its verdict, so the warp-wide TMEM loads stay convergent
-      int got = 0;
-      if (lane == 0) got = (!*abort_flag && mbar_wait(afull + buf, aph, abort_flag)) ? 1 : 0;
-      got = __shfl_sync(0xffffffffu, got, 0);
-      if (!got) { ok = false; break; }
-      tc_fence_after();
-      const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(buf * 2 * TC_BN + half * EC);
+    unsigned g = 0;
+    for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+      const int tn = t % ntn, tm = (t / ntn) % ntm, b = t / (ntn * ntm);
+      float acc[EC];
 #pragma unroll
-      for (int j = 0; j < EC / 32; j++) {
-        float v[32], w[32];
-        tmem_ld32(ta + 32 * j, v);          // corrections
-        tmem_ld32(ta + TC_BN + 32 * j, w);  // leading term
+      for (int j = 0; j < EC; j++) acc[j] = 0.f;
+      for (int kb = 0; kb < nk; kb++, g++) {
+        const int buf = g & 1u;
+        const uint32_t aph = (g >> 1) & 1u;
+        // lane 0 waits and the warp follows its verdict, so the warp-wide TMEM loads stay convergent
+        int got = 0;
+        if (lane == 0) got = (!*abort_flag && mbar_wait(afull + buf, aph, abort_flag)) ? 1 : 0;
+        got = __shfl_sync(0xffffffffu, got, 0);
+        if (!got) { ok = false; break; }
+        tc_fence_after();
+        const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(buf * 2 * TC_BN + half * EC);
 #pragma unroll
-        for (int i = 0; i < 32; i++) acc[32 * j + i] = __fadd_rn(acc[32 * j + i], __fadd_rn(w[i], v[i]));
+        for (int j = 0; j < EC / 32; j++) {
+          float v[32], w[32];
+          tmem_ld32(ta + 32 * j, v);          // corrections
+          tmem_ld32(ta + TC_BN + 32 * j, w);  // leading term
+#pragma unroll
+          for (int i = 0; i < 32; i++) acc[32 * j + i] = __fadd_rn(acc[32 * j + i], __fadd_rn(w[i], v[i]));
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(aempty + buf);
       }
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(aempty + buf);
-    }
-    if (!ok) {
-      *abort_flag = 1;
-    } else {
+      if (!ok) break;
       // row r < 64: real part of complex row m0 + r; r >= 64: imaginary part of m0 + r - 64
       const int part = r >= 64;
-      const int gi = blockIdx.y * 64 + (r & 63);
+      const int gi = tm * 64 + (r & 63);
       double* Cd = reinterpret_cast<double*>(C + (long)b * sC);
       if (gi < M) {
 #pragma unroll
         for (int j = 0; j < EC; j++) {
-          const int gj = blockIdx.x * TC_BN + half * EC + j;
+          const int gj = tn * TC_BN + half * EC + j;
           if (gj < N) Cd[2 * (gi + (long)gj * ldc) + part] = (double)acc[j];
         }
       }
     }
+    if (!ok) *abort_flag = 1;
   }
   tc_fence_before();
   __syncthreads();
@@ -486,9 +499,13 @@ int zgemm_tc(cudaStream_t s, int opA, int opB, int M, int N, int K, const double
   QR_TRY(make_map(&ma, as, Kp, 2L * Mp, 3L * batch));
   QR_TRY(make_map(&mb, bs, Kp, Np, 3L * (bshared ? 1 : batch)));
   QR_TRY(set_func_attr_once((const void*)zgemm_tc_k, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
-  dim3 grid(Np / TC_BN, Mp / 64, batch);
+  const int ntn = Np / TC_BN, ntm = Mp / 64;
+  const long ntiles = (long)ntn * ntm * batch;
+  int sms = 0;
+  QR_TRY(device_sm_count(&sms));
+  const int grid = (int)std::min<long>(ntiles, sms);  // one CTA per SM (its shared memory allows no more)
   const int nk = (int)(Kp / TC_BK);
-  zgemm_tc_k<<<grid, TC_THREADS, TC_SMEM, s>>>(ma, mb, C, ldc, sC, M, N, nk, bshared ? 1 : 0, err);
+  zgemm_tc_k<<<grid, TC_THREADS, TC_SMEM, s>>>(ma, mb, C, ldc, sC, M, N, nk, bshared ? 1 : 0, ntm, ntn, batch, err);
   QR_CHECK_LAUNCH("zgemm_tc_k");
   prof_end(s, pr);
   return QR_OK;

@@ -24,6 +24,7 @@ namespace qr {
 namespace {
 
 constexpr int TPB = 256;
+constexpr int QR_COOP_NT = 512;  // threads per CTA of the persistent factorisation
 
 __device__ double block_sum_d(double v, double* red) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -133,35 +134,43 @@ __global__ void extract_r_k(const double2* A, long lda, int k, int n, double2* R
   }
 }
 
-// zlarfg scalars of x = A[j:m, j] (len = m - j), computed by every CTA alike: returns skip (tau = 0)
-// or beta, tau and scal = 1 / (alpha - beta) through shared memory.
+// zlarfg scalars of x = A[j:m, j] (len = m - j), computed by every CTA alike (the same reduction
+// order everywhere gives the same bits): tau = 0 (skip), or beta, tau and
+// scal = 1 / (alpha - beta), through shared memory.
 struct Reflector {
   double2 tau, scal;
   double beta;
   int skip;
 };
-__device__ void reflector_of(const double2* x, int len, double* red, Reflector* out) {
+__device__ __forceinline__ double warp_sum_d(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ void reflector_of(const double2* x, int len, Reflector* out, double* red) {
   double acc = 0.0;
+#pragma unroll 4
   for (int t = 1 + threadIdx.x; t < len; t += blockDim.x) acc += x[t].x * x[t].x + x[t].y * x[t].y;
   const double xnorm2 = block_sum_d(acc, red);
-  if (threadIdx.x == 0) {
-    const double2 alpha = x[0];
-    Reflector r;
-    if (xnorm2 == 0.0 && alpha.y == 0.0) {
-      r.tau = make_double2(0.0, 0.0);
-      r.scal = make_double2(0.0, 0.0);
-      r.beta = alpha.x;
-      r.skip = 1;
-    } else {
-      const double beta = -copysign(sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xnorm2), alpha.x);
-      r.tau = make_double2((beta - alpha.x) / beta, -alpha.y / beta);
-      const double2 den = make_double2(alpha.x - beta, alpha.y);
-      const double dd = den.x * den.x + den.y * den.y;
-      r.scal = make_double2(den.x / dd, -den.y / dd);
-      r.beta = beta;
-      r.skip = 0;
+  {
+    if (threadIdx.x == 0) {
+      const double2 alpha = x[0];
+      Reflector r;
+      if (xnorm2 == 0.0 && alpha.y == 0.0) {
+        r.tau = make_double2(0.0, 0.0);
+        r.scal = make_double2(0.0, 0.0);
+        r.beta = alpha.x;
+        r.skip = 1;
+      } else {
+        const double beta = -copysign(sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xnorm2), alpha.x);
+        r.tau = make_double2((beta - alpha.x) / beta, -alpha.y / beta);
+        const double2 den = make_double2(alpha.x - beta, alpha.y);
+        const double dd = den.x * den.x + den.y * den.y;
+        r.scal = make_double2(den.x / dd, -den.y / dd);
+        r.beta = beta;
+        r.skip = 0;
+      }
+      *out = r;
     }
-    *out = r;
   }
   __syncthreads();
 }
@@ -173,53 +182,59 @@ __device__ void store_reflector(double2* x, int len, const Reflector& r) {
   if (threadIdx.x == 0) x[0] = make_double2(r.beta, 0.0);
 }
 
-__global__ void house_qr_coop_k(double2* A, int m, int n, long lda, double2* tau, unsigned* bar) {
-  __shared__ double red[32];
+// One warp per owned column: col[0:len) -= v (conj(tau) v^H col), v = (1, x[1:] scal)
+__global__ void __launch_bounds__(QR_COOP_NT) house_qr_coop_k(double2* A, int m, int n, long lda, double2* tau,
+                                                               unsigned* bar) {
   __shared__ Reflector cur;
+  __shared__ double red[32];
   Reflector prev;
   prev.skip = 1;
   const int k = m < n ? m : n;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int G = (int)gridDim.x, b = (int)blockIdx.x;
   for (int j = 0; j < k; j++) {
-    if (j > 0 && (int)((j - 1) % gridDim.x) == (int)blockIdx.x)
-      store_reflector(A + (j - 1) + (long)(j - 1) * lda, m - (j - 1), prev);
+    if (j > 0 && (j - 1) % G == b) store_reflector(A + (j - 1) + (long)(j - 1) * lda, m - (j - 1), prev);
     const double2* x = A + j + (long)j * lda;
     const int len = m - j;
-    reflector_of(x, len, red, &cur);
+    reflector_of(x, len, &cur, red);
     const Reflector r = cur;
-    if ((int)(j % gridDim.x) == (int)blockIdx.x) {
+    if (j % G == b) {
       if (threadIdx.x == 0) tau[j] = r.tau;
       prev = r;
     }
     if (!r.skip) {
       const double2 tc = make_double2(r.tau.x, -r.tau.y);
-      // own columns c > j: the first is the smallest c = blockIdx.x (mod grid) above j
-      int c0 = j + 1 + (int)(((long)blockIdx.x - (j + 1)) % (long)gridDim.x + gridDim.x) % (int)gridDim.x;
-      for (int c = c0; c < n; c += gridDim.x) {
+      const int c0 = j + 1 + ((b - (j + 1)) % G + G) % G;  // smallest owned column above j
+      for (int c = c0 + warp * G; c < n; c += nw * G) {
         double2* col = A + j + (long)c * lda;
-        double2 acc = make_double2(0.0, 0.0);
-        for (int t = threadIdx.x; t < len; t += blockDim.x) {
+        double wr = 0.0, wi = 0.0;
+#pragma unroll 8
+        for (int t = lane; t < len; t += 32) {
           const double2 v = t == 0 ? make_double2(1.0, 0.0) : cmul(x[t], r.scal);
-          acc = cadd(acc, cmulc(v, col[t]));
+          const double2 y = col[t];
+          wr += v.x * y.x + v.y * y.y;
+          wi += v.x * y.y - v.y * y.x;
         }
-        const double2 w = cmul(tc, block_sum_z(acc, red));
-        for (int t = threadIdx.x; t < len; t += blockDim.x) {
+        const double2 w = cmul(tc, make_double2(warp_sum_d(wr), warp_sum_d(wi)));
+#pragma unroll 8
+        for (int t = lane; t < len; t += 32) {
           const double2 v = t == 0 ? make_double2(1.0, 0.0) : cmul(x[t], r.scal);
           col[t] = csub(col[t], cmul(v, w));
         }
-        __syncthreads();
       }
     }
     if (!grid_barrier(bar)) return;
   }
-  if (k > 0 && (int)((k - 1) % gridDim.x) == (int)blockIdx.x)
-    store_reflector(A + (k - 1) + (long)(k - 1) * lda, m - (k - 1), prev);
+  if (k > 0 && (k - 1) % G == b) store_reflector(A + (k - 1) + (long)(k - 1) * lda, m - (k - 1), prev);
 }
 
-// Q (m x k) = H_0 .. H_{k-1} [I; 0]: CTA b forms the columns c = b (mod grid), each from e_c
-// through H_{k-1}, ..., H_0 (H_j touches rows j.. of the columns c >= j only)
+// Q (m x k) = H_0 .. H_{k-1} [I; 0]: one CTA per column c, formed from e_c through H_c, ..., H_0
+// (H_j touches rows j.. of the columns c >= j only, so columns need no synchronisation).  The
+// longest columns (most reflectors) are dealt first.
 __global__ void house_q_cols_k(double2* Q, int m, int k, long ldq, const double2* V, long ldv, const double2* tau) {
   __shared__ double red[32];
-  for (int c = blockIdx.x; c < k; c += gridDim.x) {
+  for (int cc = blockIdx.x; cc < k; cc += gridDim.x) {
+    const int c = k - 1 - cc;
     double2* col = Q + (long)c * ldq;
     for (int t = threadIdx.x; t < m; t += blockDim.x) col[t] = make_double2(t == c ? 1.0 : 0.0, 0.0);
     __syncthreads();
@@ -229,11 +244,13 @@ __global__ void house_q_cols_k(double2* Q, int m, int k, long ldq, const double2
       const double2* v = V + j + (long)j * ldv;
       const int len = m - j;
       double2 acc = make_double2(0.0, 0.0);
+#pragma unroll 4
       for (int t = threadIdx.x; t < len; t += blockDim.x) {
         const double2 vr = t == 0 ? make_double2(1.0, 0.0) : v[t];
         acc = cadd(acc, cmulc(vr, col[j + t]));
       }
       const double2 w = cmul(tj, block_sum_z(acc, red));
+#pragma unroll 4
       for (int t = threadIdx.x; t < len; t += blockDim.x) {
         const double2 vr = t == 0 ? make_double2(1.0, 0.0) : v[t];
         col[j + t] = csub(col[j + t], cmul(vr, w));
@@ -286,10 +303,11 @@ int zqr_thin(cudaStream_t s, double2* A, int m, int n, long lda, double2* Q, lon
   const int k = m < n ? m : n;
   int sms = 0, per_sm = 0;
   QR_TRY(device_sm_count(&sms));
-  QR_TRY(blocks_per_sm((const void*)house_qr_coop_k, TPB, 0, &per_sm));
+  QR_TRY(blocks_per_sm((const void*)house_qr_coop_k, QR_COOP_NT, 0, &per_sm));
   if (per_sm < 1) return zqr_thin_steps(s, A, m, n, lda, Q, ldq, R, ldr, tau);
-  // one CTA per trailing column while they last; more CTAs only add barrier arrivals
-  int grid = std::min(per_sm * sms, std::max(1, n - 1));
+  // one 512-thread CTA per SM, one warp per owned column: a step is the reflector (warp 0 of every
+  // CTA), the column updates of the CTA's warps in parallel, and the grid barrier
+  int grid = std::min(sms, std::max(1, n - 1));
   unsigned* bar = nullptr;
   cudaError_t e = cudaMallocAsync((void**)&bar, 4 * sizeof(unsigned), s);
   if (e != cudaSuccess) return fail(QR_ENOMEM, std::string("QR barrier: ") + cudaGetErrorString(e));
@@ -301,7 +319,7 @@ int zqr_thin(cudaStream_t s, double2* A, int m, int n, long lda, double2* Q, lon
     double2* tp = tau;
     unsigned* bp = bar;
     void* args[] = {&Ap, &mm, &nn, &ld, &tp, &bp};
-    rc = cuda_ok_qr(cudaLaunchCooperativeKernel((const void*)house_qr_coop_k, dim3(grid), dim3(TPB), args, 0, s));
+    rc = cuda_ok_qr(cudaLaunchCooperativeKernel((const void*)house_qr_coop_k, dim3(grid), dim3(QR_COOP_NT), args, 0, s));
     count_launch();
   }
   unsigned hb[3] = {0, 0, 0};

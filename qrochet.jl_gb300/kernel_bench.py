@@ -5,6 +5,7 @@
     python qrochet.jl_gb300/kernel_bench.py qr M N
     python qrochet.jl_gb300/kernel_bench.py zgemm_tc M N K [iters] [batch]
     python qrochet.jl_gb300/kernel_bench.py batch CHI_MAX REQUESTS fp64|mixed
+    python qrochet.jl_gb300/kernel_bench.py mpo_env N CHI split|fp64 [reps]
     python qrochet.jl_gb300/kernel_bench.py upload CHI
 
 Inputs are seeded complex Gaussians; prints one JSON line with the event-timed duration, the
@@ -95,6 +96,28 @@ def main(argv):
             dt = time.perf_counter() - t0
             out = {"op": "batch", "chi_max": chi, "requests": nreq, "precision": prec,
                    "gates": sum(len(r.gates) for r in reqs), "wall_s": dt, **b.info()}
+    elif what == "mpo_env":
+        # <psi|H_XXZ|psi> environment sweep on an n-site chain with bonds min(chi, 2^i) mirrored
+        import time
+        import qrochet as Q
+        n, chi, prec = int(argv[1]), int(argv[2]), argv[3]
+        reps = int(argv[4]) if len(argv) > 4 else 1
+        arrays = []
+        for i in range(n):
+            cl = 1 if i == 0 else min(chi, 2 ** i, 2 ** (n - i))
+            cr = 1 if i == n - 1 else min(chi, 2 ** (i + 1), 2 ** (n - i - 1))
+            a = R.complex_gaussian(g, (2, cl, cr)) / np.sqrt(2.0 * cl)
+            arrays.append(np.asfortranarray(a[:, 0, :] if i == 0 else a[:, :, 0] if i == n - 1 else a))
+        psi = Q.MPS(arrays)
+        psi.set_precision("mixed+split" if prec == "split" else "fp64")
+        H = Q.MPO(R.xxz_mpo_arrays(n, 1.0, 0.7))
+        Q.mpo_expect(psi, H)
+        psi.sync()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            e = Q.mpo_expect(psi, H)
+        dt = (time.perf_counter() - t0) / reps
+        out = {"op": "mpo_env", "n": n, "chi": chi, "precision": prec, "ms": 1e3 * dt, "energy": [e.real, e.imag]}
     elif what == "upload":
         # a 3-site chain whose middle site is (2, chi, chi) in the reference's (o, l, r) order: the
         # upload permutes it to the device layout (l, o, r)

@@ -70,3 +70,25 @@ def test_batch_full_bond_class_matches_server(precision):
                 assert max(b.bond_dims(rid)) == 64
                 scale = max(1e-300, float(np.max(np.abs(ref))))
                 assert np.max(np.abs(b.values(rid) - ref)) <= 1e-9 * scale, rid
+
+
+def test_batch_edge_cases():
+    """Two-site chains, a chain with no gates, an identity string (<psi|psi>), and a threshold
+    that keeps no singular value (the engine flags that request with QR_EINVAL instead of leaving
+    a size-0 bond in its fixed-capacity layout; the others are unaffected)."""
+    g = R.rng(47)
+    two = S.random_request(g, n_range=(2, 2), depth_range=(3, 3), chi_choices=(2,), nobs=2, weight_range=(1, 2))
+    none = S.Request(n=5, chi_max=4, gates=[], observables=[[(1, "Z")], [(3, "X")]])
+    ident = S.random_request(g, n_range=(6, 6), depth_range=(4, 4), chi_choices=(8,), nobs=1)
+    ident.observables = [[]]
+    empty = S.random_request(g, n_range=(4, 4), depth_range=(1, 1), chi_choices=(4,), nobs=1, threshold=10.0)
+    with Batch() as b:
+        ids = [b.add(r) for r in (two, none, ident, empty)]
+        b.run()
+        for rid, r in zip(ids[:3], (two, none, ident)):
+            ref, vals = _oracle(r)
+            assert b.bond_dims(rid) == ref.bond_dims()
+            nrm2 = abs(O.overlap(ref, ref))
+            assert np.max(np.abs(b.values(rid) - vals)) <= 1e-10 * max(nrm2, 1e-300), rid
+        assert np.allclose(b.values(ids[1]), [1.0, 0.0])
+        assert b.result(ids[3])["status"] == 1  # QR_EINVAL
