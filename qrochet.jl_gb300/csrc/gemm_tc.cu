@@ -179,8 +179,8 @@ __device__ __forceinline__ void put3(__nv_bfloat16* o, long plane, long e, const
 
 // A side: elements (i, k), (i, k + 1) of op(A) (M x K) of batch b go to the four real-ified
 // positions of their 128-row tile.  One thread per (k pair, i), k fastest.
-template <int OPA>
-__global__ void split_a_k(const double2* __restrict__ A, long lda, long sA, int M, int K, int Mp, int Kh,
+template <int OPA, class CT>
+__global__ void split_a_k(const CT* __restrict__ A, long lda, long sA, int M, int K, int Mp, int Kh,
                           __nv_bfloat16* __restrict__ out) {
   const int b = blockIdx.z;
   const long Kp = 2L * Kh, rows = 2L * Mp;
@@ -195,7 +195,7 @@ __global__ void split_a_k(const double2* __restrict__ A, long lda, long sA, int 
 #pragma unroll
     for (int u = 0; u < 2; u++) {
       if (i < M && k + u < K) {
-        const double2 v = (OPA == OP_N || OPA == OP_R) ? A[i + (long)(k + u) * lda] : A[k + u + (long)i * lda];
+        const CT v = (OPA == OP_N || OPA == OP_R) ? A[i + (long)(k + u) * lda] : A[k + u + (long)i * lda];
         ar[u] = v.x;
         ai[u] = (OPA == OP_C || OPA == OP_R) ? -v.y : v.y;
       }
@@ -211,8 +211,8 @@ __global__ void split_a_k(const double2* __restrict__ A, long lda, long sA, int 
 
 // B side: elements (k, n), (k + 1, n) of op(B) (K x N) go to row n, columns k (real parts) and
 // Kh + k (imaginary parts).
-template <int OPB>
-__global__ void split_b_k(const double2* __restrict__ B, long ldb, long sB, int K, int N, int Np, int Kh,
+template <int OPB, class CT>
+__global__ void split_b_k(const CT* __restrict__ B, long ldb, long sB, int K, int N, int Np, int Kh,
                           __nv_bfloat16* __restrict__ out) {
   const int b = blockIdx.z;
   const long Kp = 2L * Kh;
@@ -227,7 +227,7 @@ __global__ void split_b_k(const double2* __restrict__ B, long ldb, long sB, int 
 #pragma unroll
     for (int u = 0; u < 2; u++) {
       if (n < N && k + u < K) {
-        const double2 v = (OPB == OP_N || OPB == OP_R) ? B[k + u + (long)n * ldb] : B[n + (long)(k + u) * ldb];
+        const CT v = (OPB == OP_N || OPB == OP_R) ? B[k + u + (long)n * ldb] : B[n + (long)(k + u) * ldb];
         br[u] = v.x;
         bi[u] = (OPB == OP_C || OPB == OP_R) ? -v.y : v.y;
       }
@@ -459,9 +459,11 @@ size_t zgemm_tc_workspace(int M, int N, int K, int batch, bool bshared) {
   return a + bb + 256;
 }
 
-int zgemm_tc(cudaStream_t s, int opA, int opB, int M, int N, int K, const double2* A, long lda, long sA,
-             const double2* B, long ldb, long sB, double2* C, long ldc, long sC, int batch, void* ws,
-             unsigned* err) {
+// complex FP64 (double2) or FP32 (float2) operands; the split passes round to FP32 either way
+template <class CT>
+static int zgemm_tc_t(cudaStream_t s, int opA, int opB, int M, int N, int K, const CT* A, long lda, long sA,
+                      const CT* B, long ldb, long sB, double2* C, long ldc, long sC, int batch, void* ws,
+                      unsigned* err) {
   if (M <= 0 || N <= 0 || batch <= 0) return QR_OK;
   if (K <= 0) return zscale_matrix(s, M, N, make_double2(0.0, 0.0), C, ldc, sC, batch);
   const bool bshared = sB == 0;
@@ -477,20 +479,20 @@ int zgemm_tc(cudaStream_t s, int opA, int opB, int M, int N, int K, const double
     const long ta = (long)Mp * (Kh / 2);
     dim3 g((unsigned)std::min<long>((ta + 255) / 256, 152 * 16), 1, batch);
     switch (opA) {
-      case OP_N: split_a_k<OP_N><<<g, 256, 0, s>>>(A, lda, sA, M, K, Mp, Kh, as); break;
-      case OP_T: split_a_k<OP_T><<<g, 256, 0, s>>>(A, lda, sA, M, K, Mp, Kh, as); break;
-      case OP_C: split_a_k<OP_C><<<g, 256, 0, s>>>(A, lda, sA, M, K, Mp, Kh, as); break;
-      case OP_R: split_a_k<OP_R><<<g, 256, 0, s>>>(A, lda, sA, M, K, Mp, Kh, as); break;
+      case OP_N: split_a_k<OP_N, CT><<<g, 256, 0, s>>>(A, lda, sA, M, K, Mp, Kh, as); break;
+      case OP_T: split_a_k<OP_T, CT><<<g, 256, 0, s>>>(A, lda, sA, M, K, Mp, Kh, as); break;
+      case OP_C: split_a_k<OP_C, CT><<<g, 256, 0, s>>>(A, lda, sA, M, K, Mp, Kh, as); break;
+      case OP_R: split_a_k<OP_R, CT><<<g, 256, 0, s>>>(A, lda, sA, M, K, Mp, Kh, as); break;
       default: return fail(QR_EINVAL, "zgemm_tc: bad opA");
     }
     QR_CHECK_LAUNCH("split_a_k");
     const long tb = (long)Np * (Kh / 2);
     dim3 gb((unsigned)std::min<long>((tb + 255) / 256, 152 * 16), 1, bshared ? 1 : batch);
     switch (opB) {
-      case OP_N: split_b_k<OP_N><<<gb, 256, 0, s>>>(B, ldb, sB, K, N, Np, Kh, bs); break;
-      case OP_T: split_b_k<OP_T><<<gb, 256, 0, s>>>(B, ldb, sB, K, N, Np, Kh, bs); break;
-      case OP_C: split_b_k<OP_C><<<gb, 256, 0, s>>>(B, ldb, sB, K, N, Np, Kh, bs); break;
-      case OP_R: split_b_k<OP_R><<<gb, 256, 0, s>>>(B, ldb, sB, K, N, Np, Kh, bs); break;
+      case OP_N: split_b_k<OP_N, CT><<<gb, 256, 0, s>>>(B, ldb, sB, K, N, Np, Kh, bs); break;
+      case OP_T: split_b_k<OP_T, CT><<<gb, 256, 0, s>>>(B, ldb, sB, K, N, Np, Kh, bs); break;
+      case OP_C: split_b_k<OP_C, CT><<<gb, 256, 0, s>>>(B, ldb, sB, K, N, Np, Kh, bs); break;
+      case OP_R: split_b_k<OP_R, CT><<<gb, 256, 0, s>>>(B, ldb, sB, K, N, Np, Kh, bs); break;
       default: return fail(QR_EINVAL, "zgemm_tc: bad opB");
     }
     QR_CHECK_LAUNCH("split_b_k");
@@ -509,6 +511,17 @@ int zgemm_tc(cudaStream_t s, int opA, int opB, int M, int N, int K, const double
   QR_CHECK_LAUNCH("zgemm_tc_k");
   prof_end(s, pr);
   return QR_OK;
+}
+
+int zgemm_tc(cudaStream_t s, int opA, int opB, int M, int N, int K, const double2* A, long lda, long sA,
+             const double2* B, long ldb, long sB, double2* C, long ldc, long sC, int batch, void* ws,
+             unsigned* err) {
+  return zgemm_tc_t<double2>(s, opA, opB, M, N, K, A, lda, sA, B, ldb, sB, C, ldc, sC, batch, ws, err);
+}
+int zgemm_tc(cudaStream_t s, int opA, int opB, int M, int N, int K, const float2* A, long lda, long sA,
+             const float2* B, long ldb, long sB, double2* C, long ldc, long sC, int batch, void* ws,
+             unsigned* err) {
+  return zgemm_tc_t<float2>(s, opA, opB, M, N, K, A, lda, sA, B, ldb, sB, C, ldc, sC, batch, ws, err);
 }
 
 }  // namespace qr

@@ -18,6 +18,10 @@ size_t zgemm_tc_workspace(int M, int N, int K, int batch, bool bshared);
 int zgemm_tc(cudaStream_t s, int opA, int opB, int M, int N, int K, const double2* A, long lda, long sA,
              const double2* B, long ldb, long sB, double2* C, long ldc, long sC, int batch, void* ws,
              unsigned* err);
+// the same product of complex FP32 operands (the FP32 Jacobi stage's Gram matrices)
+int zgemm_tc(cudaStream_t s, int opA, int opB, int M, int N, int K, const float2* A, long lda, long sA,
+             const float2* B, long ldb, long sB, double2* C, long ldc, long sC, int batch, void* ws,
+             unsigned* err);
 
 // ---- gemm_df.cu: complex GEMM in double-float (hi, lo FP32 pairs) on the FP32 pipes
 enum { DF_STORE = 0, DF_I_MINUS = 1, DF_F32_AXPY = 2, DF_GRAM = 3 };
@@ -107,6 +111,9 @@ enum SvdPath {
   SP_QR_PRECOND_FP64,    // FP64 path on R^H of a Householder QR
   SP_QR_PRECOND_MIXED,   // mixed path restarted on R^H after its FP32 probe
   SP_REORTH,             // Householder re-orthonormalisation of the kept singular vectors
+  SP_BLOCK_MASKED,       // FP32 block sweeps over the block pairs a Gram test marks
+  SP_DF_MASKED,          // double-float polish sweep over the marked pairs in round order
+  SP_DF_LINEAR,          // double-float polish: marked pairs rotated at once to first order
   SP_COUNT
 };
 extern std::atomic<uint64_t> g_svd_path[SP_COUNT];

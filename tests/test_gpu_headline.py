@@ -32,7 +32,7 @@ pytestmark = pytest.mark.gpu
 HERE = os.path.dirname(os.path.abspath(__file__))
 PATHS = ["cluster", "block_cluster", "block_barrier", "block_dataflow", "f64_barrier", "f64_dataflow",
          "f32_barrier", "f32_dataflow", "df_cluster", "df_barrier", "df_dataflow", "qr_precond_fp64",
-         "qr_precond_mixed", "reorth"]
+         "qr_precond_mixed", "reorth", "block_masked", "df_masked", "df_linear"]
 
 
 def svd_paths():
@@ -62,7 +62,7 @@ def _graded(g, n, decades):
 
 
 @pytest.mark.parametrize("mode,case,n,expect_paths", [
-    (1, "gaussian", 2048, ("block_dataflow", "df_dataflow")),
+    (1, "gaussian", 2048, ("block_dataflow", "block_masked", "df_dataflow", "df_linear")),
     (1, "graded", 2048, ("qr_precond_mixed", "block_dataflow", "df_dataflow")),
     (0, "gaussian", 1024, ("qr_precond_fp64", "f64_dataflow")),
 ])
