@@ -51,6 +51,10 @@ def parse():
     p.add_argument("--launch-list", action="store_true",
                    help="only the warm-up and timed steps of the mixed path (for ncu launch lists)")
     p.add_argument("--batched", type=int, default=128, help="requests in the batched sample (0: skip)")
+    p.add_argument("--canonize-full", action="store_true",
+                   help="also time the whole canonize! of the MPO leg's chain (about a minute)")
+    p.add_argument("--batched-full", type=int, default=8,
+                   help="requests of the full batched distribution, chi_max up to 512 (0: skip)")
     p.add_argument("--serve", type=int, default=24, help="requests in the serving sample (0: skip)")
     p.add_argument("--serve-sat", type=int, default=64,
                    help="requests in the saturated mixed-precision serving sample (0: skip)")
@@ -270,6 +274,47 @@ def run_batched(args, Q, dist, rank, world):
     return out
 
 
+def run_batched_full(args, Q, dist, rank, world):
+    """Batched solves/s on a sample of the whole batched distribution: n ~ U[8,96], depth ~ U[4,32],
+    chi_max log-uniform in {16, ..., 512}, cutoff 1e-10 (`--batched-full` requests, seed 12: chi_max
+    512, 256, 3 x 128, 64, 2 x 32).  Requests with chi_max <= 64 run on the batched engine (one
+    graph), the larger ones on the request server (one chain and stream per request; their gates take
+    the multi-CTA SVD), one after the other; solves/s = requests / the two wall times.  A sample:
+    per-request cost is heavy-tailed (a chi_max = 512 request with n ~ 90 runs ~1000 gates, most at
+    theta 1024 x 1024), so the 512-request distribution would take tens of minutes at these rates."""
+    from qrochet import serve as S
+    from qrochet.batch import Batch
+
+    reqs = shard(S.batched_requests(args.batched_full, seed=12, chi_log2=(4, 9), nobs=1), rank, world)
+    small = [r for r in reqs if r.chi_max <= 64]
+    large = [r for r in reqs if r.chi_max > 64]
+    gates = dist.sum(sum(len(r.gates) for r in reqs))
+    t_eng = t_srv = 0.0
+    if small:
+        with Batch(device=0, precision="mixed") as bt:
+            for r in small:
+                bt.add(r)
+            dist.barrier()
+            t0 = time.perf_counter()
+            bt.run()
+            t_eng = dist.max(time.perf_counter() - t0)
+    lat = []
+    if large:
+        with S.Server(workers=args.workers, precision="mixed") as sv:
+            dist.barrier()
+            t0 = time.perf_counter()
+            tickets = [sv.submit(r) for r in large]
+            res = [sv.wait(t) for t in tickets]
+            t_srv = dist.max(time.perf_counter() - t0)
+        lat = [x["latency_ms"] for x in res]
+    n_all = int(dist.sum(len(reqs)))
+    return {"requests": n_all, "gates": int(gates), "chi_max": sorted((r.chi_max for r in reqs), reverse=True),
+            "solves_per_s": n_all / max(1e-9, t_eng + t_srv), "gate_steps_per_s": gates / max(1e-9, t_eng + t_srv),
+            "engine_s": t_eng, "engine_requests": len(small), "server_s": t_srv, "server_requests": len(large),
+            "server_latency_ms": sorted(float(x) for x in lat), "precision": "mixed",
+            "sample": f"{args.batched_full} requests of the full batched distribution (chi_max 16..512), seed 12"}
+
+
 def run_serving(args, Q, dist, rank, world):
     """Serving: Poisson arrivals at 200 req/s of random brick-wall circuits with 8 Pauli strings of
     weight 1-4; p50/p99 latency and solves/s.  Bounded samples:
@@ -375,6 +420,17 @@ def run_mpo_env(args, Q):
         t2 = time.perf_counter()
         canon[prec] = {"qr_step_ms": 1e3 * (t1 - t0), "svd_step_ms": 1e3 * (t2 - t1)}
         del c
+    if args.canonize_full:
+        # the whole canonize! (Chain.jl:469-497) of this chain, per precision, on a copy
+        for prec in ("mixed", "fp64"):
+            c = psi.copy()
+            c.set_precision(prec)
+            c.sync()
+            t0 = time.perf_counter()
+            Q.canonize_(c)
+            c.sync()
+            canon[prec]["canonize_s"] = time.perf_counter() - t0
+            del c
     bonds = [1] + [min(chi, 2 ** (i + 1), 2 ** (n - i - 1)) for i in range(n - 1)] + [1]
     wdim = [1] + [5] * (n - 1) + [1]
     flops = sum(8.0 * (wdim[i] * bonds[i] * 2 * bonds[i + 1] * bonds[i] + bonds[i + 1] * bonds[i + 1] * 2 * bonds[i] *
@@ -561,6 +617,26 @@ def run_ours(args, chi):
         d64 = dist.max(t64.stop())
         fp64 = {"value": world * args.fp64_steps / d64, "unit": "gate-steps/s",
                 "ms_per_step": 1e3 * d64 / args.fp64_steps, "steps": args.fp64_steps}
+        # how the FP64 arm uses its pipe: two more steps under the kernel-class profiler
+        Q.prof_enable(True)
+        for i in range(2):
+            step(p64, 1 + args.fp64_steps + i)
+        p64.sync()
+        st64 = {k: Q.prof_read(k) for k in Q.PROF_KINDS}
+        Q.prof_enable(False)
+        dfma = Q.probe_peak("dfma")
+        ms64 = sum(v["ms"] for v in st64.values())
+        ex64 = sum(v["flops"] for v in st64.values())
+        fp64["pipe"] = {
+            "peak_dfma_tflops": dfma,
+            "algorithmic_frac_of_dfma": (gate_flops(chi) / (fp64["ms_per_step"] * 1e-3)) / (dfma * 1e12),
+            "executed_tflops": ex64 / (ms64 * 1e-3) / 1e12 if ms64 > 0 else 0.0,
+            "executed_frac_of_dfma": ex64 / (ms64 * 1e-3) / (dfma * 1e12) if ms64 > 0 else 0.0,
+            "time_share": {k: round(v["ms"] / max(1e-9, ms64), 4) for k, v in st64.items() if v["ms"] > 0},
+            "note": "executed = the FP64 operations the kernels count (Jacobi inner products and rotations, "
+                    "Householder QR, DMMA GEMMs) over their event time: one-sided Jacobi does ~4x the "
+                    "Golub-Van Loan R-SVD count, so the executed rate, not the algorithmic one, shows how "
+                    "busy the FP64 pipe is"}
         del p64
 
     # ---- e2e through the C ABI with pinned host buffers --------------------------------------------
@@ -684,6 +760,9 @@ def run_ours(args, chi):
                     float(np.max(np.abs(lv - lam_oracle)) / lam_oracle[0]) if lv.size == lam_oracle.size else None)
 
     batched = run_batched(args, Q, dist, rank, world) if (args.batched > 0 and not args.quick) else None
+    if args.batched_full > 0 and not args.quick:
+        batched = batched or {}
+        batched["full_distribution"] = run_batched_full(args, Q, dist, rank, world)
     serving = run_serving(args, Q, dist, rank, world) if (args.serve > 0 and not args.quick) else None
     mpo_env = run_mpo_env(args, Q) if (args.mpo_sites > 0 and not args.quick) else None
     tebd = run_tebd(args, Q, local) if not (args.no_tebd or args.quick) else None

@@ -17,6 +17,7 @@
 //  - zqr_thin_steps: one reflector launch and one trailing-update launch per column (and one
 //    Q launch per column), no scratch beyond tau; the allocation-free SVD uses it.
 #include "kernels.cuh"
+#include "prof.cuh"
 #include "grid_sync.cuh"
 
 namespace qr {
@@ -297,14 +298,28 @@ int zqr_thin_steps(cudaStream_t s, double2* A, int m, int n, long lda, double2* 
   return QR_OK;
 }
 
+static int zqr_thin_coop(cudaStream_t s, double2* A, int m, int n, long lda, double2* Q, long ldq, double2* R,
+                         long ldr, double2* tau, int sms);
+
 int zqr_thin(cudaStream_t s, double2* A, int m, int n, long lda, double2* Q, long ldq, double2* R,
              long ldr, double2* tau) {
   if (m <= 0 || n <= 0) return QR_OK;
-  const int k = m < n ? m : n;
   int sms = 0, per_sm = 0;
   QR_TRY(device_sm_count(&sms));
   QR_TRY(blocks_per_sm((const void*)house_qr_coop_k, QR_COOP_NT, 0, &per_sm));
   if (per_sm < 1) return zqr_thin_steps(s, A, m, n, lda, Q, ldq, R, ldr, tau);
+  // complex flops: factorisation 8 (m n^2 - n^3 / 3), the same again to form Q
+  const double fl = 8.0 * ((double)m * n * n - (double)n * n * n / 3.0) * (Q ? 2.0 : 1.0);
+  const int pr = prof_begin(s, PK_QR, fl, 16.0 * (double)m * n * (Q ? 3.0 : 2.0));
+  const int rc0 = zqr_thin_coop(s, A, m, n, lda, Q, ldq, R, ldr, tau, sms);
+  prof_end(s, pr);
+  return rc0;
+}
+
+// the cooperative factorisation, R and Q of zqr_thin
+static int zqr_thin_coop(cudaStream_t s, double2* A, int m, int n, long lda, double2* Q, long ldq, double2* R,
+                         long ldr, double2* tau, int sms) {
+  const int k = m < n ? m : n;
   // one 512-thread CTA per SM, one warp per owned column: a step is the reflector (warp 0 of every
   // CTA), the column updates of the CTA's warps in parallel, and the grid barrier
   int grid = std::min(sms, std::max(1, n - 1));
