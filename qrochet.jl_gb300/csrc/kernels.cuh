@@ -114,6 +114,7 @@ enum SvdPath {
   SP_BLOCK_MASKED,       // FP32 block sweeps over the block pairs a Gram test marks
   SP_DF_MASKED,          // double-float polish sweep over the marked pairs in round order
   SP_DF_LINEAR,          // double-float polish: marked pairs rotated at once to first order
+  SP_DF_BLOCK,           // double-float polish: full sweeps over pairs of 2-column blocks
   SP_COUNT
 };
 extern std::atomic<uint64_t> g_svd_path[SP_COUNT];

@@ -1135,10 +1135,62 @@ __device__ __forceinline__ void df_rot_small(float2& xh, float2& xl, float2& yh,
   yl = make_float2(nyr.l, nyi.l);
 }
 
+// a.h b.h + c.h d.h exactly (FMA products, TwoSum) plus the hi x lo cross terms, as (sum, lo)
+__device__ __forceinline__ dfl df_prod2(dfl a, dfl b, dfl c, dfl d) {
+  const float p1 = __fmul_rn(a.h, b.h), e1 = fmaf(a.h, b.h, -p1);
+  const float p2 = __fmul_rn(c.h, d.h), e2 = fmaf(c.h, d.h, -p2);
+  const dfl s = df_two_sum(p1, p2);
+  float lo = __fadd_rn(__fadd_rn(s.l, e1), e2);
+  lo = fmaf(a.h, b.l, lo);
+  lo = fmaf(a.l, b.h, lo);
+  lo = fmaf(c.h, d.l, lo);
+  lo = fmaf(c.l, d.h, lo);
+  return {s.h, lo};
+}
+// x + v - delta x_hi for double-float x, unnormalised v and FP32 delta
+__device__ __forceinline__ dfl df_add_shift(dfl x, dfl v, float delta) {
+  const dfl s = df_two_sum(x.h, v.h);
+  float lo = __fadd_rn(__fadd_rn(s.l, x.l), v.l);
+  lo = fmaf(-delta, x.h, lo);
+  return df_fast_two_sum(s.h, lo);
+}
+// Medium-angle rotation (|t| <= 2^-12), the same map as df_rot in ~2/3 of its instructions:
+// c = 1 - delta with delta = (1 - c_hi) - c_lo <= 3e-8 (1 - c_hi is exact), x' = x - conj(s) y -
+// delta x and y' = y + s x - delta y.  The s y products are exact FP32 products of the high parts
+// plus the hi x lo cross terms (the lo x lo terms are below 2^-48 |s| |y|), and delta x takes the
+// high part only: delta |x_lo| and the FP32 rounding of delta x_hi are below 2^-48 |x|.
+__device__ __forceinline__ void df_rot_medium(float2& xh, float2& xl, float2& yh, float2& yl, dfl c, dfl sr, dfl si) {
+  const float delta = __fsub_rn(__fsub_rn(1.f, c.h), c.l);
+  const dfl xr{xh.x, xl.x}, xi{xh.y, xl.y}, yr{yh.x, yl.x}, yi{yh.y, yl.y};
+  const dfl nsi = df_neg(si);
+  const dfl px = df_prod2(sr, yr, si, yi);   // Re(conj(s) y)
+  const dfl qx = df_prod2(sr, yi, nsi, yr);  // Im(conj(s) y)
+  const dfl py = df_prod2(sr, xr, nsi, xi);  // Re(s x)
+  const dfl qy = df_prod2(sr, xi, si, xr);   // Im(s x)
+  const dfl nxr = df_add_shift(xr, df_neg(px), delta), nxi = df_add_shift(xi, df_neg(qx), delta);
+  const dfl nyr = df_add_shift(yr, py, delta), nyi = df_add_shift(yi, qy, delta);
+  xh = make_float2(nxr.h, nxi.h);
+  xl = make_float2(nxr.l, nxi.l);
+  yh = make_float2(nyr.h, nyi.h);
+  yl = make_float2(nyr.l, nyi.l);
+}
+struct DfParams {
+  dfl c, sr, si;
+  float tabs;
+  int go;
+};
+
+// The rotation of DfParams P in its cheapest exact form.
+__device__ __forceinline__ void df_rot_any(float2& xh, float2& xl, float2& yh, float2& yl, const DfParams& P) {
+  if (P.tabs < 0x1p-24f) df_rot_small(xh, xl, yh, yl, P.sr.h, P.si.h);
+  else if (P.tabs <= 0x1p-12f) df_rot_medium(xh, xl, yh, yl, P.c, P.sr, P.si);
+  else df_rot(xh, xl, yh, yl, P.c, P.sr, P.si);
+}
+
 // Staged double-float rotation of rows [0, len) of a column pair (as rot_cols_staged).
 template <int NT, int RPT>
-__device__ __forceinline__ void df_rot_cols_staged(float2* ph, float2* pl, float2* qh, float2* ql, int len, dfl c,
-                                                   dfl sr, dfl si, bool small) {
+__device__ __forceinline__ void df_rot_cols_staged(float2* ph, float2* pl, float2* qh, float2* ql, int len,
+                                                   const DfParams& P) {
   for (int base = 0; base < len; base += NT * RPT) {
     float2 xh[RPT], xl[RPT], yh[RPT], yl[RPT];
 #pragma unroll
@@ -1153,19 +1205,14 @@ __device__ __forceinline__ void df_rot_cols_staged(float2* ph, float2* pl, float
     for (int j = 0; j < RPT; j++) {
       const int r = base + threadIdx.x + j * NT;
       if (r < len) {
-        if (small) df_rot_small(xh[j], xl[j], yh[j], yl[j], sr.h, si.h);
-        else df_rot(xh[j], xl[j], yh[j], yl[j], c, sr, si);
+        df_rot_any(xh[j], xl[j], yh[j], yl[j], P);
         __stcg(ph + r, xh[j]); __stcg(pl + r, xl[j]); __stcg(qh + r, yh[j]); __stcg(ql + r, yl[j]);
       }
     }
   }
 }
 
-struct DfParams {
-  dfl c, sr, si;
-  float tabs;
-  int go;
-};
+
 
 // 1 / sqrt(u) in double-float for u in [1/4, 4]: FP32 seed and two Newton steps with the
 // residual 1 - u c^2 formed in double-float.
@@ -1284,21 +1331,18 @@ __device__ __forceinline__ void jacobi_pair_df(float2* __restrict__ Bh, float2* 
     if (SV) asm volatile("cp.async.wait_group 0;\n" ::: "memory");  // SV is refilled by the next pair
     return;
   }
-  const dfl cd = P.c, srd = P.sr, sid = P.si;
-  const bool small = P.tabs < 0x1p-24f;
+  const DfParams Pl = P;
   if (fits) {
 #pragma unroll
     for (int j = 0; j < RPT; j++) {
       const int r = threadIdx.x + j * NT;
-      if (small) df_rot_small(xh[j], xl[j], yh[j], yl[j], srd.h, sid.h);
-      else df_rot(xh[j], xl[j], yh[j], yl[j], cd, srd, sid);
+      df_rot_any(xh[j], xl[j], yh[j], yl[j], Pl);
       if (r < m) { __stcg(bph + r, xh[j]); __stcg(bpl + r, xl[j]); __stcg(bqh + r, yh[j]); __stcg(bql + r, yl[j]); }
     }
   } else {  // rows beyond NT * RPT (rare): reload and rotate row by row
     for (int r = threadIdx.x; r < m; r += NT) {
       float2 uh = __ldcg(bph + r), ul = __ldcg(bpl + r), wh = __ldcg(bqh + r), wl = __ldcg(bql + r);
-      if (small) df_rot_small(uh, ul, wh, wl, srd.h, sid.h);
-      else df_rot(uh, ul, wh, wl, cd, srd, sid);
+      df_rot_any(uh, ul, wh, wl, Pl);
       __stcg(bph + r, uh); __stcg(bpl + r, ul); __stcg(bqh + r, wh); __stcg(bql + r, wl);
     }
   }
@@ -1308,12 +1352,11 @@ __device__ __forceinline__ void jacobi_pair_df(float2* __restrict__ Bh, float2* 
     __syncthreads();  // rows were copied by other threads
     for (int r = threadIdx.x; r < n; r += NT) {
       float2 uh = SV[r], ul = SV[n + r], wh = SV[2 * n + r], wl = SV[3 * n + r];
-      if (small) df_rot_small(uh, ul, wh, wl, srd.h, sid.h);
-      else df_rot(uh, ul, wh, wl, cd, srd, sid);
+      df_rot_any(uh, ul, wh, wl, Pl);
       __stcg(vcol[0] + r, uh); __stcg(vcol[1] + r, ul); __stcg(vcol[2] + r, wh); __stcg(vcol[3] + r, wl);
     }
   } else {
-    df_rot_cols_staged<NT, RPT / 2>(vcol[0], vcol[1], vcol[2], vcol[3], n, cd, srd, sid, small);
+    df_rot_cols_staged<NT, RPT / 2>(vcol[0], vcol[1], vcol[2], vcol[3], n, Pl);
   }
   if (threadIdx.x == 0) {
     atomicAdd(count, 1u);
@@ -1401,6 +1444,234 @@ __global__ void __launch_bounds__(128) jacobi_cluster_df_k(float2* __restrict__ 
     state[0] = conv ? 1u : 0u;
     state[1] = sweep;
   }
+}
+
+// ---- double-float block polish: pairs of 2-column blocks -------------------------------------
+// A work item is a pair of 2-column blocks, 4 columns that one 512-thread CTA holds in registers
+// (4 rows x 4 columns of double-float complex per thread, up to 2048 rows).  Its pairs are met in
+// local rounds of 2 disjoint pairs: all 6 in 3 rounds in round 0 of a sweep (the pairs inside the
+// blocks too), the 4 cross pairs in 2 rounds later, so each pair is met once per sweep.  A local
+// round forms both pairs' double-float sums with one transposed warp reduction each and a
+// shared-memory reduction across warps, two lanes form the two rotations in parallel, and every
+// thread rotates its registers.  V's 4 columns (hi and lo) are staged in shared memory by
+// cp.async while B is loaded and the local rounds run; the item's rotations are replayed on them
+// in order afterwards.  Against the scalar sweep (one pair per item): half the dependent rounds
+// per sweep (k / 2 - 1 instead of k - 1), half of B's and V's column loads and stores per pair,
+// one flag wait and post per 4 pairs, and the two pairs' parameters formed side by side.
+constexpr int DB_NT = 512, DB_RPT = 4, DB_C = 4;
+constexpr int DB_MAXROWS = DB_NT * DB_RPT;  // 2048
+
+struct DbShared {
+  float red[2][8][DB_NT / 32];  // [pair][value (a, b, gr, gi) x (hi, lo)][warp]
+  DfParams P[6];                // the item's rotations: slot 2 lr + g of local round lr, pair g
+  int col[DB_C];
+  int rotated;
+};
+
+// pair g (0, 1) of local round lr: round 0 of a sweep (FULL) meets (0,1)(2,3), (0,2)(1,3),
+// (0,3)(1,2); later rounds meet the cross pairs (0,2)(1,3), (0,3)(1,2)
+__device__ __forceinline__ void db_pair(bool full, int lr, int g, int& p, int& q) {
+  if (full && lr == 0) {
+    p = 2 * g;
+    q = 2 * g + 1;
+  } else {
+    const int r = full ? lr - 1 : lr;
+    p = g;
+    q = r == 0 ? 2 + g : 3 - g;
+  }
+}
+
+template <bool FULL, int LR>
+__device__ __forceinline__ void db_local_round(float2 (&xh)[DB_C][DB_RPT], float2 (&xl)[DB_C][DB_RPT], DbShared& sh,
+                                               int m, float tol, float smax, int k0, unsigned* cnt) {
+  const int tid = threadIdx.x, l = tid & 31, w = tid >> 5;
+  int p0, q0, p1, q1;
+  db_pair(FULL, LR, 0, p0, q0);
+  db_pair(FULL, LR, 1, p1, q1);
+  DotAcc a0{0.f, 0.f}, b0{0.f, 0.f}, r0{0.f, 0.f}, i0{0.f, 0.f};
+  DotAcc a1{0.f, 0.f}, b1{0.f, 0.f}, r1{0.f, 0.f}, i1{0.f, 0.f};
+#pragma unroll
+  for (int j = 0; j < DB_RPT; j++) {
+    df_dot_acc(xh[p0][j], xl[p0][j], xh[q0][j], xl[q0][j], a0, b0, r0, i0);
+    df_dot_acc(xh[p1][j], xl[p1][j], xh[q1][j], xl[q1][j], a1, b1, r1, i1);
+  }
+  const dfl k0s = df_warp_sum4_t(dot_final(a0), dot_final(b0), dot_final(r0), dot_final(i0));
+  const dfl k1s = df_warp_sum4_t(dot_final(a1), dot_final(b1), dot_final(r1), dot_final(i1));
+  if ((l & 7) == 0) {
+    const int v = l >> 3;  // value index: a, b, gr, gi
+    sh.red[0][2 * v][w] = k0s.h;
+    sh.red[0][2 * v + 1][w] = k0s.l;
+    sh.red[1][2 * v][w] = k1s.h;
+    sh.red[1][2 * v + 1][w] = k1s.l;
+  }
+  __syncthreads();
+  if (w == 0) {
+    dfl v{0.f, 0.f};
+    if (l < 8) {  // lanes 0-3: pair 0's values, 4-7: pair 1's
+      const int g = l >> 2, vi = l & 3;
+#pragma unroll
+      for (int i = 0; i < DB_NT / 32; i++) v = df_add(v, {sh.red[g][2 * vi][i], sh.red[g][2 * vi + 1][i]});
+    }
+    const int base = (l >> 2) << 2;
+    const dfl sa = df_shfl(v, base & 7), sb = df_shfl(v, (base + 1) & 7);
+    const dfl sgr = df_shfl(v, (base + 2) & 7), sgi = df_shfl(v, (base + 3) & 7);
+    if (l == 0 || l == 4) {
+      const int g = l >> 2;
+      const int p = g ? p1 : p0, q = g ? q1 : q0;
+      const int cp = sh.col[p], cq = sh.col[q];
+      DfParams P;
+      const bool live = cp >= 0 && cq >= 0 && (cp < cq ? cp : cq) < k0;
+      const bool go = live && rotation_params_df(sa, sb, sgr, sgi, tol, smax, P);
+      P.go = go ? 1 : 0;
+      sh.P[2 * LR + g] = P;
+      if (go) {
+        atomicAdd(cnt, 1u);
+        atomicMax(cnt + 1, __float_as_uint(P.tabs));
+        sh.rotated = 1;
+      }
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int g = 0; g < 2; g++) {
+    const DfParams& P = sh.P[2 * LR + g];
+    if (!P.go) continue;
+    const int p = g ? p1 : p0, q = g ? q1 : q0;
+#pragma unroll
+    for (int j = 0; j < DB_RPT; j++) df_rot_any(xh[p][j], xl[p][j], xh[q][j], xl[q][j], P);
+  }
+  (void)m;
+}
+
+// The item's rotations (sh.P, slot 2 lr + g) replayed in order on the staged rows of V's 4 columns,
+// then V's columns stored; each thread takes rows tid, tid + DB_NT, ...
+template <bool FULL>
+__device__ __forceinline__ void db_replay_v(float2* __restrict__ Vh, float2* __restrict__ Vl, long ldv, int n,
+                                            const DbShared& sh, const float2* SV) {
+  constexpr int NLR = FULL ? 3 : 2;
+  for (int r = threadIdx.x; r < n; r += DB_NT) {
+    float2 vh[DB_C], vl[DB_C];
+#pragma unroll
+    for (int c = 0; c < DB_C; c++) {
+      vh[c] = SV[(long)(2 * c) * n + r];
+      vl[c] = SV[(long)(2 * c + 1) * n + r];
+    }
+#pragma unroll
+    for (int lr = 0; lr < NLR; lr++)
+#pragma unroll
+      for (int g = 0; g < 2; g++) {
+        const DfParams& P = sh.P[2 * lr + g];
+        if (!P.go) continue;
+        int p, q;
+        db_pair(FULL, lr, g, p, q);  // compile-time after unrolling
+        df_rot_any(vh[p], vl[p], vh[q], vl[q], P);
+      }
+#pragma unroll
+    for (int c = 0; c < DB_C; c++) {
+      const int col = sh.col[c];
+      if (col < 0) continue;
+      __stcg(Vh + (long)col * ldv + r, vh[c]);
+      __stcg(Vl + (long)col * ldv + r, vl[c]);
+    }
+  }
+}
+
+// One work item: block pair (bp, bq) of round `round`.  SV: 4 columns x (hi, lo) x n staging.
+__device__ __forceinline__ void db_block_pair(float2* __restrict__ Bh, float2* __restrict__ Bl, long ldb, int m, int n,
+                                              float2* __restrict__ Vh, float2* __restrict__ Vl, long ldv, int nb,
+                                              int bp, int bq, int round, float tol, float smax, int k0,
+                                              unsigned* cnt, DbShared& sh, float2* SV) {
+  const int tid = threadIdx.x;
+  if (tid < DB_C) {
+    const int blk = tid < 2 ? bp : bq, c = 2 * blk + (tid & 1);
+    sh.col[tid] = (blk < nb && c < n) ? c : -1;
+  }
+  if (tid < 6) sh.P[tid].go = 0;
+  if (tid == 0) sh.rotated = 0;
+  __syncthreads();
+  if (2 * bp >= k0) return;  // all four columns at or beyond k0: none of its pairs rotates
+  // V's live columns into shared memory while B is loaded and the local rounds run
+  const int chunks = n / 2;  // 16-byte chunks per column (n even)
+#pragma unroll
+  for (int c = 0; c < DB_C; c++) {
+    const int col = sh.col[c];
+    if (col < 0) continue;
+    for (int h = tid; h < chunks; h += DB_NT) {
+      cp_async16_l2(SV + ((long)(2 * c) * n) + 2 * h, Vh + (long)col * ldv + 2 * h);
+      cp_async16_l2(SV + ((long)(2 * c + 1) * n) + 2 * h, Vl + (long)col * ldv + 2 * h);
+    }
+  }
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+  float2 xh[DB_C][DB_RPT], xl[DB_C][DB_RPT];
+#pragma unroll
+  for (int c = 0; c < DB_C; c++) {
+    const int col = sh.col[c];
+#pragma unroll
+    for (int j = 0; j < DB_RPT; j++) {
+      const int r = tid + DB_NT * j;
+      const bool ok = col >= 0 && r < m;
+      xh[c][j] = ok ? __ldcg(Bh + (long)col * ldb + r) : make_float2(0.f, 0.f);
+      xl[c][j] = ok ? __ldcg(Bl + (long)col * ldb + r) : make_float2(0.f, 0.f);
+    }
+  }
+  if (round == 0) {
+    db_local_round<true, 0>(xh, xl, sh, m, tol, smax, k0, cnt);
+    db_local_round<true, 1>(xh, xl, sh, m, tol, smax, k0, cnt);
+    db_local_round<true, 2>(xh, xl, sh, m, tol, smax, k0, cnt);
+  } else {
+    db_local_round<false, 0>(xh, xl, sh, m, tol, smax, k0, cnt);
+    db_local_round<false, 1>(xh, xl, sh, m, tol, smax, k0, cnt);
+  }
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+  __syncthreads();  // the rotated flag is final; every thread's staged V rows have landed
+  if (!sh.rotated) return;
+#pragma unroll
+  for (int c = 0; c < DB_C; c++) {
+    const int col = sh.col[c];
+    if (col < 0) continue;
+#pragma unroll
+    for (int j = 0; j < DB_RPT; j++) {
+      const int r = tid + DB_NT * j;
+      if (r < m) {
+        __stcg(Bh + (long)col * ldb + r, xh[c][j]);
+        __stcg(Bl + (long)col * ldb + r, xl[c][j]);
+      }
+    }
+  }
+  // the item's rotations on V's rows, in the order they were made (each thread its own rows)
+  if (round == 0) db_replay_v<true>(Vh, Vl, ldv, n, sh, SV);
+  else db_replay_v<false>(Vh, Vl, ldv, n, sh, SV);
+}
+
+// One block polish sweep (state, flags over the nbp blocks and convergence as jacobi_sweep_df_k).
+__global__ void __launch_bounds__(DB_NT, 1)
+    jacobi_block_df_k(float2* __restrict__ Bh, float2* __restrict__ Bl, long ldb, int m, int n, float2* __restrict__ Vh,
+                      float2* __restrict__ Vl, long ldv, int nbp, double tol, const double* __restrict__ smax_p,
+                      unsigned* __restrict__ state, int sweep, unsigned* __restrict__ flags, int k0) {
+  __shared__ DbShared sh;
+  extern __shared__ __align__(16) float2 db_sv[];
+  if (((volatile unsigned*)state)[0]) return;
+  const float smax = (float)(smax_p[0] / smax_p[1]);
+  unsigned* cnt = state + 8 + SW_STRIDE * sweep;
+  const int nb = (n + 1) / 2;
+  const int npairs = nbp / 2;
+  const unsigned base = (unsigned)sweep * (unsigned)(nbp - 1);
+  const bool dataflow = npairs > (int)gridDim.x;
+  const long nit = dataflow ? ((long)(nbp - 1) * npairs - blockIdx.x + gridDim.x - 1) / gridDim.x : (long)(nbp - 1);
+  for (long t = 0; t < nit; t++) {
+    const long it = dataflow ? blockIdx.x + t * (long)gridDim.x : t * npairs + blockIdx.x;
+    const int round = (int)(it / npairs), pair = (int)(it % npairs);
+    int bp, bq;
+    pair_cols(nbp, round, pair, bp, bq);
+    if (dataflow && !wait_cols(flags, bp, bq, nb, base + round, state)) return;
+    if (bp < nb) db_block_pair(Bh, Bl, ldb, m, n, Vh, Vl, ldv, nb, bp, bq, round, (float)tol, smax, k0, cnt, sh, db_sv);
+    if (dataflow) post_cols(flags, bp, bq, nb, base + round + 1);
+    else {
+      __syncthreads();
+      if (!grid_barrier(state + 2)) return;
+    }
+  }
+  finish_sweep(state, cnt, sweep, 1e-7f);
 }
 
 template <int NT, int RPT>
@@ -1935,7 +2206,22 @@ int jacobi_df(cudaStream_t s, SvdWork* w, float2* Bh, float2* Bl, long ldb, int 
   int grid = std::min(per_sm * sms, np / 2);
   if (grid < 1) grid = 1;
   const bool cluster = k <= 128 && rows <= 32 * CCR;
-  svd_path(cluster ? SP_DF_CLUSTER : (np / 2 > grid ? SP_DF_DATAFLOW : SP_DF_BARRIER));
+  // full sweeps as block sweeps (pairs of 2-column blocks) when the rows fit the registers and
+  // V's columns can be staged by 16-byte copies
+  const bool blockdf = !cluster && rows <= DB_MAXROWS && k % 2 == 0 && ldv % 2 == 0;
+  const int nbp = (k + 1) / 2 + (((k + 1) / 2) & 1);
+  const size_t dbsm = sizeof(float2) * 8 * (size_t)k;
+  int dbgrid = 1;
+  if (blockdf) {
+    int dper = 0;
+    QR_TRY(set_func_attr_once((const void*)jacobi_block_df_k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)(sizeof(float2) * 8 * DB_MAXROWS)));
+    QR_TRY(blocks_per_sm((const void*)jacobi_block_df_k, DB_NT, dbsm, &dper));
+    if (dper < 1) return fail(QR_ECUDA, "double-float block sweep kernel cannot be resident");
+    dbgrid = std::max(1, std::min(dper * sms, nbp / 2));
+  }
+  svd_path(cluster ? SP_DF_CLUSTER
+                   : blockdf ? SP_DF_BLOCK : (np / 2 > grid ? SP_DF_DATAFLOW : SP_DF_BARRIER));
   // hs[nstate], hs[nstate + 1] receive a masked sweep's marked-pair count and largest tangent
   unsigned* hs = static_cast<unsigned*>(host_scratch(sizeof(unsigned) * (nstate + 2)));
   if (!hs) return fail(QR_ENOMEM, "page-locked host scratch");
@@ -2046,7 +2332,13 @@ int jacobi_df(cudaStream_t s, SvdWork* w, float2* Bh, float2* Bl, long ldb, int 
     int kz = k0;
     unsigned* dn = done;
     void* args[] = {&a1, &a2, &l1, &mm, &kk, &a3, &a4, &l2, &npp, &tl, &sm, &st, &sw, &fl, &kz, &mk, &dn};
-    QR_CUDA(cudaLaunchCooperativeKernel((const void*)jacobi_sweep_df_k<NT, RPT>, dim3(grid), dim3(NT), args, vsm, s));
+    if (blockdf && !mk) {
+      int nbb = nbp;
+      void* bargs[] = {&a1, &a2, &l1, &mm, &kk, &a3, &a4, &l2, &nbb, &tl, &sm, &st, &sw, &fl, &kz};
+      QR_CUDA(cudaLaunchCooperativeKernel((const void*)jacobi_block_df_k, dim3(dbgrid), dim3(DB_NT), bargs, dbsm, s));
+    } else {
+      QR_CUDA(cudaLaunchCooperativeKernel((const void*)jacobi_sweep_df_k<NT, RPT>, dim3(grid), dim3(NT), args, vsm, s));
+    }
     count_launch();
     prof_end(s, pr);
     QR_CUDA(cudaMemcpyAsync(hs, state, sizeof(unsigned) * nstate, cudaMemcpyDeviceToHost, s));

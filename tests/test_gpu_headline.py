@@ -32,7 +32,7 @@ pytestmark = pytest.mark.gpu
 HERE = os.path.dirname(os.path.abspath(__file__))
 PATHS = ["cluster", "block_cluster", "block_barrier", "block_dataflow", "f64_barrier", "f64_dataflow",
          "f32_barrier", "f32_dataflow", "df_cluster", "df_barrier", "df_dataflow", "qr_precond_fp64",
-         "qr_precond_mixed", "reorth", "block_masked", "df_masked", "df_linear"]
+         "qr_precond_mixed", "reorth", "block_masked", "df_masked", "df_linear", "df_block"]
 
 
 def svd_paths():
@@ -62,8 +62,10 @@ def _graded(g, n, decades):
 
 
 @pytest.mark.parametrize("mode,case,n,expect_paths", [
-    (1, "gaussian", 2048, ("block_dataflow", "block_masked", "df_dataflow", "df_linear")),
-    (1, "graded", 2048, ("qr_precond_mixed", "block_dataflow", "df_dataflow")),
+    (1, "gaussian", 2048, ("block_dataflow", "block_masked", "df_block")),
+    (1, "graded", 2048, ("qr_precond_mixed", "block_dataflow", "df_block")),
+    # an odd column count keeps the scalar double-float sweep (the block sweep pairs 2-column blocks)
+    (1, "gaussian", 2047, ("block_dataflow", "df_dataflow")),
     (0, "gaussian", 1024, ("qr_precond_fp64", "f64_dataflow")),
 ])
 def test_svd_dataflow_ordering_against_lapack(mode, case, n, expect_paths):
@@ -74,6 +76,10 @@ def test_svd_dataflow_ordering_against_lapack(mode, case, n, expect_paths):
     after = svd_paths()
     for p in expect_paths:
         assert after[p] > before[p], (p, before, after)
+    if "df_block" in expect_paths and case == "gaussian":
+        # the polish ends with the Gram test: one first-order rotation or a listed sweep
+        fin = ("df_linear", "df_masked")
+        assert sum(after[p] - before[p] for p in fin) > 0, (before, after)
     s_ref = np.linalg.svd(A, compute_uv=False)
     smax = s_ref[0]
     assert np.all(np.diff(S) <= 1e-14 * smax)
@@ -111,7 +117,7 @@ def test_gate_step_chi1024_against_oracle(chi1024_reference, precision):
     after = svd_paths()
     if precision == "mixed":
         assert after["block_dataflow"] > before["block_dataflow"]
-        assert after["df_dataflow"] > before["df_dataflow"]
+        assert after["df_block"] > before["df_block"]
     else:
         assert after["f64_dataflow"] > before["f64_dataflow"]
     assert psi.bond_dims() == ref.bond_dims()
