@@ -505,6 +505,40 @@ def test_rank_deficient_and_zero_singular_values():
 SPLIT_RTOL = 1e-5
 
 
+def test_mpo_energy_config3_sites_reduced_chi_against_oracle():
+    """The MPS-MPO workload's shape at 128 sites (XXZ, Jz = 1, Jxy = 0.7, w = 5) with chi = 16 in
+    place of 1024, so the oracle's contraction finishes in seconds: the FP64 path within 1e-10
+    and the split (tcgen05 BF16x3) path within the split tolerance of the oracle's energy."""
+    n, chi = 128, 16
+    g = R.rng(3)
+    arrays = []
+    for i in range(n):
+        cl = 1 if i == 0 else min(chi, 2 ** i, 2 ** (n - i))
+        cr = 1 if i == n - 1 else min(chi, 2 ** (i + 1), 2 ** (n - i - 1))
+        a = R.complex_gaussian(g, (2, cl, cr)) / np.sqrt(2.0 * cl)
+        arrays.append(np.asfortranarray(a[:, 0, :] if i == 0 else a[:, :, 0] if i == n - 1 else a))
+    ref = O.from_reference_arrays(arrays)
+    arrs = R.xxz_mpo_arrays(n, 1.0, 0.7)
+    ws = []
+    for i, a in enumerate(arrs):
+        a = np.asarray(a)
+        if i == 0:
+            a = a[:, :, None, :]
+        elif i == n - 1:
+            a = a[:, :, :, None]
+        ws.append(np.transpose(a, (2, 0, 1, 3)))
+    e_ref = O.mpo_expect(ref, ws)
+    scale = abs(O.norm(ref)) ** 2 * n
+    H = Q.MPO(arrs)
+    psi = Q.MPS(arrays)
+    e64 = Q.mpo_expect(psi, H)
+    assert abs(e64 - e_ref) <= 1e-10 * scale
+    psi.set_precision("mixed+split")
+    es = Q.mpo_expect(psi, H)
+    assert abs(es - e_ref) <= SPLIT_RTOL * scale
+    assert abs(es - e64) <= SPLIT_RTOL * scale
+
+
 def test_split_contractions_match_fp64():
     n = 10
     psi, ref = _pair(n, 24, seed=91)
