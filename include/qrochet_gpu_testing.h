@@ -42,8 +42,17 @@ int qr_test_svd(int mode, int m, int n, const double* A, double* U, double* S, d
    2 / 3 FP32 block sweep with grid barrier / per-block flags, 4 / 5 FP64 sweep barrier / flags,
    6 / 7 FP32 scalar sweep barrier / flags, 8 double-float cluster polish, 9 / 10 double-float
    sweep barrier / flags, 11 FP64 QR preconditioning, 12 mixed restart on R^H, 13 Householder
-   re-orthonormalisation.  Copies min(n, *total) counters; *total = number of paths. */
+   re-orthonormalisation, 14 masked FP32 block sweeps, 15 masked (listed) double-float sweep, 16
+   first-order final polish rotation, 17 double-float block sweep.  Copies min(n, *total)
+   counters; *total = number of paths. */
 int qr_test_svd_paths(uint64_t* counts, int n, int* total);
+/* The host-side greedy colour schedule of a masked Jacobi sweep (no GPU needed).  mask: nv rows
+   of ceil(nv / 32) words, bit (q & 31) of word p * ceil(nv / 32) + q / 32 marks pair p < q; flag:
+   nv words (or NULL), 1 = the pairs inside vertex v need a visit (with use_flag).  items
+   (nv (nv - 1) / 2 words): listed pairs as p | q << 15 | full << 30, colour class by colour class;
+   ord (2 per item): listed pairs before the item on p and on q.  nv even, 2 <= nv < 32768. */
+int qr_test_schedule_pairs(const unsigned* mask, const unsigned* flag, int nv, int use_flag, unsigned* items,
+                           unsigned* ord, long* listed, int* classes);
 int qr_test_qr(int m, int n, const double* A, double* Q, double* R, double* ms);
 
 #ifdef __cplusplus

@@ -94,6 +94,9 @@ void svd_work_free(SvdWork* w);
 // when their singular values are many decades below sigma_max (callers then discard them).
 int zsvd_thin(cudaStream_t s, SvdWork* w, int mode, const double2* A, int m, int n, long lda,
               double2* U, long ldu, double* S, double2* Vh, long ldvh, int keep = 0);
+// The greedy colour schedule of a masked Jacobi sweep, on host arrays (tests; see svd.cu).
+long schedule_pairs_host(const unsigned* mask, const unsigned* flag, int nv, int use_flag, unsigned* items,
+                         unsigned* ord, int* classes);
 // Process-wide counts of the SVD code paths taken (one per Jacobi stage of a call), so tests can
 // check which ordering and which kernel a size reached.
 enum SvdPath {

@@ -2059,6 +2059,25 @@ static long schedule_pairs(unsigned* hb, int nv, bool use_flag, int* classes) {
   return (long)e.size();
 }
 
+}  // namespace
+
+// The host schedule of a masked sweep on caller arrays (for tests): mask and flag as in
+// MaskedList (nv rows of ceil(nv / 32) words; flag: nv words or null), items and ord of
+// nv (nv - 1) / 2 and 2 nv (nv - 1) / 2 words.  Returns the listed pairs; *classes = colour classes.
+long schedule_pairs_host(const unsigned* mask, const unsigned* flag, int nv, int use_flag, unsigned* items,
+                         unsigned* ord, int* classes) {
+  std::vector<unsigned> hb(masked_list_words(nv), 0u);
+  const MaskedList H = masked_list(hb.data(), nv);
+  std::copy(mask, mask + (size_t)nv * H.mw, H.mask);
+  if (flag) std::copy(flag, flag + nv, H.flag);
+  const long n = schedule_pairs(hb.data(), nv, use_flag != 0, classes);
+  std::copy(H.items, H.items + n, items);
+  std::copy(H.ord, H.ord + 2 * n, ord);
+  return n;
+}
+
+namespace {
+
 // Brings the mask, flags and counts of the device MaskedList (w->ml, nv vertices) to the host,
 // schedules the marked pairs and uploads the schedule and its length (count[2]).  Synchronises s.
 static int upload_schedule(cudaStream_t s, SvdWork* w, int nv, bool use_flag, long* listed, int* classes) {

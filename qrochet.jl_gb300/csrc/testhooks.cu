@@ -168,6 +168,14 @@ int qr_test_zgemm_df(int mode, int opA, int M, int N, int K, const double* A, lo
 
 // Thin SVD of the m x n column-major A: U (m x k), S (k), Vh (k x n), k = min(m, n).
 // counts[i] = how often SVD code path i ran in this process (i < min(n, SP_COUNT)); *total = SP_COUNT
+int qr_test_schedule_pairs(const unsigned* mask, const unsigned* flag, int nv, int use_flag, unsigned* items,
+                           unsigned* ord, long* listed, int* classes) {
+  if (nv < 2 || nv % 2 || nv >= 32768 || !mask || !items || !ord || !listed || !classes)
+    return fail(QR_EINVAL, "schedule: nv must be even, in [2, 32768), and the arrays given");
+  *listed = schedule_pairs_host(mask, flag, nv, use_flag, items, ord, classes);
+  return QR_OK;
+}
+
 int qr_test_svd_paths(uint64_t* counts, int n, int* total) {
   for (int i = 0; i < n && i < SP_COUNT; i++) counts[i] = g_svd_path[i].load(std::memory_order_relaxed);
   if (total) *total = SP_COUNT;

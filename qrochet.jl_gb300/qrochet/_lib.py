@@ -118,6 +118,8 @@ SIGNATURES = {
     "qr_test_zgemm_df": [_I, _I, _I, _I, _I, _PD, C.c_long, _PD, C.c_long, _PD, _PD, C.c_long, _I, _PD],
     "qr_test_svd": [_I, _I, _I, _PD, _PD, _PD, _PD, _PD],
     "qr_test_svd_paths": [C.POINTER(C.c_uint64), _I, C.POINTER(C.c_int)],
+    "qr_test_schedule_pairs": [C.c_void_p, C.c_void_p, _I, _I, C.c_void_p, C.c_void_p, C.POINTER(C.c_long),
+                               C.POINTER(C.c_int)],
     "qr_test_qr": [_I, _I, _PD, _PD, _PD, _PD],
 }
 
