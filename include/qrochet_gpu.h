@@ -127,6 +127,12 @@ int qr_evolve_1site(qr_chain* h, int site, const double* gate /* d x d */);
 /* threshold NaN and maxdim < 0 together mean: no truncate! call */
 int qr_evolve_2site(qr_chain* h, int site_l, const double* gate /* d^2 x d^2 */,
                     double threshold, int maxdim, int iscanonical, int renormalize);
+/* A layer of two-site gates on disjoint site pairs (the inner loop of a brick-wall evolve!),
+   each as qr_evolve_2site on sites[i] (0-based left site) with the gate at gates + 2 d^4 i;
+   `lanes` gates run at a time on their own streams (<= 0: 4).  Replaces a loop of evolve! calls
+   over one layer (Chain.jl:543-661); renormalize = 1 runs the gates one after another. */
+int qr_evolve_layer(qr_chain* h, int ngates, const int* sites, const double* gates, double threshold,
+                    int maxdim, int iscanonical, int renormalize, int lanes);
 
 /* ---- contractions (Chain.jl:724-748, Ansatz.jl:101-109) ---------------------------------- */
 /* <b|a> (b conjugated), written as (re, im) */

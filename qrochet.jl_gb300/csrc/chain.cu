@@ -19,6 +19,7 @@
 #include <mutex>
 #include <map>
 #include <tuple>
+#include <thread>
 #include "kernels.cuh"
 
 namespace qr {
@@ -143,6 +144,10 @@ struct qr_chain {
   double2* ws = nullptr;          // theta / factorisation workspace
   size_t ws_cap = 0;
   double* scal = nullptr;         // small device scalars
+  // execution lanes of qr_evolve_layer: chains that own only a stream and workspaces (the
+  // fields above from `svd` on); their bookkeeping vectors are filled from this chain per layer
+  std::vector<qr_chain*> lanes;
+  bool is_lane = false;
   int cl(int i) const { return i == 0 ? (periodic ? bd[n - 1] : 1) : bd[i - 1]; }
   int cr(int i) const { return i == n - 1 ? (periodic ? bd[n - 1] : 1) : bd[i]; }
   size_t elems(int i) const { return (size_t)cl(i) * d * cr(i); }
@@ -932,8 +937,12 @@ static int chain_create(int n, int d, const int* bond_dims, bool periodic, qr_ch
 int qr_chain_free(qr_chain* h) {
   if (!h) return QR_OK;
   cudaStreamSynchronize(h->stream);
-  for (auto p : h->site) if (p) cudaFree(p);
-  for (auto p : h->lam) if (p) cudaFree(p);
+  for (qr_chain* l : h->lanes) qr_chain_free(l);
+  h->lanes.clear();
+  if (!h->is_lane) {
+    for (auto p : h->site) if (p) cudaFree(p);
+    for (auto p : h->lam) if (p) cudaFree(p);
+  }
   if (h->gate) cudaFree(h->gate);
   if (h->gate_host) cudaFreeHost(h->gate_host);
   if (h->scal) cudaFree(h->scal);
@@ -1413,6 +1422,86 @@ int qr_evolve_2site(qr_chain* h, int site_l, const double* gate, double threshol
   if (!gate) return fail(QR_EINVAL, "null gate");
   QR_TRY(evolve2_impl(h, site_l, gate, threshold, maxdim, iscanonical, renormalize));
   QR_CUDA(cudaStreamSynchronize(h->stream));
+  return QR_OK;
+}
+
+// A brick-wall layer of two-site gates on disjoint site pairs, several gates at a time.
+// A gate on sites (s, s + 1) writes sites s and s + 1, bond s and its Lambda, and reads only bonds
+// s - 1 and s + 1 (their sizes, and their Lambdas for iscanonical), which no other gate of the
+// layer writes: the gates are independent, as in the reference's evolve! loop over a layer.  Each
+// lane is a chain that owns a stream and the workspaces (theta, gate staging, SVD) and works on a
+// shallow copy of this chain's bookkeeping (bond sizes, site and Lambda pointers); a host thread
+// per lane runs its gates through evolve2_impl, and the entries each gate wrote are copied back.
+// renormalize=true sweeps the whole chain per gate (normalize!), so that case runs in order.
+int qr_evolve_layer(qr_chain* h, int ngates, const int* sites, const double* gates, double threshold, int maxdim,
+                    int iscanonical, int renormalize, int lanes) {
+  if (!h) return fail(QR_EINVAL, "null chain");
+  if (ngates < 0 || (ngates > 0 && (!sites || !gates))) return fail(QR_EINVAL, "bad gate list");
+  const int g4 = 2 * h->d * h->d * h->d * h->d;  // doubles per gate matrix
+  for (int i = 0; i < ngates; i++) {
+    if (sites[i] < 0 || sites[i] + 1 >= h->n) return fail(QR_EINVAL, "The sites in the bond must be between 1 and n");
+    for (int j = 0; j < i; j++)
+      if (std::abs(sites[i] - sites[j]) < 2) return fail(QR_EINVAL, "gates of a layer must act on disjoint sites");
+  }
+  const int L = std::max(1, std::min(ngates, lanes > 0 ? lanes : 4));
+  if (L <= 1 || renormalize) {
+    for (int i = 0; i < ngates; i++)
+      QR_TRY(evolve2_impl(h, sites[i], gates + (size_t)g4 * i, threshold, maxdim, iscanonical, renormalize));
+    QR_CUDA(cudaStreamSynchronize(h->stream));
+    return QR_OK;
+  }
+  QR_CUDA(cudaStreamSynchronize(h->stream));
+  int dev = 0;
+  QR_CUDA(cudaGetDevice(&dev));
+  while ((int)h->lanes.size() < L) {
+    qr_chain* l = new qr_chain();
+    l->n = h->n;
+    l->d = h->d;
+    l->periodic = h->periodic;
+    l->is_lane = true;
+    cudaError_t e = cudaStreamCreateWithFlags(&l->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { delete l; return cuda_fail(e, "cudaStreamCreate"); }
+    l->svd = svd_work_create();
+    int rc = dalloc((void**)&l->gate, sizeof(double2) * 256, l->stream);
+    if (!rc) rc = cuda_ok(cudaHostAlloc((void**)&l->gate_host, sizeof(double2) * 256, cudaHostAllocDefault), "cudaHostAlloc");
+    if (!rc) rc = dalloc((void**)&l->scal, sizeof(double) * 16, l->stream);
+    h->lanes.push_back(l);
+    if (rc) return rc;
+  }
+  for (int j = 0; j < L; j++) {
+    qr_chain* l = h->lanes[j];
+    l->precision = h->precision;
+    l->bd = h->bd;
+    l->site = h->site;
+    l->lam = h->lam;
+    l->lamlen = h->lamlen;
+  }
+  std::vector<int> rcs(L, QR_OK);
+  std::vector<std::string> msgs(L);
+  std::vector<std::thread> th;
+  for (int j = 0; j < L; j++)
+    th.emplace_back([&, j]() {
+      qr_chain* l = h->lanes[j];
+      int rc = cuda_ok(cudaSetDevice(dev), "cudaSetDevice");
+      for (int i = j; i < ngates && !rc; i += L)
+        rc = evolve2_impl(l, sites[i], gates + (size_t)g4 * i, threshold, maxdim, iscanonical, 0);
+      if (!rc) rc = cuda_ok(cudaStreamSynchronize(l->stream), "lane synchronisation");
+      else cudaStreamSynchronize(l->stream);
+      rcs[j] = rc;
+      if (rc) msgs[j] = qr_last_error_string();
+    });
+  for (auto& t : th) t.join();
+  for (int i = 0; i < ngates; i++) {  // the entries each gate wrote, from its lane's view
+    const qr_chain* l = h->lanes[i % L];
+    const int s0 = sites[i];
+    h->site[s0] = l->site[s0];
+    h->site[s0 + 1] = l->site[s0 + 1];
+    h->bd[s0] = l->bd[s0];
+    h->lam[s0] = l->lam[s0];
+    h->lamlen[s0] = l->lamlen[s0];
+  }
+  for (int j = 0; j < L; j++)
+    if (rcs[j]) return fail(rcs[j], msgs[j]);
   return QR_OK;
 }
 

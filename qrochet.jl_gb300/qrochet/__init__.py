@@ -7,7 +7,7 @@ from ._lib import (ArgumentError, DimensionMismatch, GPUError, MissingSchmidtCoe
                    launch_count)
 from .chain import (MPO, MPS, pMPS, Chain, Open, Periodic, canonicality_error, canonize, canonize_,
                     canonize_site, canonize_site_, contract_between, contract_between_, device_count,
-                    evolve_, expect, isleftcanonical, isrightcanonical, mixed_canonize, mixed_canonize_,
+                    evolve_, evolve_layer_, expect, isleftcanonical, isrightcanonical, mixed_canonize, mixed_canonize_,
                     mpo_expect, norm, normalize_, overlap, truncate, truncate_, zeros_chain,
                     PinnedArray, probe_peak, prof_enable, prof_read, set_device, PROF_KINDS, rand,
                     sampler_bond_dims)
@@ -19,7 +19,7 @@ __all__ = [
     "ArgumentError", "DimensionMismatch", "GPUError", "MissingSchmidtCoefficientsException",
     "launch_count", "MPO", "MPS", "pMPS", "Chain", "Open", "Periodic", "canonicality_error", "canonize",
     "canonize_", "canonize_site", "canonize_site_", "contract_between", "contract_between_",
-    "device_count", "evolve_", "expect", "isleftcanonical", "isrightcanonical", "mixed_canonize",
+    "device_count", "evolve_", "evolve_layer_", "expect", "isleftcanonical", "isrightcanonical", "mixed_canonize",
     "mixed_canonize_", "mpo_expect", "norm", "normalize_", "overlap", "truncate", "truncate_",
     "zeros_chain", "Dense", "Operator", "State", "gate_from_matrix", "validate_gate", "Site",
     "nextindex", "site", "PinnedArray", "probe_peak", "prof_enable", "prof_read", "set_device",

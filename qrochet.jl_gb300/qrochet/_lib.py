@@ -88,6 +88,7 @@ SIGNATURES = {
     "qr_truncate": [_P, _I, _I, _D, _I],
     "qr_evolve_1site": [_P, _I, _PD],
     "qr_evolve_2site": [_P, _I, _PD, _D, _I, _I, _I],
+    "qr_evolve_layer": [_P, _I, _PI, _PD, _D, _I, _I, _I, _I],
     "qr_overlap": [_P, _P, _PD],
     "qr_norm": [_P, _PD],
     "qr_expect": [_P, _I, _PI, _PI, _PD, _PD],

@@ -542,6 +542,26 @@ def evolve_(psi: Chain, gate: Dense, threshold=None, maxdim=None, iscanonical=Fa
     return psi
 
 
+def evolve_layer_(psi: Chain, gates, threshold=None, maxdim=None, iscanonical=False, renormalize=False, lanes=0):
+    """A layer of two-site gates on disjoint site pairs: the same result as ``evolve!`` of each
+    gate in turn (Chain.jl:543-661), with `lanes` gates at a time on their own streams (0: the
+    library's default)."""
+    sites, mats = [], []
+    for g in gates:
+        ls = validate_gate(psi.n, g)
+        if len(ls) != 2:
+            raise ArgumentError("evolve_layer_ takes two-site gates")
+        sites.append(ls[0] - 1)
+        mats.append(np.ascontiguousarray(g.matrix(ls)).ravel())
+    k = len(sites)
+    packed = np.ascontiguousarray(np.concatenate(mats) if mats else np.zeros(1, dtype=np.complex128))
+    th = float("nan") if threshold is None else float(threshold)
+    md = -1 if maxdim is None else int(maxdim)
+    check(lib().qr_evolve_layer(psi._h, k, (C.c_int * max(k, 1))(*sites), dptr(packed), th, md,
+                                int(bool(iscanonical)), int(bool(renormalize)), int(lanes)))
+    return psi
+
+
 # ---- contractions ---------------------------------------------------------------------------------------
 def overlap(a: Chain, b: Chain):
     """``overlap(a, b)`` = <b|a> (Chain.jl:740-748)."""

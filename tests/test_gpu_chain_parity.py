@@ -273,6 +273,41 @@ def test_tebd_with_truncation(precision):
         assert abs(e - e_ref) <= tol * max(1.0, abs(e_ref))
 
 
+@pytest.mark.parametrize("precision,lanes", [("fp64", 4), ("mixed", 4), ("mixed", 3)])
+def test_layer_evolve_matches_gate_by_gate(precision, lanes):
+    """evolve_layer_ runs a brick-wall layer's gates on several streams at once: the result is the
+    gate-by-gate evolve! result (bond dims exact, Lambdas and sites to rounding), here through
+    bonds up to 128 (theta 256 x 256: the multi-CTA FP32 / double-float sweeps run side by side),
+    and the oracle's on the same gates."""
+    n, depth, maxdim = 16, 10, 128
+    arrays = R.zero_product_arrays(n)
+    a, b = Q.MPS(arrays), Q.MPS(arrays)
+    ref = O.from_reference_arrays(arrays)
+    a.set_precision(precision)
+    b.set_precision(precision)
+    for layer in R.brickwall_layers(n, depth, seed=77):
+        Q.evolve_layer_(a, [Q.gate_from_matrix(u, [s_, s_ + 1]) for s_, u in layer], threshold=1e-10, maxdim=maxdim,
+                        lanes=lanes)
+        for s_, u in layer:
+            Q.evolve_(b, Q.gate_from_matrix(u, [s_, s_ + 1]), threshold=1e-10, maxdim=maxdim)
+            O.evolve_2site_(ref, s_ - 1, u, threshold=1e-10, maxdim=maxdim)
+        assert a.bond_dims() == b.bond_dims() == ref.bond_dims()
+    assert max(a.bond_dims()) == maxdim
+    for bnd in range(1, n):
+        la, lb = a.lambda_between(bnd, bnd + 1), b.lambda_between(bnd, bnd + 1)
+        assert np.max(np.abs(la - lb)) <= 1e-12 * lb[0]
+    tol = RTOL if precision == "fp64" else 1e-8
+    _check_same(a, ref, rtol=tol)
+    assert abs(Q.overlap(a, b) - Q.norm(a) * Q.norm(b)) <= 1e-10 * Q.norm(a) * Q.norm(b)
+
+
+def test_layer_evolve_rejects_overlapping_gates():
+    psi = Q.MPS(R.zero_product_arrays(6))
+    u = R.haar_unitary(R.rng(1), 4)
+    with pytest.raises(Q.ArgumentError):
+        Q.evolve_layer_(psi, [Q.gate_from_matrix(u, [2, 3]), Q.gate_from_matrix(u, [3, 4])], maxdim=4)
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_truncated_gate_on_large_bond(precision):
     """A gate on a chi = 128 bond (theta 256 x 256: the mixed path's FP32-preconditioned SVD with
