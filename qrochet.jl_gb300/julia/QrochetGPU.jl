@@ -234,6 +234,25 @@ function Qrochet.evolve!(c::GPUChain, gate::Dense; threshold = nothing, maxdim =
     return c
 end
 
+# A brick-wall layer of two-site gates on disjoint site pairs, several at a time (the inner loop of
+# a TEBD evolve! over one layer); the result is that of evolve! on each gate in turn.
+function evolve_layer!(c::GPUChain, gates::AbstractVector{<:Dense}; threshold = nothing, maxdim = nothing,
+                       iscanonical = false, renormalize = false, lanes = 0)
+    sites = Cint[]
+    mats = ComplexF64[]
+    for gate in gates
+        ls = sort!(map(Qrochet.id, Qrochet.outputs(gate)))
+        (length(ls) == 2 && ls[2] == ls[1] + 1) || throw(ArgumentError("evolve_layer! takes two-site gates on contiguous lanes"))
+        push!(sites, ls[1] - 1)
+        append!(mats, vec(permutedims(ComplexF64.(gatematrix(gate, ls)))))  # row-major d^2 x d^2
+    end
+    check(ccall((:qr_evolve_layer, libqrochet), Cint,
+                (Ptr{Cvoid}, Cint, Ptr{Cint}, Ptr{ComplexF64}, Cdouble, Cint, Cint, Cint, Cint),
+                c.handle, length(sites), sites, mats, isnothing(threshold) ? NaN : Float64(threshold),
+                isnothing(maxdim) ? -1 : maxdim, iscanonical, renormalize, lanes))
+    return c
+end
+
 function Qrochet.overlap(a::GPUChain, b::GPUChain)
     out = Ref{ComplexF64}(0)
     check(ccall((:qr_overlap, libqrochet), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ref{ComplexF64}), a.handle, b.handle, out))
