@@ -244,7 +244,7 @@ function evolve_layer!(c::GPUChain, gates::AbstractVector{<:Dense}; threshold = 
         ls = sort!(map(Qrochet.id, Qrochet.outputs(gate)))
         (length(ls) == 2 && ls[2] == ls[1] + 1) || throw(ArgumentError("evolve_layer! takes two-site gates on contiguous lanes"))
         push!(sites, ls[1] - 1)
-        append!(mats, vec(permutedims(ComplexF64.(gatematrix(gate, ls)))))  # row-major d^2 x d^2
+        append!(mats, vec(ComplexF64.(gatematrix(gate, ls))))  # memory order as qr_evolve_2site takes it
     end
     check(ccall((:qr_evolve_layer, libqrochet), Cint,
                 (Ptr{Cvoid}, Cint, Ptr{Cint}, Ptr{ComplexF64}, Cdouble, Cint, Cint, Cint, Cint),
