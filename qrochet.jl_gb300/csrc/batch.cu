@@ -30,6 +30,7 @@
 #include <algorithm>
 #include "kernels.cuh"
 #include "jacobi_rot.cuh"
+#include "jacobi_df.cuh"
 
 namespace qr {
 namespace {
@@ -124,6 +125,118 @@ __device__ bool cta_sweeps(cplx_t<T>* __restrict__ B, cplx_t<T>* __restrict__ V,
     __syncthreads();
   }
   return converged;
+}
+
+// ---- the mixed finish in double-float (FP32 pairs, on the FP32 pipes) ----------------------------
+// One CTA's double-float Hestenes sweeps on B (Bh, Bl: rows x k, ld rows) accumulating V (Vh,
+// Vl: k x k, ld k): round-robin pairs, one warp per pair.  Every lane forms the pair's
+// compensated sums over its rows, the warp reduces them, and every lane derives the same rotation
+// from the broadcast sums (rotation_params_df), so a pair needs no shared memory; a CTA barrier
+// between rounds.  Stops after a sweep that rotates nothing or whose largest tangent is below
+// tan_stop; returns that verdict.
+__device__ bool cta_sweeps_df(float2* __restrict__ Bh, float2* __restrict__ Bl, float2* __restrict__ Vh,
+                              float2* __restrict__ Vl, int rows, int k, float tol, float smax, int max_sweeps,
+                              float tan_stop, unsigned* rot_count, unsigned* tmax_bits) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int np = k + (k & 1), npairs = np / 2;
+  bool converged = false;
+  for (int sweep = 0; sweep < max_sweeps && !converged; sweep++) {
+    if (threadIdx.x == 0) { *rot_count = 0u; *tmax_bits = 0u; }
+    __syncthreads();
+    for (int round = 0; round < np - 1; round++) {
+      for (int pair = warp; pair < npairs; pair += nw) {
+        int p, q;
+        if (pair == 0) { p = round; q = np - 1; }
+        else { p = (round + pair) % (np - 1); q = (round - pair + np - 1) % (np - 1); }
+        if (p > q) { const int x = p; p = q; q = x; }
+        if (q >= k) continue;
+        float2 *bph = Bh + (long)rows * p, *bpl = Bl + (long)rows * p;
+        float2 *bqh = Bh + (long)rows * q, *bql = Bl + (long)rows * q;
+        DotAcc a{0.f, 0.f}, b{0.f, 0.f}, gr{0.f, 0.f}, gi{0.f, 0.f};
+        for (int r = lane; r < rows; r += 32) df_dot_acc(bph[r], bpl[r], bqh[r], bql[r], a, b, gr, gi);
+        const dfl k4 = df_warp_sum4_t(dot_final(a), dot_final(b), dot_final(gr), dot_final(gi));
+        DfParams P;
+        if (!rotation_params_df(df_shfl(k4, 0), df_shfl(k4, 8), df_shfl(k4, 16), df_shfl(k4, 24), tol, smax, P))
+          continue;
+        for (int r = lane; r < rows; r += 32) {
+          float2 xh = bph[r], xl = bpl[r], yh = bqh[r], yl = bql[r];
+          df_rot_any(xh, xl, yh, yl, P);
+          bph[r] = xh; bpl[r] = xl; bqh[r] = yh; bql[r] = yl;
+        }
+        float2 *vph = Vh + (long)k * p, *vpl = Vl + (long)k * p;
+        float2 *vqh = Vh + (long)k * q, *vql = Vl + (long)k * q;
+        for (int r = lane; r < k; r += 32) {
+          float2 xh = vph[r], xl = vpl[r], yh = vqh[r], yl = vql[r];
+          df_rot_any(xh, xl, yh, yl, P);
+          vph[r] = xh; vpl[r] = xl; vqh[r] = yh; vql[r] = yl;
+        }
+        if (lane == 0) {
+          atomicAdd(rot_count, 1u);
+          atomicMax(tmax_bits, __float_as_uint(P.tabs));
+        }
+      }
+      __syncthreads();
+    }
+    converged = *rot_count == 0u || __uint_as_float(*tmax_bits) < tan_stop;
+    __syncthreads();
+  }
+  return converged;
+}
+
+// R = I - X^H X (FP32 values of compensated double-float sums), X = (Xh, Xl) k x k, ld k.
+__device__ void cta_gram_df(const float2* __restrict__ Xh, const float2* __restrict__ Xl, int k, float2* __restrict__ R) {
+  for (int t = threadIdx.x; t < k * k; t += blockDim.x) {
+    const int i = t % k, j = t / k;
+    DotAcc re{0.f, 0.f}, im{0.f, 0.f};
+    for (int x = 0; x < k; x++) {
+      const float2 ah = Xh[x + (long)k * i], al = Xl[x + (long)k * i];
+      const float2 bh = Xh[x + (long)k * j], bl = Xl[x + (long)k * j];
+      dot2_step(re, ah.x, al.x, bh.x, bl.x);  // conj(a) b
+      dot2_step(re, ah.y, al.y, bh.y, bl.y);
+      dot2_step(im, ah.x, al.x, bh.y, bl.y);
+      dot2_step(im, -ah.y, -al.y, bh.x, bl.x);
+    }
+    const dfl r = df_add({i == j ? 1.f : 0.f, 0.f}, df_neg(dot_final(re))), m = df_neg(dot_final(im));
+    R[t] = make_float2(r.h + r.l, m.h + m.l);
+  }
+}
+
+// Y = X + X_hi R / 2: FP32 products (|R| << 1), double-float sum; k x k, ld k.
+__device__ void cta_ns_update(const float2* __restrict__ Xh, const float2* __restrict__ Xl, const float2* __restrict__ R,
+                              int k, float2* __restrict__ Yh, float2* __restrict__ Yl) {
+  for (int t = threadIdx.x; t < k * k; t += blockDim.x) {
+    const int i = t % k, j = t / k;
+    float ar = 0.f, ai = 0.f;
+    for (int x = 0; x < k; x++) {
+      const float2 a = Xh[i + (long)k * x], r = R[x + (long)k * j];
+      ar = fmaf(a.x, r.x, fmaf(-a.y, r.y, ar));
+      ai = fmaf(a.x, r.y, fmaf(a.y, r.x, ai));
+    }
+    const dfl yr = df_add_f({Xh[t].x, Xl[t].x}, 0.5f * ar), yi = df_add_f({Xh[t].y, Xl[t].y}, 0.5f * ai);
+    Yh[t] = make_float2(yr.h, yi.h);
+    Yl[t] = make_float2(yr.l, yi.l);
+  }
+}
+
+// C = A X in double-float: A (Ah, Al) rows x k (ld rows), X (Xh, Xl) k x k, C rows x k (ld rows).
+__device__ void cta_gemm_df(const float2* __restrict__ Ah, const float2* __restrict__ Al, int rows,
+                            const float2* __restrict__ Xh, const float2* __restrict__ Xl, int k, float2* __restrict__ Ch,
+                            float2* __restrict__ Cl) {
+  for (int t = threadIdx.x; t < rows * k; t += blockDim.x) {
+    const int i = t % rows, j = t / rows;
+    DotAcc re{0.f, 0.f}, im{0.f, 0.f};
+    for (int x = 0; x < k; x++) {
+      const float2 ah = Ah[i + (long)rows * x], al = Al[i + (long)rows * x];
+      const float2 bh = Xh[x + (long)k * j], bl = Xl[x + (long)k * j];
+      dot2_step(re, ah.x, al.x, bh.x, bl.x);
+      dot2_step(re, -ah.y, -al.y, bh.y, bl.y);
+      dot2_step(im, ah.x, al.x, bh.y, bl.y);
+      dot2_step(im, ah.y, al.y, bh.x, bl.x);
+    }
+    const dfl r = dot_final(re), m = dot_final(im);
+    Ch[t] = make_float2(r.h, m.h);
+    Cl[t] = make_float2(r.l, m.l);
+  }
 }
 
 // One CTA per task (strided over the layer's tasks).  ws: BT_SLOT double2 per CTA.  dry = 1 runs
@@ -230,37 +343,56 @@ __global__ void __launch_bounds__(512, 1)
       __syncthreads();
       const float tol32 = fmaxf(4e-6f, 2.f * sqrtf((float)rows) * Eps<float>::v);
       cta_sweeps<float>(B32, V32, rows, k, tol32, (float)smax, 20, 0.15f, &rot_count, &tmax_bits);
-      for (int t = tid; t < k * k; t += blockDim.x) V[t] = make_double2((double)V32[t].x, (double)V32[t].y);
+      // the finish in double-float on the FP32 pipes.  The CTA's four slot regions (B, V, W, Tm;
+      // 2 BT_MAXK^2 float2 each) hold, phase by phase:
+      //   W: B32 | V32 -> theta (hi | lo) -> X (hi | lo) before the conversion back
+      //   Tm: X0 (hi | lo) -> R2 | X2 hi
+      //   V: R1 | X1 hi -> B' (hi | lo) -> V (FP64)
+      //   B: theta (FP64) -> X1 lo | X2 lo -> B (FP64)
+      constexpr size_t H = (size_t)BT_MAXK * BT_MAXK;  // float2 per half region
+      float2 *rW = reinterpret_cast<float2*>(W), *rT = reinterpret_cast<float2*>(Tm);
+      float2 *rV = reinterpret_cast<float2*>(V), *rB = reinterpret_cast<float2*>(B);
+      for (int t = tid; t < k * k; t += blockDim.x) { rT[t] = V32[t]; rT[H + t] = make_float2(0.f, 0.f); }
       __syncthreads();
-      // Tm = I - X^H X, then W = X + X Tm / 2 -> V
-      for (int t = tid; t < k * k; t += blockDim.x) {
-        const int i = t % k, j = t / k;
-        double2 acc = make_double2(i == j ? 1.0 : 0.0, 0.0);
-        for (int x = 0; x < k; x++) acc = csub(acc, cmulc(V[x + (long)k * i], V[x + (long)k * j]));
-        Tm[t] = acc;
-      }
-      __syncthreads();
-      for (int t = tid; t < k * k; t += blockDim.x) {
-        const int i = t % k, j = t / k;
-        double2 acc = make_double2(0.0, 0.0);
-        for (int x = 0; x < k; x++) acc = cadd(acc, zmul(V[i + (long)k * x], Tm[x + (long)k * j]));
-        W[t] = cadd(V[t], cscale(acc, 0.5));
-      }
-      __syncthreads();
-      for (int t = tid; t < k * k; t += blockDim.x) V[t] = W[t];
-      __syncthreads();
-      // B <- B X
       for (int t = tid; t < rows * k; t += blockDim.x) {
-        const int i = t % rows, j = t / rows;
-        double2 acc = make_double2(0.0, 0.0);
-        for (int x = 0; x < k; x++) acc = cadd(acc, zmul(B[i + (long)rows * x], V[x + (long)k * j]));
-        Tm[t] = acc;
+        const dfl re = df_from(B[t].x), im = df_from(B[t].y);
+        rW[t] = make_float2(re.h, im.h);
+        rW[H + t] = make_float2(re.l, im.l);
       }
       __syncthreads();
-      for (int t = tid; t < rows * k; t += blockDim.x) B[t] = Tm[t];
+      // two Newton-Schulz steps X <- X + X (I - X^H X) / 2 (1e-6 -> 1e-12 -> rounding)
+      cta_gram_df(rT, rT + H, k, rV);
+      __syncthreads();
+      cta_ns_update(rT, rT + H, rV, k, rV + H, rB);
+      __syncthreads();
+      cta_gram_df(rV + H, rB, k, rT);
+      __syncthreads();
+      cta_ns_update(rV + H, rB, rT, k, rT + H, rB + H);
+      __syncthreads();
+      float2 *Xh = rT + H, *Xl = rB + H;
+      // B' = theta X into V's region, then the double-float sweeps on (B', X)
+      cta_gemm_df(rW, rW + H, rows, Xh, Xl, k, rV, rV + H);
+      __syncthreads();
+      const float toldf = (float)(32.0 * sqrt((double)rows) * Eps<double>::v);
+      const bool conv_df = cta_sweeps_df(rV, rV + H, Xh, Xl, rows, k, toldf, (float)smax, BT_MAX_SWEEPS, 1e-7f,
+                                         &rot_count, &tmax_bits);
+      if (!conv_df && tid == 0) atomicExch(T.status, (int)QR_ENOCONV);
+      // back to FP64: X into W first (its lo part sits in B's region), then B, then V
+      for (int t = tid; t < k * k; t += blockDim.x) { rW[t] = Xh[t]; rW[H + t] = Xl[t]; }
+      __syncthreads();
+      for (int t = tid; t < rows * k; t += blockDim.x) {
+        const float2 h = rV[t], l = rV[H + t];
+        B[t] = make_double2((double)h.x + l.x, (double)h.y + l.y);
+      }
+      __syncthreads();
+      for (int t = tid; t < k * k; t += blockDim.x) {
+        const float2 h = rW[t], l = rW[H + t];
+        V[t] = make_double2((double)h.x + l.x, (double)h.y + l.y);
+      }
       __syncthreads();
     }
-    const bool converged = cta_sweeps<double>(B, V, rows, k, tol, smax, BT_MAX_SWEEPS, 1e-8f, &rot_count, &tmax_bits);
+    const bool converged = (MIXED && k > BT_MIXED_MIN) ||
+                           cta_sweeps<double>(B, V, rows, k, tol, smax, BT_MAX_SWEEPS, 1e-8f, &rot_count, &tmax_bits);
     if (!converged && tid == 0) atomicExch(T.status, (int)QR_ENOCONV);
 
     // ---- sigma, descending order (ties by index), truncation on the device
