@@ -12,7 +12,7 @@
 //     threshold) is taken on the device, so no layer waits for the host;
 //   - one CTA runs one whole gate step: theta = A_l diag(Lambda) A_r, the gate, a one-sided
 //     Jacobi SVD (theta of at most 128 x 128: chi_max <= 64; FP64, or with QR_MIXED FP32 sweeps
-//     first and FP64 sweeps to finish), the sort, the truncation,
+//     first and a double-float finish on the FP32 pipes), the sort, the truncation,
 //     re-orthonormalisation of the kept vectors when their singular values fall below 1e-3
 //     sigma_max (classical Gram-Schmidt twice), and the write-back of U, Vh and Lambda.  A
 //     layer's gates sit on disjoint bonds, so the CTAs of one launch never touch the same site;
@@ -242,9 +242,10 @@ __device__ void cta_gemm_df(const float2* __restrict__ Ah, const float2* __restr
 // One CTA per task (strided over the layer's tasks).  ws: BT_SLOT double2 per CTA.  dry = 1 runs
 // the arithmetic without writing the chain (the autotuner's timing runs).  MIXED: above
 // BT_MIXED_MIN columns the SVD first runs FP32 sweeps on a copy of theta (64x the FP64 rate on
-// this part), makes their rotations unitary to ~1e-12 with one FP64 Newton-Schulz step
-// X <- X + X (I - X^H X) / 2, forms B = theta X in FP64 and lets the FP64 sweeps finish from
-// couplings of ~1e-6 (two or three sweeps instead of eight to ten).
+// this part), then finishes in double-float on the FP32 pipes: two Newton-Schulz steps
+// X <- X + X (I - X^H X) / 2 make the rotations unitary to rounding, B = theta X is formed with
+// compensated products, and double-float sweeps (cta_sweeps_df) finish from couplings of ~1e-6
+// in two or three sweeps.  The FP64 finish this replaces kept the FP64 pipe 76 % busy.
 template <bool MIXED>
 __global__ void __launch_bounds__(512, 1)
     batch_gate_k(const BTask* __restrict__ tasks, int ntasks, double2* __restrict__ ws, int dry) {
