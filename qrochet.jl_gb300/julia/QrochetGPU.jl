@@ -15,7 +15,7 @@ using Qrochet: Chain, Site, Dense, Open, State, MissingSchmidtCoefficientsExcept
 const libqrochet = get(ENV, "QROCHET_GPU_LIB", joinpath(@__DIR__, "..", "lib", "libqrochet_gpu.so"))
 
 const QR_OK, QR_EINVAL, QR_EASSERT, QR_ENO_SCHMIDT, QR_EDIM = 0, 1, 2, 3, 4
-const QR_FP64, QR_MIXED = 0, 1
+const QR_FP64, QR_MIXED, QR_SPLIT_CONTRACT = 0, 1, 2
 const QR_DIR_LEFT, QR_DIR_RIGHT = 0, 1
 const QR_METHOD_QR, QR_METHOD_SVD = 0, 1
 
@@ -76,9 +76,16 @@ function GPUChain(arrays::Vector{<:AbstractArray}; order = (:o, :l, :r), precisi
     return chain
 end
 
-setprecision!(c::GPUChain, p::Symbol) =
-    check(ccall((:qr_chain_set_precision, libqrochet), Cint, (Ptr{Cvoid}, Cint), c.handle,
-                p === :mixed ? QR_MIXED : QR_FP64))
+# :fp64 (all ComplexF64), :mixed (the mixed-precision SVD and theta GEMM of two-site gates),
+# :split (environment contractions on the tensor cores as BF16x3 products), :mixed_split (both)
+const PRECISIONS = Dict(:fp64 => QR_FP64, :mixed => QR_MIXED, :split => QR_SPLIT_CONTRACT,
+                        :mixed_split => QR_MIXED | QR_SPLIT_CONTRACT)
+
+function setprecision!(c::GPUChain, p::Symbol)
+    haskey(PRECISIONS, p) || throw(ArgumentError("Unknown precision=:$p"))
+    check(ccall((:qr_chain_set_precision, libqrochet), Cint, (Ptr{Cvoid}, Cint), c.handle, PRECISIONS[p]))
+    return c
+end
 
 function Base.copy(c::GPUChain)
     h = Ref{Ptr{Cvoid}}(C_NULL)
