@@ -45,10 +45,11 @@ typedef struct qr_mpo qr_mpo;     /* one open-boundary MPO resident in device me
 #define QR_EASSERT 2      /* AssertionError (@assert) */
 #define QR_ENO_SCHMIDT 3  /* MissingSchmidtCoefficientsException (src/Ansatz.jl:91-99) */
 #define QR_EDIM 4         /* DimensionMismatch */
-#define QR_ENOMEM 5       /* device allocation failed */
+#define QR_ENOMEM 5       /* device or host allocation failed */
 #define QR_ECUDA 6        /* CUDA runtime error */
 #define QR_ENODEV 7       /* no CUDA device */
 #define QR_ENOCONV 8      /* SVD sweeps did not converge */
+#define QR_EHOST 9        /* other host-side failure (a worker thread that could not start) */
 
 /* Precision of a chain's arithmetic (qr_chain_set_precision), a bit mask. */
 #define QR_FP64 0           /* plain: all ComplexF64 */

@@ -54,6 +54,11 @@ int qr_test_svd_paths(uint64_t* counts, int n, int* total);
 int qr_test_schedule_pairs(const unsigned* mask, const unsigned* flag, int nv, int use_flag, unsigned* items,
                            unsigned* ord, long* listed, int* classes);
 int qr_test_qr(int m, int n, const double* A, double* Q, double* R, double* ms);
+/* Throws a C++ exception inside an exported function (kind 0: std::bad_alloc, 1: a standard
+   std::runtime_error, 2: an object of no standard type) so that a test sees the ABI guard turn it
+   into a status (QR_ENOMEM, QR_EHOST, QR_EHOST) and a message; any other kind returns QR_OK.
+   Host only: no GPU needed. */
+int qr_test_host_exception(int kind);
 
 #ifdef __cplusplus
 }

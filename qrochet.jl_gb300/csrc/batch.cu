@@ -741,30 +741,30 @@ int autotune(qr_batch* bt, cudaStream_t s, int chi, int slots, double2* ws) {
 
 extern "C" {
 
-int qr_batch_create(int device, qr_batch** out) {
+int qr_batch_create(int device, qr_batch** out) try {
   if (!out) return fail(QR_EINVAL, "null output");
   qr_batch* b = new qr_batch();
   b->device = device;
   *out = b;
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_batch_set_precision(qr_batch* b, int mode) {
+int qr_batch_set_precision(qr_batch* b, int mode) try {
   if (!b) return fail(QR_EINVAL, "null batch");
   if (b->ran) return fail(QR_EINVAL, "the batch has already run");
   if (mode < 0 || mode > 3) return fail(QR_EINVAL, "bad precision");
   b->precision = mode;
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_batch_free(qr_batch* b) {
+int qr_batch_free(qr_batch* b) try {
   delete b;
   return QR_OK;
-}
+} QR_ABI_CATCH
 
 int qr_batch_add(qr_batch* bt, int n, int chi_max, double threshold, int ngates, const int* gate_site,
                  const double* gate_mats, int nobs, const int* obs_weight, const int* obs_sites, const int* obs_paulis,
-                 int* id) {
+                 int* id) try {
   if (!bt || !id) return fail(QR_EINVAL, "null argument");
   if (bt->ran) return fail(QR_EINVAL, "the batch has already run");
   if (n < 2 || chi_max < 1) return fail(QR_EINVAL, "a request needs n >= 2 sites and chi_max >= 1");
@@ -806,10 +806,10 @@ int qr_batch_add(qr_batch* bt, int n, int chi_max, double threshold, int ngates,
   bt->reqs.push_back(std::move(r));
   *id = (int)bt->reqs.size() - 1;
   return QR_OK;
-}
+} QR_ABI_CATCH
 
 // layer index of every gate of request `id` (host-side schedule; no device needed)
-int qr_batch_plan(const qr_batch* bt, int id, int* layer_of_gate, int* nlayers) {
+int qr_batch_plan(const qr_batch* bt, int id, int* layer_of_gate, int* nlayers) try {
   if (!bt || id < 0 || id >= (int)bt->reqs.size()) return fail(QR_EINVAL, "bad batch request id");
   const BReq& r = bt->reqs[id];
   int mx = -1;
@@ -819,9 +819,9 @@ int qr_batch_plan(const qr_batch* bt, int id, int* layer_of_gate, int* nlayers) 
   }
   if (nlayers) *nlayers = mx + 1;
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_batch_run(qr_batch* bt, double* ms) {
+int qr_batch_run(qr_batch* bt, double* ms) try {
   if (!bt) return fail(QR_EINVAL, "null batch");
   if (bt->ran) return fail(QR_EINVAL, "the batch has already run");
   if (bt->reqs.empty()) return fail(QR_EINVAL, "empty batch");
@@ -1047,9 +1047,9 @@ int qr_batch_run(qr_batch* bt, double* ms) {
   }
   bt->ran = true;
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_batch_result(const qr_batch* bt, int id, int* status, double* values) {
+int qr_batch_result(const qr_batch* bt, int id, int* status, double* values) try {
   if (!bt || id < 0 || id >= (int)bt->reqs.size()) return fail(QR_EINVAL, "bad batch request id");
   if (!bt->ran) return fail(QR_EINVAL, "the batch has not run");
   const BReq& r = bt->reqs[id];
@@ -1060,17 +1060,17 @@ int qr_batch_result(const qr_batch* bt, int id, int* status, double* values) {
       values[2 * j + 1] = r.values[j].y;
     }
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_batch_bond_dims(const qr_batch* bt, int id, int* out) {
+int qr_batch_bond_dims(const qr_batch* bt, int id, int* out) try {
   if (!bt || id < 0 || id >= (int)bt->reqs.size()) return fail(QR_EINVAL, "bad batch request id");
   if (!bt->ran) return fail(QR_EINVAL, "the batch has not run");
   const BReq& r = bt->reqs[id];
   for (int b = 0; b < r.n - 1; b++) out[b] = r.bd[b];
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_batch_lambda(const qr_batch* bt, int id, int bond, double* out, int* len) {
+int qr_batch_lambda(const qr_batch* bt, int id, int bond, double* out, int* len) try {
   if (!bt || id < 0 || id >= (int)bt->reqs.size()) return fail(QR_EINVAL, "bad batch request id");
   if (!bt->ran) return fail(QR_EINVAL, "the batch has not run");
   const BReq& r = bt->reqs[id];
@@ -1079,12 +1079,12 @@ int qr_batch_lambda(const qr_batch* bt, int id, int bond, double* out, int* len)
   if (out)
     for (size_t j = 0; j < r.lam[bond].size(); j++) out[j] = r.lam[bond][j];
   return QR_OK;
-}
+} QR_ABI_CATCH
 
 // layers, kernel launches in the graph, graph nodes, warps per CTA chosen, 1 if the choice came
 // from the tuning cache, graph time (ms), autotuning time (ms)
 int qr_batch_info(const qr_batch* bt, int* layers, int* launches, int* graph_nodes, int* warps, int* cached,
-                  double* run_ms, double* tune_ms) {
+                  double* run_ms, double* tune_ms) try {
   if (!bt) return fail(QR_EINVAL, "null batch");
   if (layers) *layers = bt->layers;
   if (launches) *launches = bt->launches;
@@ -1094,6 +1094,6 @@ int qr_batch_info(const qr_batch* bt, int* layers, int* launches, int* graph_nod
   if (run_ms) *run_ms = bt->run_ms;
   if (tune_ms) *tune_ms = bt->tune_ms;
   return QR_OK;
-}
+} QR_ABI_CATCH
 
 }  // extern "C"

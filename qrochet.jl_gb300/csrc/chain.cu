@@ -20,6 +20,7 @@
 #include <map>
 #include <tuple>
 #include <thread>
+#include <system_error>
 #include "kernels.cuh"
 
 namespace qr {
@@ -860,45 +861,45 @@ extern "C" {
 
 const char* qr_last_error_string(void) { return t_err.c_str(); }
 
-int qr_version(int* major, int* minor) {
+int qr_version(int* major, int* minor) try {
   if (major) *major = 0;
   if (minor) *minor = 1;
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_device_count(int* count) {
+int qr_device_count(int* count) try {
   int c = 0;
   cudaError_t e = cudaGetDeviceCount(&c);
   if (count) *count = (e == cudaSuccess) ? c : 0;
   if (e != cudaSuccess) return cuda_fail(e, "cudaGetDeviceCount");
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_set_device(int device) {
+int qr_set_device(int device) try {
   QR_CUDA(cudaSetDevice(device));
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_launch_count(uint64_t* count) {
+int qr_launch_count(uint64_t* count) try {
   if (count) *count = g_launches.load();
   return QR_OK;
-}
+} QR_ABI_CATCH
 
 static int chain_create(int n, int d, const int* bond_dims, bool periodic, qr_chain** out);
 
-int qr_chain_create(int n, int d, const int* bond_dims, qr_chain** out) {
+int qr_chain_create(int n, int d, const int* bond_dims, qr_chain** out) try {
   return chain_create(n, d, bond_dims, false, out);
-}
+} QR_ABI_CATCH
 
-int qr_chain_create_periodic(int n, int d, const int* bond_dims, qr_chain** out) {
+int qr_chain_create_periodic(int n, int d, const int* bond_dims, qr_chain** out) try {
   return chain_create(n, d, bond_dims, true, out);
-}
+} QR_ABI_CATCH
 
-int qr_chain_boundary(const qr_chain* h, int* periodic) {
+int qr_chain_boundary(const qr_chain* h, int* periodic) try {
   if (!h || !periodic) return fail(QR_EINVAL, "null argument");
   *periodic = h->periodic ? 1 : 0;
   return QR_OK;
-}
+} QR_ABI_CATCH
 
 static int chain_create(int n, int d, const int* bond_dims, bool periodic, qr_chain** out) {
   if (!out) return fail(QR_EINVAL, "null output");
@@ -934,7 +935,7 @@ static int chain_create(int n, int d, const int* bond_dims, bool periodic, qr_ch
   return QR_OK;
 }
 
-int qr_chain_free(qr_chain* h) {
+int qr_chain_free(qr_chain* h) try {
   if (!h) return QR_OK;
   cudaStreamSynchronize(h->stream);
   for (qr_chain* l : h->lanes) qr_chain_free(l);
@@ -951,9 +952,9 @@ int qr_chain_free(qr_chain* h) {
   cudaStreamDestroy(h->stream);
   delete h;
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_chain_copy(const qr_chain* src, qr_chain** out) {
+int qr_chain_copy(const qr_chain* src, qr_chain** out) try {
   if (!src || !out) return fail(QR_EINVAL, "null chain");
   QR_CUDA(cudaStreamSynchronize(src->stream));
   QR_TRY(chain_create(src->n, src->d, src->bd.data(), src->periodic, out));
@@ -964,9 +965,9 @@ int qr_chain_copy(const qr_chain* src, qr_chain** out) {
   for (int b = 0; b < src->n - 1; b++)
     if (src->lam[b]) QR_TRY(put_lambda(h, b, src->lam[b], src->lamlen[b]));
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_chain_upload_site(qr_chain* h, int site, const double* host, const char* order) {
+int qr_chain_upload_site(qr_chain* h, int site, const double* host, const char* order) try {
   QR_TRY(check_site(h, site));
   if (!host) return fail(QR_EINVAL, "null host array");
   if (!is_perm(order ? order : "", "olr")) return fail(QR_EINVAL, "order must be a permutation of (o, l, r)");
@@ -979,9 +980,9 @@ int qr_chain_upload_site(qr_chain* h, int site, const double* host, const char* 
   QR_TRY(zpermute(h->stream, h->ws, h->site[site], p));
   QR_CUDA(cudaStreamSynchronize(h->stream));
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_chain_download_site(const qr_chain* hc, int site, double* host, const char* order) {
+int qr_chain_download_site(const qr_chain* hc, int site, double* host, const char* order) try {
   qr_chain* h = const_cast<qr_chain*>(hc);
   QR_TRY(check_site(h, site));
   if (!host) return fail(QR_EINVAL, "null host array");
@@ -1004,7 +1005,7 @@ int qr_chain_download_site(const qr_chain* hc, int site, double* host, const cha
   QR_CUDA(cudaMemcpyAsync(host, h->ws, sizeof(double2) * ne, cudaMemcpyDeviceToHost, h->stream));
   QR_CUDA(cudaStreamSynchronize(h->stream));
   return QR_OK;
-}
+} QR_ABI_CATCH
 
 // ---- rand(Chain, Open, State / Operator) on the device ---------------------------------------
 // Bond dimensions follow the reference's sampler (src/Ansatz/Chain.jl:223-297): site i (1-based)
@@ -1029,7 +1030,7 @@ void sampler_dims(int n, long p, long chi, int i, long& l, long& r) {
 }
 }  // namespace
 
-int qr_chain_random(int n, int d, int chi, uint64_t seed, int complex_entries, qr_chain** out) {
+int qr_chain_random(int n, int d, int chi, uint64_t seed, int complex_entries, qr_chain** out) try {
   if (!out) return fail(QR_EINVAL, "null output");
   *out = nullptr;
   if (n < 2 || d < 2 || chi < d) return fail(QR_EINVAL, "rand(Chain, Open, State) needs n >= 2, p >= 2 and chi >= p");
@@ -1081,9 +1082,9 @@ int qr_chain_random(int n, int d, int chi, uint64_t seed, int complex_entries, q
   }
   *out = h;
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_mpo_random(int n, int d, int chi, uint64_t seed, int complex_entries, qr_mpo** out) {
+int qr_mpo_random(int n, int d, int chi, uint64_t seed, int complex_entries, qr_mpo** out) try {
   if (!out) return fail(QR_EINVAL, "null output");
   *out = nullptr;
   if (n < 2 || d < 2 || chi < 1) return fail(QR_EINVAL, "rand(Chain, Open, Operator) needs n >= 2, p >= 2 and chi >= 1");
@@ -1139,7 +1140,7 @@ int qr_mpo_random(int n, int d, int chi, uint64_t seed, int complex_entries, qr_
   }
   *out = w;
   return QR_OK;
-}
+} QR_ABI_CATCH
 
 // ---- checkpoint / export ---------------------------------------------------------------------
 // File layout (little-endian), written so a Julia reader can rebuild MPS(arrays) / pMPS(arrays):
@@ -1157,7 +1158,7 @@ struct FileCloser {
 };
 }  // namespace
 
-int qr_chain_save(const qr_chain* h, const char* path) {
+int qr_chain_save(const qr_chain* h, const char* path) try {
   if (!h || !path) return fail(QR_EINVAL, "null argument");
   FileCloser fc{fopen(path, "wb")};
   if (!fc.f) return fail(QR_EINVAL, std::string("cannot open for writing: ") + path);
@@ -1183,9 +1184,9 @@ int qr_chain_save(const qr_chain* h, const char* path) {
   }
   if (!ok) return fail(QR_EINVAL, std::string("write failed: ") + path);
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_chain_load(const char* path, qr_chain** out) {
+int qr_chain_load(const char* path, qr_chain** out) try {
   if (!path || !out) return fail(QR_EINVAL, "null argument");
   *out = nullptr;
   FileCloser fc{fopen(path, "rb")};
@@ -1226,29 +1227,29 @@ int qr_chain_load(const char* path, qr_chain** out) {
   }
   *out = h;
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_chain_site_dims(const qr_chain* h, int site, int* chi_l, int* d, int* chi_r) {
+int qr_chain_site_dims(const qr_chain* h, int site, int* chi_l, int* d, int* chi_r) try {
   QR_TRY(check_site(h, site));
   if (chi_l) *chi_l = h->cl(site);
   if (d) *d = h->d;
   if (chi_r) *chi_r = h->cr(site);
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_chain_bond_dims(const qr_chain* h, int* out) {
+int qr_chain_bond_dims(const qr_chain* h, int* out) try {
   if (!h || !out) return fail(QR_EINVAL, "null argument");
   for (int b = 0; b < (int)h->bd.size(); b++) out[b] = h->bd[b];
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_chain_has_lambda(const qr_chain* h, int bond, int* flag) {
+int qr_chain_has_lambda(const qr_chain* h, int bond, int* flag) try {
   if (!h || !flag || bond < 0 || bond >= h->n - 1) return fail(QR_EINVAL, "Invalid bond");
   *flag = h->lam[bond] != nullptr;
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_chain_get_lambda(const qr_chain* h, int bond, double* out, int* len) {
+int qr_chain_get_lambda(const qr_chain* h, int bond, double* out, int* len) try {
   if (!h || bond < 0 || bond >= h->n - 1) return fail(QR_EINVAL, "Invalid bond");
   if (!h->lam[bond]) {
     if (len) *len = 0;
@@ -1260,9 +1261,9 @@ int qr_chain_get_lambda(const qr_chain* h, int bond, double* out, int* len) {
     QR_CUDA(cudaStreamSynchronize(h->stream));
   }
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_chain_set_lambda(qr_chain* h, int bond, const double* lam, int len) {
+int qr_chain_set_lambda(qr_chain* h, int bond, const double* lam, int len) try {
   if (!h || bond < 0 || bond >= h->n - 1) return fail(QR_EINVAL, "Invalid bond");
   if (!lam) { drop_lambda(h, bond); return QR_OK; }
   if (len != h->bd[bond]) return fail(QR_EDIM, "Lambda length must equal the bond dimension");
@@ -1274,56 +1275,56 @@ int qr_chain_set_lambda(qr_chain* h, int bond, const double* lam, int len) {
   h->lam[bond] = p;
   h->lamlen[bond] = len;
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_chain_ntensors(const qr_chain* h, int* out) {
+int qr_chain_ntensors(const qr_chain* h, int* out) try {
   if (!h || !out) return fail(QR_EINVAL, "null argument");
   int c = h->n;
   for (auto p : h->lam) c += (p != nullptr);
   *out = c;
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_chain_nsites(const qr_chain* h, int* out) {
+int qr_chain_nsites(const qr_chain* h, int* out) try {
   if (!h || !out) return fail(QR_EINVAL, "null argument");
   *out = h->n;
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_chain_set_precision(qr_chain* h, int mode) {
+int qr_chain_set_precision(qr_chain* h, int mode) try {
   if (!h) return fail(QR_EINVAL, "null chain");
   if (mode < 0 || mode > (QR_MIXED | QR_SPLIT_CONTRACT))
     return fail(QR_EINVAL, "precision must be a combination of QR_MIXED and QR_SPLIT_CONTRACT");
   h->precision = mode;
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_chain_get_precision(const qr_chain* h, int* mode) {
+int qr_chain_get_precision(const qr_chain* h, int* mode) try {
   if (!h || !mode) return fail(QR_EINVAL, "null argument");
   *mode = h->precision;
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_chain_stream(const qr_chain* h, void** stream) {
+int qr_chain_stream(const qr_chain* h, void** stream) try {
   if (!h || !stream) return fail(QR_EINVAL, "null argument");
   *stream = (void*)h->stream;
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_chain_sync(const qr_chain* h) {
+int qr_chain_sync(const qr_chain* h) try {
   if (!h) return fail(QR_EINVAL, "null chain");
   QR_CUDA(cudaStreamSynchronize(h->stream));
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_canonize_site(qr_chain* h, int site, int direction, int method) {
+int qr_canonize_site(qr_chain* h, int site, int direction, int method) try {
   QR_TRY(canonize_site_impl(h, site, direction, method));
   QR_CUDA(cudaStreamSynchronize(h->stream));
   return QR_OK;
-}
+} QR_ABI_CATCH
 
 // canonize! (Chain.jl:469-497)
-int qr_canonize(qr_chain* h) {
+int qr_canonize(qr_chain* h) try {
   if (!h) return fail(QR_EINVAL, "null chain");
   const int n = h->n;
   for (int i = n - 1; i >= 1; i--) QR_TRY(canonize_site_impl(h, i, QR_DIR_LEFT, QR_METHOD_QR));
@@ -1345,22 +1346,22 @@ int qr_canonize(qr_chain* h) {
   }
   QR_CUDA(cudaStreamSynchronize(h->stream));
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_mixed_canonize(qr_chain* h, int center) {
+int qr_mixed_canonize(qr_chain* h, int center) try {
   QR_TRY(mixed_canonize_impl(h, center));
   QR_CUDA(cudaStreamSynchronize(h->stream));
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_normalize(qr_chain* h, int root) {
+int qr_normalize(qr_chain* h, int root) try {
   QR_TRY(normalize_impl(h, root));
   QR_CUDA(cudaStreamSynchronize(h->stream));
   return QR_OK;
-}
+} QR_ABI_CATCH
 
 // contract!(::Chain, Val(:between)) (Chain.jl:309-333)
-int qr_contract_between(qr_chain* h, int site1, int site2, int direction, int delete_lambda) {
+int qr_contract_between(qr_chain* h, int site1, int site2, int direction, int delete_lambda) try {
   QR_TRY(check_site(h, site1));
   QR_TRY(check_site(h, site2));
   if (site2 != site1 + 1) return fail(QR_EINVAL, "sites must be adjacent");
@@ -1377,9 +1378,9 @@ int qr_contract_between(qr_chain* h, int site1, int site2, int direction, int de
   if (delete_lambda) drop_lambda(h, b);
   QR_CUDA(cudaStreamSynchronize(h->stream));
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_canonicality_error(const qr_chain* hc, int site, int direction, double* err) {
+int qr_canonicality_error(const qr_chain* hc, int site, int direction, double* err) try {
   qr_chain* h = const_cast<qr_chain*>(hc);
   QR_TRY(check_site(h, site));
   if (!err) return fail(QR_EINVAL, "null output");
@@ -1398,16 +1399,16 @@ int qr_canonicality_error(const qr_chain* hc, int site, int direction, double* e
   QR_CUDA(cudaMemcpyAsync(err, h->scal, sizeof(double), cudaMemcpyDeviceToHost, s));
   QR_CUDA(cudaStreamSynchronize(s));
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_truncate(qr_chain* h, int site1, int site2, double threshold, int maxdim) {
+int qr_truncate(qr_chain* h, int site1, int site2, double threshold, int maxdim) try {
   QR_TRY(truncate_impl(h, site1, site2, threshold, maxdim));
   QR_CUDA(cudaStreamSynchronize(h->stream));
   return QR_OK;
-}
+} QR_ABI_CATCH
 
 // evolve_1site! (Chain.jl:586-603)
-int qr_evolve_1site(qr_chain* h, int site, const double* gate) {
+int qr_evolve_1site(qr_chain* h, int site, const double* gate) try {
   QR_TRY(check_site(h, site));
   if (!gate) return fail(QR_EINVAL, "null gate");
   QR_TRY(require_nonempty(h));
@@ -1415,15 +1416,15 @@ int qr_evolve_1site(qr_chain* h, int site, const double* gate) {
   QR_TRY(zgate1(h->stream, h->site[site], h->cl(site), h->d, h->cr(site), h->gate));
   QR_CUDA(cudaStreamSynchronize(h->stream));
   return QR_OK;
-}
+} QR_ABI_CATCH
 
 int qr_evolve_2site(qr_chain* h, int site_l, const double* gate, double threshold, int maxdim, int iscanonical,
-                    int renormalize) {
+                    int renormalize) try {
   if (!gate) return fail(QR_EINVAL, "null gate");
   QR_TRY(evolve2_impl(h, site_l, gate, threshold, maxdim, iscanonical, renormalize));
   QR_CUDA(cudaStreamSynchronize(h->stream));
   return QR_OK;
-}
+} QR_ABI_CATCH
 
 // A brick-wall layer of two-site gates on disjoint site pairs, several gates at a time.
 // A gate on sites (s, s + 1) writes sites s and s + 1, bond s and its Lambda, and reads only bonds
@@ -1434,7 +1435,7 @@ int qr_evolve_2site(qr_chain* h, int site_l, const double* gate, double threshol
 // per lane runs its gates through evolve2_impl, and the entries each gate wrote are copied back.
 // renormalize=true sweeps the whole chain per gate (normalize!), so that case runs in order.
 int qr_evolve_layer(qr_chain* h, int ngates, const int* sites, const double* gates, double threshold, int maxdim,
-                    int iscanonical, int renormalize, int lanes) {
+                    int iscanonical, int renormalize, int lanes) try {
   if (!h) return fail(QR_EINVAL, "null chain");
   if (ngates < 0 || (ngates > 0 && (!sites || !gates))) return fail(QR_EINVAL, "bad gate list");
   const int g4 = 2 * h->d * h->d * h->d * h->d;  // doubles per gate matrix
@@ -1478,18 +1479,29 @@ int qr_evolve_layer(qr_chain* h, int ngates, const int* sites, const double* gat
   }
   std::vector<int> rcs(L, QR_OK);
   std::vector<std::string> msgs(L);
-  std::vector<std::thread> th;
-  for (int j = 0; j < L; j++)
-    th.emplace_back([&, j]() {
-      qr_chain* l = h->lanes[j];
-      int rc = cuda_ok(cudaSetDevice(dev), "cudaSetDevice");
+  auto run_lane = [&](int j) {
+    qr_chain* l = h->lanes[j];
+    int rc = cuda_ok(cudaSetDevice(dev), "cudaSetDevice");
+    try {
       for (int i = j; i < ngates && !rc; i += L)
         rc = evolve2_impl(l, sites[i], gates + (size_t)g4 * i, threshold, maxdim, iscanonical, 0);
-      if (!rc) rc = cuda_ok(cudaStreamSynchronize(l->stream), "lane synchronisation");
-      else cudaStreamSynchronize(l->stream);
-      rcs[j] = rc;
-      if (rc) msgs[j] = qr_last_error_string();
-    });
+    } catch (const std::bad_alloc&) {
+      rc = fail(QR_ENOMEM, "host memory allocation failed");
+    }
+    if (!rc) rc = cuda_ok(cudaStreamSynchronize(l->stream), "lane synchronisation");
+    else cudaStreamSynchronize(l->stream);
+    rcs[j] = rc;
+    if (rc) msgs[j] = qr_last_error_string();
+  };
+  std::vector<std::thread> th;
+  th.reserve(L);
+  for (int j = 0; j < L; j++) {
+    try {
+      th.emplace_back(run_lane, j);
+    } catch (const std::system_error&) {
+      run_lane(j);  // no thread to spare: this lane's gates run on the calling thread
+    }
+  }
   for (auto& t : th) t.join();
   for (int i = 0; i < ngates; i++) {  // the entries each gate wrote, from its lane's view
     const qr_chain* l = h->lanes[i % L];
@@ -1503,26 +1515,26 @@ int qr_evolve_layer(qr_chain* h, int ngates, const int* sites, const double* gat
   for (int j = 0; j < L; j++)
     if (rcs[j]) return fail(rcs[j], msgs[j]);
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_overlap(const qr_chain* a, const qr_chain* b, double* out) {
+int qr_overlap(const qr_chain* a, const qr_chain* b, double* out) try {
   if (!a || !b || !out) return fail(QR_EINVAL, "null argument");
   if (a->n != b->n || a->d != b->d) return fail(QR_EASSERT, "Ansatzes must have the same sites");
   QR_CUDA(cudaStreamSynchronize(b->stream));
   return env_sweep(a, b, nullptr, a->stream, out);
-}
+} QR_ABI_CATCH
 
-int qr_norm(const qr_chain* h, double* out) {
+int qr_norm(const qr_chain* h, double* out) try {
   if (!h || !out) return fail(QR_EINVAL, "null argument");
   double z[2];
   QR_TRY(env_sweep(h, h, nullptr, h->stream, z));
   *out = std::abs(std::sqrt(std::complex<double>(z[0], z[1])));
   return QR_OK;
-}
+} QR_ABI_CATCH
 
 // expect (Chain.jl:724-735): the product operator O_{k-1}...O_0 is built as a small MPO on the
 // host (bond dimension d^2 per two-site observable) and contracted in one environment sweep.
-int qr_expect(const qr_chain* h, int nobs, const int* first, const int* nlanes, const double* mats, double* out) {
+int qr_expect(const qr_chain* h, int nobs, const int* first, const int* nlanes, const double* mats, double* out) try {
   if (!h || !out) return fail(QR_EINVAL, "null argument");
   if (nobs < 0 || (nobs > 0 && (!first || !nlanes || !mats))) return fail(QR_EINVAL, "bad observable list");
   const int n = h->n, d = h->d;
@@ -1636,9 +1648,9 @@ int qr_expect(const qr_chain* h, int nobs, const int* first, const int* nlanes, 
   cudaStreamSynchronize(h->stream);
   for (auto p : dev) if (p) cudaFreeAsync(p, h->stream);
   return rc;
-}
+} QR_ABI_CATCH
 
-int qr_mpo_create(int n, int d, const int* bond_dims, qr_mpo** out) {
+int qr_mpo_create(int n, int d, const int* bond_dims, qr_mpo** out) try {
   if (!out) return fail(QR_EINVAL, "null output");
   *out = nullptr;
   if (n < 2 || d < 2 || d > 4 || !bond_dims) return fail(QR_EINVAL, "bad MPO shape");
@@ -1654,16 +1666,16 @@ int qr_mpo_create(int n, int d, const int* bond_dims, qr_mpo** out) {
   }
   *out = w;
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_mpo_free(qr_mpo* w) {
+int qr_mpo_free(qr_mpo* w) try {
   if (!w) return QR_OK;
   for (auto p : w->site) if (p) cudaFree(p);
   delete w;
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_mpo_upload_site(qr_mpo* w, int site, const double* host, const char* order) {
+int qr_mpo_upload_site(qr_mpo* w, int site, const double* host, const char* order) try {
   if (!w || site < 0 || site >= w->n || !host) return fail(QR_EINVAL, "bad MPO site");
   w->host_ok = false;
   if (!is_perm(order ? order : "", "oilr")) return fail(QR_EINVAL, "order must be a permutation of (o, i, l, r)");
@@ -1678,9 +1690,9 @@ int qr_mpo_upload_site(qr_mpo* w, int site, const double* host, const char* orde
   cudaDeviceSynchronize();
   cudaFree(tmp);
   return rc;
-}
+} QR_ABI_CATCH
 
-int qr_mpo_download_site(const qr_mpo* w, int site, double* host, const char* order) {
+int qr_mpo_download_site(const qr_mpo* w, int site, double* host, const char* order) try {
   if (!w || site < 0 || site >= w->n || !host) return fail(QR_EINVAL, "bad MPO site");
   if (!is_perm(order ? order : "", "oilr")) return fail(QR_EINVAL, "order must be a permutation of (o, i, l, r)");
   std::string ho = filtered(order, site == 0, site == w->n - 1);
@@ -1705,9 +1717,9 @@ int qr_mpo_download_site(const qr_mpo* w, int site, double* host, const char* or
   }
   cudaFree(tmp);
   return rc;
-}
+} QR_ABI_CATCH
 
-int qr_mpo_expect(const qr_chain* h, const qr_mpo* w, double* out) {
+int qr_mpo_expect(const qr_chain* h, const qr_mpo* w, double* out) try {
   if (!h || !w || !out) return fail(QR_EINVAL, "null argument");
   if (w->n != h->n || w->d != h->d) return fail(QR_EASSERT, "Outputs of the state must match inputs of the operator");
   EnvOps ops;
@@ -1729,6 +1741,6 @@ int qr_mpo_expect(const qr_chain* h, const qr_mpo* w, double* out) {
   for (int i = 0; i < h->n; i++)
     ops.has_tab[i] = build_mix_table(w->host_w[i].data(), ops.wl[i], h->d, ops.wr[i], &ops.tab[i]) ? 1 : 0;
   return env_sweep(h, h, &ops, h->stream, out);
-}
+} QR_ABI_CATCH
 
 }  // extern "C"

@@ -5,6 +5,8 @@
 #include <cmath>
 #include <string>
 #include <atomic>
+#include <exception>
+#include <new>
 
 #include "../../include/qrochet_gpu.h"
 #include "../../include/qrochet_gpu_testing.h"
@@ -66,6 +68,20 @@ inline void count_launch(uint64_t n = 1) { g_launches.fetch_add(n, std::memory_o
     cudaError_t _e = cudaGetLastError();                        \
     if (_e != cudaSuccess) return ::qr::cuda_fail(_e, what);    \
   } while (0)
+
+// Every exported function is a function-try-block ending in QR_ABI_CATCH: a C++ exception (a
+// failed host allocation, a thread or lock that cannot be created) becomes a status code and the
+// thread's error message instead of unwinding into the caller's C, Julia or Python frames.
+#define QR_ABI_CATCH                                                                              \
+  catch (const std::bad_alloc&) {                                                                 \
+    return ::qr::fail(QR_ENOMEM, "host memory allocation failed");                                \
+  }                                                                                               \
+  catch (const std::exception& _x) {                                                              \
+    return ::qr::fail(QR_EHOST, std::string("host-side failure: ") + _x.what());                  \
+  }                                                                                               \
+  catch (...) {                                                                                   \
+    return ::qr::fail(QR_EHOST, "host-side failure");                                             \
+  }
 
 #define QR_TRY(expr)              \
   do {                            \

@@ -91,7 +91,7 @@ extern "C" {
 
 // Peak rate of one arithmetic pipe, measured now on the current device: kind 0 = FP64 tensor
 // (mma.sync m8n8k4 f64), 1 = FP32 FFMA, 2 = FP64 DFMA.  Best of three timed launches.
-int qr_probe_peak(int kind, double* tflops) {
+int qr_probe_peak(int kind, double* tflops) try {
   if (!tflops || kind < 0 || kind > 2) return fail(QR_EINVAL, "bad probe kind");
   int dev = 0, sms = 0;
   QR_CUDA(cudaGetDevice(&dev));
@@ -124,9 +124,9 @@ int qr_probe_peak(int kind, double* tflops) {
   QR_CUDA(cudaGetLastError());
   *tflops = best;
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_prof_enable(int on) {
+int qr_prof_enable(int on) try {
   std::lock_guard<std::mutex> lk(g_mu);
   for (auto& r : g_recs) {
     g_pool.push_back(r.e0);
@@ -135,9 +135,9 @@ int qr_prof_enable(int on) {
   g_recs.clear();
   g_on = on != 0;
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_prof_read(int kind, double* ms, uint64_t* launches, double* flops, double* bytes) {
+int qr_prof_read(int kind, double* ms, uint64_t* launches, double* flops, double* bytes) try {
   QR_CUDA(cudaDeviceSynchronize());
   std::lock_guard<std::mutex> lk(g_mu);
   double t = 0, f = 0, b = 0;
@@ -155,17 +155,17 @@ int qr_prof_read(int kind, double* ms, uint64_t* launches, double* flops, double
   if (flops) *flops = f;
   if (bytes) *bytes = b;
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_host_alloc(uint64_t bytes, void** ptr) {
+int qr_host_alloc(uint64_t bytes, void** ptr) try {
   if (!ptr) return fail(QR_EINVAL, "null output");
   QR_CUDA(cudaHostAlloc(ptr, bytes ? bytes : 16, cudaHostAllocDefault));
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_host_free(void* ptr) {
+int qr_host_free(void* ptr) try {
   if (ptr) QR_CUDA(cudaFreeHost(ptr));
   return QR_OK;
-}
+} QR_ABI_CATCH
 
 }  // extern "C"

@@ -81,8 +81,7 @@ const double kPauli[4][8] = {
     {1, 0, 0, 0, 0, 0, -1, 0},  // Z
 };
 
-void run_request(qr_server* sv, Request* r) {
-  qr_chain* h = nullptr;
+int evolve_and_measure(qr_server* sv, Request* r, qr_chain*& h) {
   std::vector<int> bd(r->n - 1, 1);
   int rc = qr_set_device(sv->device);
   if (!rc) rc = qr_chain_create(r->n, 2, bd.data(), &h);
@@ -112,6 +111,21 @@ void run_request(qr_server* sv, Request* r) {
       continue;
     }
     rc = qr_expect(h, (int)first.size(), first.data(), nl.data(), mats.data(), &r->results[2 * j]);
+  }
+  return rc;
+}
+
+// One request on a worker thread: its status and message are the request's, and no exception
+// leaves the worker (a failed host allocation fails this request only).
+void run_request(qr_server* sv, Request* r) {
+  qr_chain* h = nullptr;
+  int rc;
+  try {
+    rc = evolve_and_measure(sv, r, h);
+  } catch (const std::bad_alloc&) {
+    rc = qr::fail(QR_ENOMEM, "host memory allocation failed");
+  } catch (const std::exception& x) {
+    rc = qr::fail(QR_EHOST, std::string("host-side failure: ") + x.what());
   }
   if (rc) r->error = qr_last_error_string();
   r->status = rc;
@@ -155,7 +169,7 @@ void worker_loop(qr_server* sv) {
 
 extern "C" {
 
-int qr_server_create(int device, int workers, uint64_t hbm_budget_bytes, int precision, qr_server** out) {
+int qr_server_create(int device, int workers, uint64_t hbm_budget_bytes, int precision, qr_server** out) try {
   if (!out) return qr::fail(QR_EINVAL, "null output");
   *out = nullptr;
   if (workers < 1 || workers > 256) return qr::fail(QR_EINVAL, "workers must be 1..256");
@@ -165,12 +179,17 @@ int qr_server_create(int device, int workers, uint64_t hbm_budget_bytes, int pre
   sv->device = device;
   sv->budget = hbm_budget_bytes;
   sv->precision = precision;
-  for (int i = 0; i < workers; i++) sv->workers.emplace_back(worker_loop, sv);
+  try {
+    for (int i = 0; i < workers; i++) sv->workers.emplace_back(worker_loop, sv);
+  } catch (const std::exception& x) {  // a worker that cannot start: stop the ones that did
+    qr_server_free(sv);
+    return qr::fail(QR_EHOST, std::string("cannot start the server's workers: ") + x.what());
+  }
   *out = sv;
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_server_free(qr_server* sv) {
+int qr_server_free(qr_server* sv) try {
   if (!sv) return QR_OK;
   {
     std::lock_guard<std::mutex> lk(sv->mu);
@@ -180,17 +199,17 @@ int qr_server_free(qr_server* sv) {
   for (auto& t : sv->workers) t.join();
   delete sv;
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_server_footprint(int n, int chi_max, uint64_t* bytes) {
+int qr_server_footprint(int n, int chi_max, uint64_t* bytes) try {
   if (!bytes || n < 2 || chi_max < 1) return qr::fail(QR_EINVAL, "bad request shape");
   *bytes = footprint_bytes(n, chi_max);
   return QR_OK;
-}
+} QR_ABI_CATCH
 
 int qr_server_submit(qr_server* sv, int n, int chi_max, double threshold, int ngates, const int* gate_site,
                      const double* gate_mats, int nobs, const int* obs_weight, const int* obs_sites,
-                     const int* obs_paulis, uint64_t* ticket) {
+                     const int* obs_paulis, uint64_t* ticket) try {
   if (!sv || !ticket) return qr::fail(QR_EINVAL, "null argument");
   if (n < 2 || chi_max < 1) return qr::fail(QR_EINVAL, "a request needs n >= 2 sites and chi_max >= 1");
   if (ngates < 0 || (ngates > 0 && (!gate_site || !gate_mats))) return qr::fail(QR_EINVAL, "bad gate list");
@@ -228,12 +247,12 @@ int qr_server_submit(qr_server* sv, int n, int chi_max, double threshold, int ng
   }
   sv->cv_work.notify_all();
   return QR_OK;
-}
+} QR_ABI_CATCH
 
 // Waits up to timeout_s (< 0: forever).  Returns QR_OK with *done = 0 on timeout.  On completion
 // copies the results and timings and forgets the ticket; *status is the request's own status.
 int qr_server_wait(qr_server* sv, uint64_t ticket, double timeout_s, int* done, int* status, double* results,
-                   double* latency_ms, double* queue_ms) {
+                   double* latency_ms, double* queue_ms) try {
   if (!sv || !done) return qr::fail(QR_EINVAL, "null argument");
   std::unique_lock<std::mutex> lk(sv->mu);
   auto it = sv->all.find(ticket);
@@ -251,10 +270,10 @@ int qr_server_wait(qr_server* sv, uint64_t ticket, double timeout_s, int* done, 
   if (r->status) qr::set_error(r->error);
   sv->all.erase(it);
   return QR_OK;
-}
+} QR_ABI_CATCH
 
 int qr_server_stats(qr_server* sv, uint64_t* submitted, uint64_t* completed, int* in_flight, uint64_t* hbm_in_use,
-                    int* queued) {
+                    int* queued) try {
   if (!sv) return qr::fail(QR_EINVAL, "null server");
   std::lock_guard<std::mutex> lk(sv->mu);
   if (submitted) *submitted = sv->submitted;
@@ -263,6 +282,6 @@ int qr_server_stats(qr_server* sv, uint64_t* submitted, uint64_t* completed, int
   if (hbm_in_use) *hbm_in_use = sv->in_use;
   if (queued) *queued = (int)sv->pending.size();
   return QR_OK;
-}
+} QR_ABI_CATCH
 
 }  // extern "C"

@@ -2654,7 +2654,7 @@ int noalloc_scratch(void** out) {
 using namespace qr;
 
 extern "C" int qr_svd_noalloc(int m, int n, const double* A, long lda, double* U, long ldu, double* S, double* Vh,
-                              long ldvh, void* stream) {
+                              long ldvh, void* stream) try {
   if (m <= 0 || n <= 0) return fail(QR_EINVAL, "qr_svd_noalloc: empty matrix");
   if (!A || !U || !S || !Vh) return fail(QR_EINVAL, "qr_svd_noalloc: null buffer");
   const bool tall = m >= n;
@@ -2823,7 +2823,7 @@ extern "C" int qr_svd_noalloc(int m, int n, const double* A, long lda, double* U
   }
   QR_CUDA(cudaStreamSynchronize(s));
   return QR_OK;
-}
+} QR_ABI_CATCH
 
 namespace qr {
 }  // namespace qr

@@ -1,6 +1,7 @@
 // Kernel-level entry points for unit tests and kernel benchmarks: host matrices in, host results
 // and CUDA-event timings out.  They have no counterpart in the reference.
 #include <vector>
+#include <stdexcept>
 #include "kernels.cuh"
 
 using namespace qr;
@@ -25,7 +26,7 @@ extern "C" {
 // recomputed from the original each time).  ms_per_iter receives the average event time.
 int qr_test_zgemm(int opA, int opB, int M, int N, int K, const double* alpha, const double* A, long lda,
                   const double* B, long ldb, const double* beta, double* C, long ldc, const double* dk,
-                  int iters, double* ms_per_iter) {
+                  int iters, double* ms_per_iter) try {
   if (M <= 0 || N <= 0 || K < 0 || iters < 1) return fail(QR_EINVAL, "bad gemm shape");
   long ra = (opA == OP_N || opA == OP_R) ? M : K, ca = (opA == OP_N || opA == OP_R) ? K : M;
   long rb = (opB == OP_N || opB == OP_R) ? K : N, cb = (opB == OP_N || opB == OP_R) ? N : K;
@@ -62,12 +63,12 @@ int qr_test_zgemm(int opA, int opB, int M, int N, int K, const double* alpha, co
   QR_CUDA(cudaMemcpy(C, dC.p, sizeof(double2) * ldc * N, cudaMemcpyDeviceToHost));
   if (ms_per_iter) *ms_per_iter = total / iters;
   return QR_OK;
-}
+} QR_ABI_CATCH
 
 // C[b] = op(A[b]) op(B[b]) with the tcgen05 split-precision kernel (gemm_tc.cu); A and B hold
 // `batch` matrices at strides sA and sB (sB = 0: one B shared by the batch), C at stride ldc * N.
 int qr_test_zgemm_tc(int opA, int opB, int M, int N, int K, int batch, const double* A, long lda, long sA,
-                     const double* B, long ldb, long sB, double* C, long ldc, int iters, double* ms_per_iter) {
+                     const double* B, long ldb, long sB, double* C, long ldc, int iters, double* ms_per_iter) try {
   if (M <= 0 || N <= 0 || K < 0 || iters < 1 || batch < 1) return fail(QR_EINVAL, "bad gemm shape");
   long ca = (opA == OP_N || opA == OP_R) ? K : M;
   long cb = (opB == OP_N || opB == OP_R) ? N : K;
@@ -107,12 +108,12 @@ int qr_test_zgemm_tc(int opA, int opB, int M, int N, int K, int batch, const dou
   QR_CUDA(cudaMemcpy(C, dC.p, sizeof(double2) * sC * batch, cudaMemcpyDeviceToHost));
   if (ms_per_iter) *ms_per_iter = total / iters;
   return QR_OK;
-}
+} QR_ABI_CATCH
 
 // Double-float GEMM (gemm_df.cu) through FP64 host matrices: inputs are split into (hi, lo) FP32
 // pairs on the device, the result converted back (mode 1 returns the FP32 value I - op(A) B).
 int qr_test_zgemm_df(int mode, int opA, int M, int N, int K, const double* A, long lda, const double* B, long ldb,
-                     const double* D, double* C, long ldc, int iters, double* ms_per_iter) {
+                     const double* D, double* C, long ldc, int iters, double* ms_per_iter) try {
   if (M <= 0 || N <= 0 || K < 0 || iters < 1 || mode < 0 || mode > 3) return fail(QR_EINVAL, "bad gemm_df shape");
   if (opA != OP_N && opA != OP_T && opA != OP_C) return fail(QR_EINVAL, "op(A) must be N, T or C");
   const long ca = opA == OP_N ? K : M, rb = K;
@@ -164,25 +165,25 @@ int qr_test_zgemm_df(int mode, int opA, int M, int N, int K, const double* A, lo
   QR_TRY(df2z(0, Ch, Cl, ldc, (int)ldc, N, nullptr, (double2*)dC.p, ldc));
   QR_CUDA(cudaMemcpy(C, dC.p, sizeof(double2) * nc, cudaMemcpyDeviceToHost));
   return QR_OK;
-}
+} QR_ABI_CATCH
 
 // Thin SVD of the m x n column-major A: U (m x k), S (k), Vh (k x n), k = min(m, n).
 // counts[i] = how often SVD code path i ran in this process (i < min(n, SP_COUNT)); *total = SP_COUNT
 int qr_test_schedule_pairs(const unsigned* mask, const unsigned* flag, int nv, int use_flag, unsigned* items,
-                           unsigned* ord, long* listed, int* classes) {
+                           unsigned* ord, long* listed, int* classes) try {
   if (nv < 2 || nv % 2 || nv >= 32768 || !mask || !items || !ord || !listed || !classes)
     return fail(QR_EINVAL, "schedule: nv must be even, in [2, 32768), and the arrays given");
   *listed = schedule_pairs_host(mask, flag, nv, use_flag, items, ord, classes);
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_test_svd_paths(uint64_t* counts, int n, int* total) {
+int qr_test_svd_paths(uint64_t* counts, int n, int* total) try {
   for (int i = 0; i < n && i < SP_COUNT; i++) counts[i] = g_svd_path[i].load(std::memory_order_relaxed);
   if (total) *total = SP_COUNT;
   return QR_OK;
-}
+} QR_ABI_CATCH
 
-int qr_test_svd(int mode, int m, int n, const double* A, double* U, double* S, double* Vh, double* ms) {
+int qr_test_svd(int mode, int m, int n, const double* A, double* U, double* S, double* Vh, double* ms) try {
   if (m <= 0 || n <= 0) return fail(QR_EINVAL, "bad svd shape");
   const int k = m < n ? m : n;
   Dev dA, dU, dV, dS;
@@ -212,10 +213,10 @@ int qr_test_svd(int mode, int m, int n, const double* A, double* U, double* S, d
   if (Vh) QR_CUDA(cudaMemcpy(Vh, dV.p, sizeof(double2) * k * n, cudaMemcpyDeviceToHost));
   if (S) QR_CUDA(cudaMemcpy(S, dS.p, sizeof(double) * k, cudaMemcpyDeviceToHost));
   return QR_OK;
-}
+} QR_ABI_CATCH
 
 // Thin Householder QR of the m x n column-major A: Q (m x k), R (k x n).
-int qr_test_qr(int m, int n, const double* A, double* Q, double* R, double* ms) {
+int qr_test_qr(int m, int n, const double* A, double* Q, double* R, double* ms) try {
   if (m <= 0 || n <= 0) return fail(QR_EINVAL, "bad qr shape");
   const int k = m < n ? m : n;
   Dev dA, dQ, dR, dT;
@@ -239,6 +240,14 @@ int qr_test_qr(int m, int n, const double* A, double* Q, double* R, double* ms) 
   QR_CUDA(cudaMemcpy(Q, dQ.p, sizeof(double2) * m * k, cudaMemcpyDeviceToHost));
   QR_CUDA(cudaMemcpy(R, dR.p, sizeof(double2) * k * n, cudaMemcpyDeviceToHost));
   return QR_OK;
-}
+} QR_ABI_CATCH
+
+int qr_test_host_exception(int kind) try {
+  struct NotStd {};
+  if (kind == 0) throw std::bad_alloc();
+  if (kind == 1) throw std::runtime_error("planted by qr_test_host_exception");
+  if (kind == 2) throw NotStd();
+  return QR_OK;
+} QR_ABI_CATCH
 
 }  // extern "C"

@@ -12,7 +12,7 @@ import threading
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(os.path.dirname(_HERE), "lib", "libqrochet_gpu.so")
 
-QR_OK, QR_EINVAL, QR_EASSERT, QR_ENO_SCHMIDT, QR_EDIM, QR_ENOMEM, QR_ECUDA, QR_ENODEV, QR_ENOCONV = range(9)
+QR_OK, QR_EINVAL, QR_EASSERT, QR_ENO_SCHMIDT, QR_EDIM, QR_ENOMEM, QR_ECUDA, QR_ENODEV, QR_ENOCONV, QR_EHOST = range(10)
 QR_FP64, QR_MIXED = 0, 1
 QR_DIR_LEFT, QR_DIR_RIGHT = 0, 1
 QR_METHOD_QR, QR_METHOD_SVD = 0, 1
@@ -122,6 +122,7 @@ SIGNATURES = {
     "qr_test_schedule_pairs": [C.c_void_p, C.c_void_p, _I, _I, C.c_void_p, C.c_void_p, C.POINTER(C.c_long),
                                C.POINTER(C.c_int)],
     "qr_test_qr": [_I, _I, _PD, _PD, _PD, _PD],
+    "qr_test_host_exception": [_I],
 }
 
 _lib = None

@@ -92,3 +92,16 @@ def test_index_counter_and_random_generators():
     arrs = R.gaussian_mps_arrays(5, 3, seed=4)
     assert arrs[0].shape == (2, 3) and arrs[2].shape == (2, 3, 3) and arrs[4].shape == (2, 3)
     assert all(a.flags.f_contiguous for a in arrs)
+
+
+@pytest.mark.parametrize("kind,code,text", [(0, "QR_ENOMEM", "host memory allocation failed"),
+                                            (1, "QR_EHOST", "planted by qr_test_host_exception"),
+                                            (2, "QR_EHOST", "host-side failure")])
+def test_abi_guard_turns_host_exceptions_into_status(lib, kind, code, text):
+    """A C++ exception inside an exported function comes back as a status and a message (no
+    unwinding into the caller); the hook throws on the host, no GPU involved."""
+    from qrochet import _lib
+
+    assert lib.qr_test_host_exception(kind) == getattr(_lib, code)
+    assert text in _lib.last_error()
+    assert lib.qr_test_host_exception(3) == _lib.QR_OK
