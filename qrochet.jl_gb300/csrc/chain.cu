@@ -956,14 +956,22 @@ int qr_chain_free(qr_chain* h) try {
 
 int qr_chain_copy(const qr_chain* src, qr_chain** out) try {
   if (!src || !out) return fail(QR_EINVAL, "null chain");
+  *out = nullptr;
   QR_CUDA(cudaStreamSynchronize(src->stream));
-  QR_TRY(chain_create(src->n, src->d, src->bd.data(), src->periodic, out));
-  qr_chain* h = *out;
+  qr_chain* h = nullptr;
+  QR_TRY(chain_create(src->n, src->d, src->bd.data(), src->periodic, &h));
   h->precision = src->precision;
-  for (int i = 0; i < src->n; i++)
-    QR_CUDA(cudaMemcpyAsync(h->site[i], src->site[i], sizeof(double2) * src->elems(i), cudaMemcpyDeviceToDevice, h->stream));
-  for (int b = 0; b < src->n - 1; b++)
-    if (src->lam[b]) QR_TRY(put_lambda(h, b, src->lam[b], src->lamlen[b]));
+  int rc = QR_OK;
+  for (int i = 0; i < src->n && !rc; i++)
+    rc = cuda_ok(cudaMemcpyAsync(h->site[i], src->site[i], sizeof(double2) * src->elems(i),
+                                 cudaMemcpyDeviceToDevice, h->stream), "cudaMemcpyAsync");
+  for (int b = 0; b < src->n - 1 && !rc; b++)
+    if (src->lam[b]) rc = put_lambda(h, b, src->lam[b], src->lamlen[b]);
+  if (rc) {  // no half-built copy is handed out
+    qr_chain_free(h);
+    return rc;
+  }
+  *out = h;
   return QR_OK;
 } QR_ABI_CATCH
 
