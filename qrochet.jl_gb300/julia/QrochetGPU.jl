@@ -149,6 +149,14 @@ function read_checkpoint(path::AbstractString)
 end
 
 Qrochet.nsites(c::GPUChain) = c.n
+# the lane queries of a Quantum network (src/Quantum.jl:118-143, 228-239): a GPUChain is a state
+Qrochet.socket(::GPUChain) = State()
+Qrochet.boundary(c::GPUChain) = c.periodic ? Qrochet.Periodic() : Qrochet.Open()
+Qrochet.sites(c::GPUChain) = [Site(i) for i in 1:c.n]
+Qrochet.outputs(c::GPUChain) = Qrochet.sites(c)
+Qrochet.inputs(::GPUChain) = Site[]
+Qrochet.noutputs(c::GPUChain) = c.n
+Qrochet.ninputs(::GPUChain) = 0
 
 function bond_dims(c::GPUChain)
     out = Vector{Cint}(undef, c.periodic ? c.n : c.n - 1)

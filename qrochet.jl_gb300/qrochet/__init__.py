@@ -11,7 +11,8 @@ from .chain import (MPO, MPS, pMPS, Chain, Open, Periodic, canonicality_error, c
                     mpo_expect, norm, normalize_, overlap, truncate, truncate_, zeros_chain,
                     PinnedArray, probe_peak, prof_enable, prof_read, set_device, PROF_KINDS, rand,
                     sampler_bond_dims)
-from .dense import Dense, Operator, State, gate_from_matrix, validate_gate
+from .dense import Dense, Operator, Scalar, State, gate_from_matrix, validate_gate
+from .quantum import inputs, isdual, ninputs, noutputs, nsites, outputs, sites, socket
 from .site import Site, nextindex, site
 from . import checkpoint
 
@@ -23,5 +24,6 @@ __all__ = [
     "mixed_canonize_", "mpo_expect", "norm", "normalize_", "overlap", "truncate", "truncate_",
     "zeros_chain", "Dense", "Operator", "State", "gate_from_matrix", "validate_gate", "Site",
     "nextindex", "site", "PinnedArray", "probe_peak", "prof_enable", "prof_read", "set_device",
-    "PROF_KINDS", "checkpoint", "rand", "sampler_bond_dims",
+    "PROF_KINDS", "checkpoint", "rand", "sampler_bond_dims", "Scalar", "inputs", "isdual", "ninputs",
+    "noutputs", "nsites", "outputs", "sites", "socket",
 ]

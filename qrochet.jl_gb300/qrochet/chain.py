@@ -313,8 +313,16 @@ class AdjointChain:
     def __init__(self, parent):
         self.parent = parent
 
+    socket = State(dual=True)
+
     def sites(self):
         return [Site(i + 1, True) for i in range(self.parent.n)]
+
+    def nsites(self):
+        return self.parent.n
+
+    def boundary(self):
+        return self.parent.boundary()
 
     def leftindex(self, site):
         ix = self.parent.leftindex(_site_id(site))
@@ -369,6 +377,16 @@ class MPO:
         w = cls.__new__(cls)
         w._h, w.n, w.d = h, n, d
         return w
+
+    def sites(self):
+        """Outputs ``Site(i)`` and inputs ``Site(i; dual=true)`` of every lane (Chain.jl:168-169)."""
+        return [Site(i + 1) for i in range(self.n)] + [Site(i + 1, True) for i in range(self.n)]
+
+    def nsites(self):
+        return self.n
+
+    def boundary(self):
+        return Open()
 
     def site_array(self, i, order=("o", "i", "l", "r")):
         """Site ``i`` (0-based) in the reference layout (ends without ``:l`` / ``:r``)."""

@@ -9,18 +9,47 @@ from ._lib import ArgumentError
 from .site import Site
 
 
-class State:
-    """Socket of a state."""
+class Scalar:
+    """Socket of a network with no open sites (src/Quantum.jl:203-208)."""
 
     def __eq__(self, other):
-        return isinstance(other, State)
+        return isinstance(other, Scalar)
+
+    def __hash__(self):
+        return hash("Scalar")
+
+    def __repr__(self):
+        return "Scalar()"
+
+
+class State:
+    """Socket of a state; ``dual=True``: a state on dual sites only, such as an adjoint
+    (src/Quantum.jl:210-217)."""
+
+    def __init__(self, dual=False):
+        self.dual = bool(dual)
+
+    def __eq__(self, other):
+        return isinstance(other, State) and other.dual == self.dual
+
+    def __hash__(self):
+        return hash(("State", self.dual))
+
+    def __repr__(self):
+        return "State(dual=true)" if self.dual else "State()"
 
 
 class Operator:
-    """Socket of an operator."""
+    """Socket of an operator (src/Quantum.jl:219-224)."""
 
     def __eq__(self, other):
         return isinstance(other, Operator)
+
+    def __hash__(self):
+        return hash("Operator")
+
+    def __repr__(self):
+        return "Operator()"
 
 
 class Dense:

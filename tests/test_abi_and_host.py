@@ -105,3 +105,34 @@ def test_abi_guard_turns_host_exceptions_into_status(lib, kind, code, text):
     assert lib.qr_test_host_exception(kind) == getattr(_lib, code)
     assert text in _lib.last_error()
     assert lib.qr_test_host_exception(3) == _lib.QR_OK
+
+
+def test_socket_and_lane_queries():
+    """socket / inputs / outputs / ninputs / noutputs / isdual (src/Quantum.jl:25,118-143,228-239)
+    on the host bookkeeping of a chain (no device buffers needed), its adjoint, an MPO's site
+    list and a gate."""
+    import qrochet as Q
+    from qrochet.chain import MPO
+
+    psi = Q.Chain(None, 5, 2)  # bookkeeping only: no handle
+    assert Q.socket(psi) == Q.State() and Q.socket(psi) != Q.State(dual=True)
+    assert Q.outputs(psi) == [Q.Site(i) for i in range(1, 6)] and Q.inputs(psi) == []
+    assert (Q.noutputs(psi), Q.ninputs(psi), Q.nsites(psi)) == (5, 0, 5)
+    adj = psi.adjoint()
+    assert Q.socket(adj) == Q.State(dual=True) == adj.socket
+    assert Q.inputs(adj) == [Q.Site(i, True) for i in range(1, 6)] and Q.noutputs(adj) == 0
+    assert all(Q.isdual(s) for s in adj.sites()) and not Q.isdual(Q.Site(2))
+    w = MPO.__new__(MPO)
+    w.n, w.d = 4, 2
+    assert Q.socket(w) == Q.Operator()
+    assert (Q.ninputs(w), Q.noutputs(w)) == (4, 4)
+    assert Q.inputs(w) == [Q.Site(i, True) for i in range(1, 5)]
+    g = Q.gate_from_matrix(np.eye(4), [3, 2])
+    assert Q.socket(g) == Q.Operator()
+    assert Q.outputs(g) == [Q.Site(2), Q.Site(3)] and Q.inputs(g) == [Q.Site(2, True), Q.Site(3, True)]
+
+    class Empty:
+        sites = ()
+
+    assert Q.socket(Empty()) == Q.Scalar()
+    assert len({Q.State(), Q.State(), Q.State(dual=True), Q.Operator(), Q.Scalar()}) == 4
