@@ -675,6 +675,13 @@ def zeros_chain(n, d=2):
     return MPS(zero_product_arrays(n, d))
 
 
+def ones_chain(n, d=2):
+    """``convert(Chain, ones(Product, n))``: |1...1> with bonds of size 1."""
+    from .random import one_product_arrays
+
+    return MPS(one_product_arrays(n, d))
+
+
 def device_count():
     c = C.c_int()
     rc = lib().qr_device_count(C.byref(c))

@@ -40,6 +40,21 @@ def noutputs(q):
     return len(outputs(q))
 
 
+def lanes(q):
+    """The lanes as non-dual sites, each once, in the order first seen over the inputs and then
+    the outputs (src/Quantum.jl:175)."""
+    out = []
+    for s in inputs(q) + outputs(q):
+        lane = s.adjoint() if isdual(s) else s
+        if lane not in out:
+            out.append(lane)
+    return out
+
+
+def nlanes(q):
+    return len(lanes(q))
+
+
 def socket(q):
     """``Scalar()`` without sites, ``State()`` with outputs only, ``State(dual=true)`` with inputs
     only, else ``Operator()`` (src/Quantum.jl:228-239)."""

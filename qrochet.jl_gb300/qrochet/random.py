@@ -152,10 +152,24 @@ def rand_chain_state_arrays(g, n, chi, p=2):
 def zero_product_arrays(n, d=2):
     """``convert(Chain, zeros(Product, n))``: |0...0> with bonds of size 1 (``Chain.jl:174-183``,
     ``Product.jl:44-46``)."""
+    return basis_product_arrays(n, d, 0)
+
+
+def one_product_arrays(n, d=2):
+    """``convert(Chain, ones(Product, n))``: |1...1> with bonds of size 1 (``Chain.jl:174-183``,
+    ``Product.jl:48-54``)."""
+    return basis_product_arrays(n, d, 1)
+
+
+def basis_product_arrays(n, d, level):
+    """Every lane in basis state ``level``: arrays as ``MPS(arrays)`` takes them, (o, r) at site 1,
+    (o, l, r) inside, (o, l) at site n, all bonds of size 1."""
+    if n < 2 or not 0 <= level < d:
+        raise ValueError("a product chain needs n >= 2 sites and 0 <= level < d")
     arrays = []
     for i in range(n):
         v = np.zeros(d, dtype=np.complex128)
-        v[0] = 1.0
+        v[level] = 1.0
         if i == 0 or i == n - 1:
             arrays.append(np.asfortranarray(v.reshape(d, 1)))
         else:

@@ -136,3 +136,28 @@ def test_socket_and_lane_queries():
 
     assert Q.socket(Empty()) == Q.Scalar()
     assert len({Q.State(), Q.State(), Q.State(dual=True), Q.Operator(), Q.Scalar()}) == 4
+
+
+def test_product_arrays_and_lanes():
+    """zeros / ones(Product, n) as MPS(arrays) takes them (Product.jl:44-54, Chain.jl:174-183),
+    and lanes / nlanes (src/Quantum.jl:171-184)."""
+    import qrochet as Q
+    from qrochet import random as R
+    from qrochet.chain import MPO
+
+    for make, level in ((R.zero_product_arrays, 0), (R.one_product_arrays, 1)):
+        arrs = make(5, 3)
+        assert [a.shape for a in arrs] == [(3, 1), (3, 1, 1), (3, 1, 1), (3, 1, 1), (3, 1)]
+        for a in arrs:
+            v = a.reshape(3)
+            assert v[level] == 1 and np.count_nonzero(v) == 1
+    with pytest.raises(ValueError):
+        R.basis_product_arrays(4, 2, 2)
+    g = Q.gate_from_matrix(np.eye(4), [3, 2])
+    assert Q.lanes(g) == [Q.Site(2), Q.Site(3)] and Q.nlanes(g) == 2 == g.nlanes()
+    psi = Q.Chain(None, 4, 2)
+    assert Q.lanes(psi) == [Q.Site(i) for i in range(1, 5)]
+    assert Q.lanes(psi.adjoint()) == Q.lanes(psi)
+    w = MPO.__new__(MPO)
+    w.n, w.d = 3, 2
+    assert Q.nlanes(w) == 3

@@ -536,6 +536,18 @@ def test_rank_deficient_and_zero_singular_values():
     assert Q.isleftcanonical(psi, 2)
 
 
+def test_ones_product_chain():
+    """convert(Chain, ones(Product, n)) (Product.jl:48-54, Chain.jl:174-183): |1...1> with bonds
+    of size 1, so <Z_i> = -1 on every site, norm 1 and no overlap with |0...0>."""
+    n = 5
+    psi = Q.ones_chain(n)
+    assert list(psi.bond_dims()) == [1] * (n - 1)
+    assert np.isclose(Q.norm(psi), 1.0, rtol=1e-14)
+    for i in range(1, n + 1):
+        assert abs(Q.expect(psi, [Q.gate_from_matrix(R.PAULI["Z"], [i])]) + 1.0) <= 1e-14
+    assert abs(Q.overlap(psi, Q.zeros_chain(n))) <= 1e-15
+
+
 # Split-precision environment contractions (QR_SPLIT_CONTRACT): ~FP32 accuracy per site step.
 SPLIT_RTOL = 1e-5
 
