@@ -8,12 +8,11 @@ reference's exception types.
 from __future__ import annotations
 
 import ctypes as C
-import math
 
 import numpy as np
 
 from . import _lib as L
-from ._lib import ArgumentError, MissingSchmidtCoefficientsException, check, dptr, lib
+from ._lib import ArgumentError, check, dptr, lib
 from .dense import Dense, Operator, State, validate_gate
 from .site import Site, nextindex
 
@@ -687,5 +686,3 @@ def device_count():
     rc = lib().qr_device_count(C.byref(c))
     return c.value if rc == 0 else 0
 
-
-_ = (math, Operator, MissingSchmidtCoefficientsException)

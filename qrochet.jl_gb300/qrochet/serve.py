@@ -11,7 +11,6 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from . import _lib as L
 from ._lib import check, dptr, lib
 from . import random as R
 

@@ -3,7 +3,6 @@ same alone and in a concurrent mix (continuous batching), within 1e-12."""
 import numpy as np
 import pytest
 
-import qrochet as Q
 from oracle import chain_oracle as O
 from qrochet import random as R
 from qrochet import serve as S
