@@ -217,7 +217,9 @@ function Qrochet.truncate!(c::GPUChain, bond; threshold = nothing, maxdim = noth
     return c
 end
 
-"""Row-major M[(o_1..o_k),(i_1..i_k)] (left lane slowest) of a Dense gate for `lanes`."""
+"""M[(o_1..o_k),(i_1..i_k)] (left lane slowest) of a Dense gate for `lanes`, returned as its
+transpose so that the array's column-major memory is M in row-major order, which is how every
+gate crosses the C ABI (`qr_evolve_1site`, `qr_evolve_2site`, `qr_evolve_layer`, `qr_expect`)."""
 function gatematrix(gate::Dense, lanes)
     arr = only(Qrochet.arrays(gate))
     ind = Qrochet.inds(gate; at = Site(first(lanes)))  # dims follow `sites` (Dense.jl:21-34)
@@ -287,7 +289,7 @@ function Qrochet.expect(c::GPUChain, observables)
         lanes = sort!(map(Qrochet.id, Qrochet.outputs(o)))
         push!(firsts, lanes[1] - 1)
         push!(nl, length(lanes))
-        append!(mats, vec(permutedims(gatematrix(o, lanes))))  # row-major flattening
+        append!(mats, vec(ComplexF64.(gatematrix(o, lanes))))  # row-major M, as for qr_evolve_2site
     end
     out = Ref{ComplexF64}(0)
     check(ccall((:qr_expect, libqrochet), Cint, (Ptr{Cvoid}, Cint, Ptr{Cint}, Ptr{Cint}, Ptr{ComplexF64}, Ref{ComplexF64}),

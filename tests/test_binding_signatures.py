@@ -6,12 +6,15 @@ return type and every argument type must match the prototype (by ABI class: int,
 uint64, string, pointer to each of those, opaque handle, pointer to a handle), and each call must
 pass exactly as many arguments as its type tuple lists.  The Python ctypes table
 (``qrochet/_lib.py``) is checked against the same prototypes, and the status, precision, direction
-and method constants of both bindings against the header's ``#define``s.
+and method constants of both bindings against the header's ``#define``s.  The gate matrices the
+Julia binding builds are checked for the C ABI's row-major memory order by a NumPy restatement of
+its column-major steps, and every call site for passing them on unchanged.
 """
 import ctypes as C
 import os
 import re
 
+import numpy as np
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -235,3 +238,46 @@ def test_prototype_parser_sees_known_shapes(name):
         "qr_truncate": ["handle", "int", "int", "double", "int"],
     }
     assert protos[name] == ("int", shapes[name])
+
+
+# ---- gate memory order across the Julia binding --------------------------------------------------
+def _julia_gatematrix_memory(array, sites, lanes):
+    """NumPy restatement of QrochetGPU.gatematrix step by step with Julia's column-major rules
+    (permutedims = axis transpose, reshape in column-major order, collect(transpose(M))), returning
+    the memory a ccall passes: the result's column-major flattening."""
+    k = len(lanes)
+    perm = [sites.index((l, False)) for l in lanes] + [sites.index((l, True)) for l in lanes]
+    t = np.transpose(array, perm)
+    t = np.transpose(t, list(reversed(range(k))) + list(reversed(range(k, 2 * k))))
+    d = t.shape[0]
+    M = np.reshape(t, (d ** k, d ** k), order="F")
+    R = M.T.copy()
+    return R.flatten(order="F"), M
+
+
+def test_julia_gate_memory_is_row_major_like_python():
+    """For a non-symmetric two-site gate given with its sites in a scrambled order, the memory the
+    Julia binding passes equals the Python mirror's row-major matrix (the C ABI's convention), and
+    the transposed form would not."""
+    import qrochet as Q
+
+    g = np.random.default_rng(7)
+    arr = g.standard_normal((2, 2, 2, 2)) + 1j * g.standard_normal((2, 2, 2, 2))
+    order = [(5, True), (4, False), (5, False), (4, True)]
+    mem, M = _julia_gatematrix_memory(arr, order, [4, 5])
+    dense = Q.Dense(Q.Operator(), arr, [Q.Site(i, dual) for i, dual in order])
+    row_major = np.ascontiguousarray(dense.matrix([4, 5])).ravel()
+    np.testing.assert_array_equal(mem, row_major)
+    assert not np.array_equal(M.flatten(order="F"), row_major), "the transposed memory differs"
+
+
+def test_julia_gate_call_sites_pass_gatematrix_unchanged():
+    """Every gate that crosses the C ABI from Julia is gatematrix's result as it is (no further
+    transpose), so evolve!, evolve_layer! and expect agree on the memory order."""
+    text = open(JULIA).read()
+    uses = [m.start() for m in re.finditer(r"gatematrix\(", text)]
+    calls = [i for i in uses if not text[max(0, i - 9):i].endswith("function ")]
+    assert len(calls) >= 3
+    for i in calls:
+        assert text[i - 12:i] == "ComplexF64.(", text[i - 40:i + 30]
+    assert "permutedims(gatematrix" not in text and "transpose(gatematrix" not in text
