@@ -212,8 +212,9 @@ LinearAlgebra.normalize!(c::GPUChain, root::Site) =
 
 function Qrochet.truncate!(c::GPUChain, bond; threshold = nothing, maxdim = nothing)
     s1, s2 = Qrochet.id.(bond)
+    # -1 tells the C ABI "no maxdim"; a maxdim below 1 keeps nothing, as 1:min(dim, maxdim) does
     check(ccall((:qr_truncate, libqrochet), Cint, (Ptr{Cvoid}, Cint, Cint, Cdouble, Cint), c.handle, s1 - 1, s2 - 1,
-                isnothing(threshold) ? NaN : Float64(threshold), isnothing(maxdim) ? -1 : maxdim), Tuple(bond))
+                isnothing(threshold) ? NaN : Float64(threshold), isnothing(maxdim) ? -1 : max(0, maxdim)), Tuple(bond))
     return c
 end
 

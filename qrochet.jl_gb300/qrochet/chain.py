@@ -530,12 +530,11 @@ def isrightcanonical(psi: Chain, site, atol=1e-12):
 
 
 def truncate_(psi: Chain, bond, threshold=None, maxdim=None):
-    """``truncate!`` (Chain.jl:390-422)."""
+    """``truncate!`` (Chain.jl:390-422).  A maxdim below 1 keeps nothing, as ``1:min(dim,
+    maxdim)`` is empty there: the bond is sliced to size 0."""
     s1, s2 = (_site_id(s) for s in bond)
     th = float("nan") if threshold is None else float(threshold)
-    md = -1 if maxdim is None else int(maxdim)
-    if maxdim is not None and md < 0:
-        raise ArgumentError("maxdim must be non-negative")
+    md = -1 if maxdim is None else max(0, int(maxdim))  # -1 tells the C ABI "no maxdim"
     check(lib().qr_truncate(psi._h, s1 - 1, s2 - 1, th, md), bond=tuple(bond))
     return psi
 

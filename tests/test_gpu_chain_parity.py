@@ -199,6 +199,14 @@ def test_truncate_to_an_empty_bond():
         Q.canonize_(psi)
     with pytest.raises(Q.ArgumentError, match="size 0"):
         Q.evolve_(psi, Q.gate_from_matrix(np.eye(4), [1, 2]), threshold=1e-10, maxdim=4)
+    # a maxdim below 1 keeps nothing either: 1:min(dim, maxdim) is empty (Chain.jl:404-406)
+    for md in (0, -3):
+        psi2, ref2 = _pair(4, 3, seed=12)
+        Q.canonize_site_(psi2, 2, "right", "svd")
+        O.canonize_site_(ref2, 1, "right", "svd")
+        Q.truncate_(psi2, (2, 3), maxdim=md)
+        O.truncate_(ref2, (1, 2), maxdim=md)
+        assert psi2.bond_dims() == ref2.bond_dims() and psi2.bond_dims()[1] == 0
 
 
 def test_contract_between():
