@@ -246,7 +246,7 @@ function Qrochet.evolve!(c::GPUChain, gate::Dense; threshold = nothing, maxdim =
     else
         check(ccall((:qr_evolve_2site, libqrochet), Cint,
                     (Ptr{Cvoid}, Cint, Ptr{ComplexF64}, Cdouble, Cint, Cint, Cint), c.handle, lanes[1] - 1, M,
-                    isnothing(threshold) ? NaN : Float64(threshold), isnothing(maxdim) ? -1 : maxdim,
+                    isnothing(threshold) ? NaN : Float64(threshold), isnothing(maxdim) ? -1 : max(0, maxdim),
                     iscanonical, renormalize))
     end
     return c
@@ -267,7 +267,7 @@ function evolve_layer!(c::GPUChain, gates::AbstractVector{<:Dense}; threshold = 
     check(ccall((:qr_evolve_layer, libqrochet), Cint,
                 (Ptr{Cvoid}, Cint, Ptr{Cint}, Ptr{ComplexF64}, Cdouble, Cint, Cint, Cint, Cint),
                 c.handle, length(sites), sites, mats, isnothing(threshold) ? NaN : Float64(threshold),
-                isnothing(maxdim) ? -1 : maxdim, iscanonical, renormalize, lanes))
+                isnothing(maxdim) ? -1 : max(0, maxdim), iscanonical, renormalize, lanes))
     return c
 end
 

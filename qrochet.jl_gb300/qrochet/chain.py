@@ -552,7 +552,7 @@ def evolve_(psi: Chain, gate: Dense, threshold=None, maxdim=None, iscanonical=Fa
         check(lib().qr_evolve_1site(psi._h, lanes[0] - 1, dptr(m)))
     else:
         th = float("nan") if threshold is None else float(threshold)
-        md = -1 if maxdim is None else int(maxdim)
+        md = -1 if maxdim is None else max(0, int(maxdim))  # below 1: the bond is sliced to size 0
         check(lib().qr_evolve_2site(psi._h, lanes[0] - 1, dptr(m), th, md, int(bool(iscanonical)),
                                     int(bool(renormalize))))
     return psi
@@ -572,7 +572,7 @@ def evolve_layer_(psi: Chain, gates, threshold=None, maxdim=None, iscanonical=Fa
     k = len(sites)
     packed = np.ascontiguousarray(np.concatenate(mats) if mats else np.zeros(1, dtype=np.complex128))
     th = float("nan") if threshold is None else float(threshold)
-    md = -1 if maxdim is None else int(maxdim)
+    md = -1 if maxdim is None else max(0, int(maxdim))
     check(lib().qr_evolve_layer(psi._h, k, (C.c_int * max(k, 1))(*sites), dptr(packed), th, md,
                                 int(bool(iscanonical)), int(bool(renormalize)), int(lanes)))
     return psi

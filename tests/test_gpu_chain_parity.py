@@ -207,6 +207,13 @@ def test_truncate_to_an_empty_bond():
         Q.truncate_(psi2, (2, 3), maxdim=md)
         O.truncate_(ref2, (1, 2), maxdim=md)
         assert psi2.bond_dims() == ref2.bond_dims() and psi2.bond_dims()[1] == 0
+    # and evolve! truncates its new bond the same way (Chain.jl:645-649 -> truncate!)
+    u = R.haar_unitary(R.rng(4), 4)
+    psi3, ref3 = _pair(4, 3, seed=12)
+    Q.evolve_(psi3, Q.gate_from_matrix(u, [2, 3]), maxdim=-2)
+    O.evolve_2site_(ref3, 1, u, maxdim=-2)
+    assert psi3.bond_dims() == ref3.bond_dims() and psi3.bond_dims()[1] == 0
+    assert Q.norm(psi3) == 0.0
 
 
 def test_contract_between():
