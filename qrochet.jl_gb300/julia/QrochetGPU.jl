@@ -235,11 +235,23 @@ function gatematrix(gate::Dense, lanes)
     return collect(transpose(M))  # row-major storage of M
 end
 
-function Qrochet.evolve!(c::GPUChain, gate::Dense; threshold = nothing, maxdim = nothing, iscanonical = false,
-                         renormalize = false)
+# the checks evolve! makes before it touches the chain (Chain.jl:552-581); returns the sorted lanes
+function checkgate(c::GPUChain, gate::Dense)
+    Qrochet.socket(gate) isa Qrochet.Operator ||
+        throw(ArgumentError("Gate must be an operator, but got $(Qrochet.socket(gate))"))
+    issetequal(adjoint.(Qrochet.inputs(gate)), Qrochet.outputs(gate)) ||
+        throw(ArgumentError("Gate inputs ($(Qrochet.inputs(gate))) and outputs ($(Qrochet.outputs(gate))) must be the same"))
+    all(s -> 1 <= Qrochet.id(s) <= c.n, Qrochet.outputs(gate)) ||
+        throw(ArgumentError("Gate inputs ($(Qrochet.inputs(gate))) must be a subset of the TN sites"))
     lanes = sort!(map(Qrochet.id, Qrochet.outputs(gate)))
     length(lanes) > 2 && throw(ArgumentError("Invalid number of lanes $(length(lanes)), maximum is 2"))
     length(lanes) == 2 && lanes[2] != lanes[1] + 1 && throw(ArgumentError("Gate lanes must be contiguous"))
+    return lanes
+end
+
+function Qrochet.evolve!(c::GPUChain, gate::Dense; threshold = nothing, maxdim = nothing, iscanonical = false,
+                         renormalize = false)
+    lanes = checkgate(c, gate)
     M = ComplexF64.(gatematrix(gate, lanes))
     if length(lanes) == 1
         check(ccall((:qr_evolve_1site, libqrochet), Cint, (Ptr{Cvoid}, Cint, Ptr{ComplexF64}), c.handle, lanes[1] - 1, M))
@@ -259,8 +271,8 @@ function evolve_layer!(c::GPUChain, gates::AbstractVector{<:Dense}; threshold = 
     sites = Cint[]
     mats = ComplexF64[]
     for gate in gates
-        ls = sort!(map(Qrochet.id, Qrochet.outputs(gate)))
-        (length(ls) == 2 && ls[2] == ls[1] + 1) || throw(ArgumentError("evolve_layer! takes two-site gates on contiguous lanes"))
+        ls = checkgate(c, gate)
+        length(ls) == 2 || throw(ArgumentError("evolve_layer! takes two-site gates"))
         push!(sites, ls[1] - 1)
         append!(mats, vec(ComplexF64.(gatematrix(gate, ls))))  # memory order as qr_evolve_2site takes it
     end
@@ -287,7 +299,7 @@ end
 function Qrochet.expect(c::GPUChain, observables)
     firsts, nl, mats = Cint[], Cint[], ComplexF64[]
     for o in observables
-        lanes = sort!(map(Qrochet.id, Qrochet.outputs(o)))
+        lanes = checkgate(c, o)
         push!(firsts, lanes[1] - 1)
         push!(nl, length(lanes))
         append!(mats, vec(ComplexF64.(gatematrix(o, lanes))))  # row-major M, as for qr_evolve_2site
