@@ -50,11 +50,27 @@ function GPUChain(arrays::Vector{<:AbstractArray}; order = (:o, :l, :r), precisi
     n = length(arrays)
     ord = collect(order)
     periodic = boundary isa Qrochet.Periodic
+    # the reference constructor's checks (Chain.jl:36-41, 64-68), plus matching bond sizes, which the
+    # library relies on when it reads each array (cl * d * cr elements)
+    n >= 2 || throw(ArgumentError("a Chain needs at least 2 sites"))
+    if periodic
+        @assert all(==(3) ∘ ndims, arrays) "All arrays must have 3 dimensions"
+    else
+        @assert ndims(arrays[1]) == 2 "First array must have 2 dimensions"
+        @assert all(==(3) ∘ ndims, arrays[2:end-1]) "All arrays must have 3 dimensions"
+        @assert ndims(arrays[end]) == 2 "Last array must have 2 dimensions"
+    end
+    issetequal(ord, [:o, :l, :r]) || throw(ArgumentError("order must be a permutation of [\"o\", \"l\", \"r\"]"))
     dims = map(enumerate(arrays)) do (i, a)
         sub = filter(x -> periodic || !((i == 1 && x == :l) || (i == n && x == :r)), ord)
         Dict(zip(sub, size(a)))
     end
     d = dims[1][:o]
+    all(x -> x[:o] == d, dims) || throw(DimensionMismatch("all sites must share the physical dimension"))
+    for i in 1:(periodic ? n : n - 1)
+        r, l = dims[i][:r], dims[mod1(i + 1, n)][:l]
+        r == l || throw(DimensionMismatch("bond $i: $r != $l"))
+    end
     h = Ref{Ptr{Cvoid}}(C_NULL)
     if periodic
         bonds = Cint[dims[i][:r] for i in 1:n]
