@@ -304,6 +304,8 @@ function Qrochet.overlap(a::GPUChain, b::GPUChain)
     check(ccall((:qr_overlap, libqrochet), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ref{ComplexF64}), a.handle, b.handle, out))
     return out[]
 end
+# the socket-dispatched form overlap(a, b) forwards to (Chain.jl:737-740)
+Qrochet.overlap(::State, a::GPUChain, ::State, b::GPUChain) = Qrochet.overlap(a, b)
 
 function LinearAlgebra.norm(c::GPUChain, p::Real = 2)
     p == 2 || throw(ArgumentError("only L2-norm is implemented yet"))
