@@ -226,6 +226,32 @@ Qrochet.mixed_canonize!(c::GPUChain, center::Site) =
 LinearAlgebra.normalize!(c::GPUChain, root::Site) =
     (check(ccall((:qr_normalize, libqrochet), Cint, (Ptr{Cvoid}, Cint), c.handle, Qrochet.id(root) - 1)); c)
 
+# the non-mutating forms (Chain.jl:335, 378, 460, 499)
+Qrochet.canonize_site(c::GPUChain, args...; kwargs...) = Qrochet.canonize_site!(copy(c), args...; kwargs...)
+Qrochet.mixed_canonize(c::GPUChain, args...; kwargs...) = Qrochet.mixed_canonize!(copy(c), args...; kwargs...)
+Qrochet.truncate(c::GPUChain, args...; kwargs...) = Qrochet.truncate!(copy(c), args...; kwargs...)
+
+"""||A^H A - I||_F of site `site` viewed [(l,o) x r] (`QR_DIR_LEFT`) or ||A A^H - I||_F over
+[l x (o,r)] (`QR_DIR_RIGHT`); the open ends get the reference's dummy dimension of size 1."""
+function canonicality_error(c::GPUChain, site::Site, dir)
+    err = Ref{Float64}(0)
+    check(ccall((:qr_canonicality_error, libqrochet), Cint, (Ptr{Cvoid}, Cint, Cint, Ref{Float64}), c.handle,
+                Qrochet.id(site) - 1, dir, err))
+    return err[]
+end
+
+# isapprox(A^H A, I; atol) with atol > 0 compares the Frobenius norm of the difference (Chain.jl:424-458)
+Qrochet.isleftcanonical(c::GPUChain, site::Site; atol::Real = 1e-12) = canonicality_error(c, site, QR_DIR_LEFT) <= atol
+Qrochet.isrightcanonical(c::GPUChain, site::Site; atol::Real = 1e-12) = canonicality_error(c, site, QR_DIR_RIGHT) <= atol
+
+# contract!(tn, Val(:between), site1, site2; direction, delete_Λ) (Chain.jl:309-333)
+function Qrochet.Tenet.contract!(c::GPUChain, ::Val{:between}, site1::Site, site2::Site; direction::Symbol = :left,
+                                 delete_Λ = true)
+    check(ccall((:qr_contract_between, libqrochet), Cint, (Ptr{Cvoid}, Cint, Cint, Cint, Cint), c.handle,
+                Qrochet.id(site1) - 1, Qrochet.id(site2) - 1, _dir(direction), delete_Λ))
+    return c
+end
+
 function Qrochet.truncate!(c::GPUChain, bond; threshold = nothing, maxdim = nothing)
     s1, s2 = Qrochet.id.(bond)
     # -1 tells the C ABI "no maxdim"; a maxdim below 1 keeps nothing, as 1:min(dim, maxdim) does

@@ -211,7 +211,8 @@ def test_julia_binds_the_reference_methods():
                 "qr_chain_copy", "qr_canonize_site", "qr_canonize", "qr_mixed_canonize", "qr_normalize",
                 "qr_truncate", "qr_evolve_1site", "qr_evolve_2site", "qr_evolve_layer", "qr_expect",
                 "qr_overlap", "qr_norm", "qr_chain_random", "qr_chain_save", "qr_chain_load",
-                "qr_chain_has_lambda", "qr_chain_get_lambda", "qr_chain_set_precision"):
+                "qr_chain_has_lambda", "qr_chain_get_lambda", "qr_chain_set_precision", "qr_canonicality_error",
+                "qr_contract_between"):
         assert sym in called, sym
 
 
