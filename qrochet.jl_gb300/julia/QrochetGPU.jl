@@ -354,6 +354,57 @@ function Qrochet.expect(c::GPUChain, observables)
     return out[]
 end
 
-export GPUChain, bond_dims, sitearray, spectrum, setprecision!, save, load, read_checkpoint
+"""
+    GPUMPO(arrays; order = (:o, :i, :l, :r))
+
+Open-boundary MPO resident on the GPU, built from the same arrays as `MPO(arrays)`
+(`Chain(Operator(), Open(), arrays; order)`, Chain.jl:133-172): the ends drop `:l` / `:r`.
+"""
+mutable struct GPUMPO
+    handle::Ptr{Cvoid}
+    n::Int
+    d::Int
+end
+
+function GPUMPO(arrays::Vector{<:AbstractArray}; order = (:o, :i, :l, :r))
+    n = length(arrays)
+    ord = collect(order)
+    n >= 2 || throw(ArgumentError("an MPO needs at least 2 sites"))
+    @assert ndims(arrays[1]) == 3 "First array must have 3 dimensions"
+    @assert all(==(4) ∘ ndims, arrays[2:end-1]) "All arrays must have 4 dimensions"
+    @assert ndims(arrays[end]) == 3 "Last array must have 3 dimensions"
+    issetequal(ord, [:o, :i, :l, :r]) || throw(ArgumentError("order must be a permutation of [\"o\", \"i\", \"l\", \"r\"]"))
+    dims = map(enumerate(arrays)) do (i, a)
+        sub = filter(x -> !((i == 1 && x == :l) || (i == n && x == :r)), ord)
+        Dict(zip(sub, size(a)))
+    end
+    d = dims[1][:o]
+    all(x -> x[:o] == d && x[:i] == d, dims) || throw(DimensionMismatch("all sites must share the physical dimension"))
+    for i in 1:n-1
+        dims[i][:r] == dims[i+1][:l] || throw(DimensionMismatch("MPO bond $i: $(dims[i][:r]) != $(dims[i+1][:l])"))
+    end
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    bonds = Cint[dims[i][:r] for i in 1:n-1]
+    check(ccall((:qr_mpo_create, libqrochet), Cint, (Cint, Cint, Ptr{Cint}, Ref{Ptr{Cvoid}}), n, d, bonds, h))
+    w = GPUMPO(h[], n, d)
+    finalizer(x -> ccall((:qr_mpo_free, libqrochet), Cint, (Ptr{Cvoid},), x.handle), w)
+    ordstr = join(String.(ord))
+    for (i, a) in enumerate(arrays)
+        buf = convert(Array{ComplexF64}, a)
+        check(ccall((:qr_mpo_upload_site, libqrochet), Cint, (Ptr{Cvoid}, Cint, Ptr{ComplexF64}, Cstring),
+                    w.handle, i - 1, buf, ordstr))
+    end
+    return w
+end
+
+"""`<ψ|H|ψ>`: `contract(merge(Quantum(ψ), Quantum(H), Quantum(ψ)'))` (src/Quantum.jl:330-348) as one
+environment sweep on the device."""
+function mpo_expect(ψ::GPUChain, H::GPUMPO)
+    out = Ref{ComplexF64}(0)
+    check(ccall((:qr_mpo_expect, libqrochet), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ref{ComplexF64}), ψ.handle, H.handle, out))
+    return out[]
+end
+
+export GPUChain, GPUMPO, mpo_expect, bond_dims, sitearray, spectrum, setprecision!, save, load, read_checkpoint
 
 end # module

@@ -212,7 +212,7 @@ def test_julia_binds_the_reference_methods():
                 "qr_truncate", "qr_evolve_1site", "qr_evolve_2site", "qr_evolve_layer", "qr_expect",
                 "qr_overlap", "qr_norm", "qr_chain_random", "qr_chain_save", "qr_chain_load",
                 "qr_chain_has_lambda", "qr_chain_get_lambda", "qr_chain_set_precision", "qr_canonicality_error",
-                "qr_contract_between"):
+                "qr_contract_between", "qr_mpo_create", "qr_mpo_upload_site", "qr_mpo_expect", "qr_mpo_free"):
         assert sym in called, sym
 
 
