@@ -8,7 +8,7 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import check, dptr, lib
+from ._lib import ArgumentError, check, dptr, lib
 from .serve import PAULI_CODE, Request
 
 
@@ -50,8 +50,13 @@ class Batch:
         self._reqs.append(req)
         return rid.value
 
+    def _req(self, rid):
+        if not isinstance(rid, (int, np.integer)) or not 0 <= rid < len(self._reqs):
+            raise ArgumentError("bad batch request id")
+        return self._reqs[rid]
+
     def plan(self, rid):
-        req = self._reqs[rid]
+        req = self._req(rid)
         out = np.zeros(max(1, len(req.gates)), dtype=np.int32)
         nl = C.c_int()
         check(lib().qr_batch_plan(self._h, rid, out.ctypes.data_as(C.POINTER(C.c_int)), C.byref(nl)))
@@ -64,7 +69,7 @@ class Batch:
 
     def result(self, rid):
         """{'values': <psi|P|psi> per string, 'status': 0 or the failing status code}"""
-        n = len(self._reqs[rid].observables)
+        n = len(self._req(rid).observables)
         vals = np.zeros(2 * max(1, n))
         st = C.c_int()
         check(lib().qr_batch_result(self._h, rid, C.byref(st), dptr(vals)))
@@ -76,7 +81,7 @@ class Batch:
         return r["values"]
 
     def bond_dims(self, rid):
-        out = np.zeros(self._reqs[rid].n - 1, dtype=np.int32)
+        out = np.zeros(self._req(rid).n - 1, dtype=np.int32)
         check(lib().qr_batch_bond_dims(self._h, rid, out.ctypes.data_as(C.POINTER(C.c_int))))
         return [int(x) for x in out]
 

@@ -49,3 +49,37 @@ def test_rejects_what_it_cannot_run(built):
         ok = b.add(S.random_request(g, n_range=(6, 6), depth_range=(2, 2), chi_choices=(8,), nobs=1))
         with pytest.raises(_lib.ArgumentError, match="not run"):
             b.result(ok)
+
+
+def test_validation_and_empty_cases(built):
+    """Each rejection qr_batch_add / qr_batch_plan / qr_batch_run make before any device work, and
+    the plan of a request without gates (no layers)."""
+    from qrochet.batch import Batch
+
+    with Batch() as b:
+        with pytest.raises(_lib.ArgumentError, match="empty batch"):
+            b.run()
+        with pytest.raises(_lib.ArgumentError, match="n >= 2"):
+            b.add(S.Request(n=1, chi_max=8, gates=[], observables=[]))
+        with pytest.raises(_lib.ArgumentError, match="Pauli string entry"):
+            b.add(S.Request(n=4, chi_max=8, gates=[], observables=[[(5, "Z")]]))
+        with pytest.raises(_lib.ArgumentError, match="gate site"):
+            b.add(S.Request(n=4, chi_max=8, gates=[(0, np.eye(4))], observables=[]))
+        rid = b.add(S.Request(n=4, chi_max=8, gates=[], observables=[[(1, "Z")]]))
+        layers, nl = b.plan(rid)
+        assert nl == 0 and len(layers) == 0
+        with pytest.raises(_lib.ArgumentError, match="request id"):
+            b.plan(rid + 1)
+
+
+def test_layers_follow_circuit_order(built):
+    """A gate opens a new layer exactly when it shares a site with a gate of the current layer,
+    so gates on disjoint sites stay together and the order of the circuit is kept."""
+    from qrochet.batch import Batch
+
+    u = np.eye(4)
+    gates = [(1, u), (3, u), (5, u), (2, u), (4, u), (1, u), (6, u), (3, u)]
+    with Batch() as b:
+        rid = b.add(S.Request(n=8, chi_max=8, gates=gates, observables=[]))
+        layers, nl = b.plan(rid)
+    assert list(layers) == [0, 0, 0, 1, 1, 2, 2, 2] and nl == 3
