@@ -9,7 +9,7 @@ import ctypes as C
 import numpy as np
 
 from ._lib import ArgumentError, check, dptr, lib
-from .serve import PAULI_CODE, Request
+from .serve import Request, pauli_codes
 
 
 class Batch:
@@ -42,7 +42,7 @@ class Batch:
                                   if req.gates else np.zeros(1, dtype=np.complex128))
         w = np.array([len(o) for o in req.observables] or [0], dtype=np.int32)
         sites = np.array([s - 1 for o in req.observables for s, _ in o] or [0], dtype=np.int32)
-        codes = np.array([PAULI_CODE[p] for o in req.observables for _, p in o] or [0], dtype=np.int32)
+        codes = np.array(pauli_codes(req.observables) or [0], dtype=np.int32)
         ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int))  # noqa: E731
         rid = C.c_int()
         check(lib().qr_batch_add(self._h, req.n, req.chi_max, float(req.threshold), len(req.gates), ip(gs), dptr(gm),

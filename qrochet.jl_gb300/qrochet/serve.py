@@ -11,10 +11,21 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from ._lib import check, dptr, lib
+from ._lib import ArgumentError, check, dptr, lib
 from . import random as R
 
 PAULI_CODE = {"I": 0, "X": 1, "Y": 2, "Z": 3}
+
+
+def pauli_codes(observables):
+    """The library's codes (0 I, 1 X, 2 Y, 3 Z) of every string's letters, in order."""
+    out = []
+    for o in observables:
+        for _, p in o:
+            if p not in PAULI_CODE:
+                raise ArgumentError(f"Pauli letter must be one of I, X, Y, Z, got {p!r}")
+            out.append(PAULI_CODE[p])
+    return out
 
 
 @dataclass
@@ -56,7 +67,7 @@ class Server:
                                   if req.gates else np.zeros(1, dtype=np.complex128))
         w = np.array([len(o) for o in req.observables], dtype=np.int32)
         sites = np.array([s - 1 for o in req.observables for s, _ in o] or [0], dtype=np.int32)
-        codes = np.array([PAULI_CODE[p] for o in req.observables for _, p in o] or [0], dtype=np.int32)
+        codes = np.array(pauli_codes(req.observables) or [0], dtype=np.int32)
         t = C.c_uint64()
         ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int))  # noqa: E731
         check(lib().qr_server_submit(self._h, req.n, req.chi_max, float(req.threshold), len(req.gates), ip(gs),

@@ -63,6 +63,8 @@ def test_validation_and_empty_cases(built):
             b.add(S.Request(n=1, chi_max=8, gates=[], observables=[]))
         with pytest.raises(_lib.ArgumentError, match="Pauli string entry"):
             b.add(S.Request(n=4, chi_max=8, gates=[], observables=[[(5, "Z")]]))
+        with pytest.raises(_lib.ArgumentError, match="Pauli letter"):
+            b.add(S.Request(n=4, chi_max=8, gates=[], observables=[[(1, "W")]]))
         with pytest.raises(_lib.ArgumentError, match="gate site"):
             b.add(S.Request(n=4, chi_max=8, gates=[(0, np.eye(4))], observables=[]))
         rid = b.add(S.Request(n=4, chi_max=8, gates=[], observables=[[(1, "Z")]]))
