@@ -1225,8 +1225,8 @@ int qr_chain_load(const char* path, qr_chain** out) try {
   }
   for (int b = 0; b < n - 1 && !rc; b++) {
     if (!fl[b]) continue;
-    buf.resize(bd[b]);
-    if (fread(buf.data(), sizeof(double), buf.size(), fc.f) != buf.size()) rc = fail(QR_EINVAL, "truncated chain checkpoint");
+    buf.resize(bd[b] > 0 ? bd[b] : 1);  // an empty bond keeps an empty Lambda: pass a non-null pointer
+    if (fread(buf.data(), sizeof(double), (size_t)bd[b], fc.f) != (size_t)bd[b]) rc = fail(QR_EINVAL, "truncated chain checkpoint");
     else rc = qr_chain_set_lambda(h, b, buf.data(), bd[b]);
   }
   if (rc) {

@@ -39,3 +39,17 @@ def test_rejects_foreign_and_truncated_files(tmp_path):
     cut.write_bytes(data[:-8])
     with pytest.raises(ValueError):
         checkpoint.read(cut)
+
+
+def test_roundtrip_with_an_empty_bond(tmp_path):
+    """A chain whose bond was sliced to size 0 by truncate! (the null state) keeps its shapes and
+    its empty Lambda through a checkpoint."""
+    arrays = R.gaussian_mps_arrays(4, 3, seed=5, uniform=True)
+    arrays[1] = np.zeros((2, arrays[1].shape[1], 0), dtype=complex)
+    arrays[2] = np.zeros((2, 0, arrays[2].shape[2]), dtype=complex)
+    lams = [None, np.zeros(0), None]
+    path = tmp_path / "e.qrchain"
+    checkpoint.write(path, arrays, lams)
+    back, lb, _ = checkpoint.read(path)
+    assert [a.shape for a in back] == [a.shape for a in arrays]
+    assert lb[1] is not None and lb[1].size == 0 and lb[0] is None and lb[2] is None
