@@ -14,6 +14,9 @@ from .serve import Request, pauli_codes
 
 class Batch:
     def __init__(self, device=0, precision="fp64"):
+        self._h = None
+        if precision not in ("fp64", "mixed"):
+            raise ArgumentError(f"the batched engine runs in \"fp64\" or \"mixed\", not {precision!r}")
         self._h = C.c_void_p()
         check(lib().qr_batch_create(device, C.byref(self._h)))
         check(lib().qr_batch_set_precision(self._h, {"fp64": 0, "mixed": 1}[precision]))

@@ -32,6 +32,14 @@ _METHOD = {"qr": L.QR_METHOD_QR, "svd": L.QR_METHOD_SVD}
 _PREC = {"fp64": 0, "mixed": 1, "split": 2, "mixed+split": 3}
 
 
+def _choice(table, key, what):
+    """table[key], or the ArgumentError the reference raises for an unknown symbol."""
+    key = str(key).lstrip(":")
+    if key not in table:
+        raise ArgumentError(f"Unknown {what}=:{key}")
+    return table[key]
+
+
 def _norm_order(order, letters):
     order = tuple(str(x).lstrip(":") for x in order)
     if len(order) != len(letters) or set(order) != set(letters):
@@ -291,7 +299,7 @@ class Chain:
         return [self.site_array(i + 1, order) for i in range(self.n)]
 
     def set_precision(self, mode):
-        check(lib().qr_chain_set_precision(self._h, _PREC[mode]))
+        check(lib().qr_chain_set_precision(self._h, _choice(_PREC, mode, "precision")))
 
     def stream(self):
         p = C.c_void_p()
@@ -515,7 +523,7 @@ def contract_between(psi, site1, site2, direction="left", delete_lambda=True):
 
 def canonicality_error(psi: Chain, site, side):
     e = C.c_double()
-    check(lib().qr_canonicality_error(psi._h, _site_id(site) - 1, _DIR[side], C.byref(e)))
+    check(lib().qr_canonicality_error(psi._h, _site_id(site) - 1, _choice(_DIR, side, "direction"), C.byref(e)))
     return e.value
 
 

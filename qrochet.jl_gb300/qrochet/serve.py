@@ -40,7 +40,11 @@ class Request:
 
 class Server:
     def __init__(self, workers=8, hbm_budget_bytes=64 << 30, precision="mixed", device=0):
-        prec = {"fp64": 0, "mixed": 1, "split": 2, "mixed+split": 3}[precision]
+        self._h = None
+        modes = {"fp64": 0, "mixed": 1, "split": 2, "mixed+split": 3}
+        if precision not in modes:
+            raise ArgumentError(f"precision must be one of {sorted(modes)}, not {precision!r}")
+        prec = modes[precision]
         self._h = C.c_void_p()
         check(lib().qr_server_create(device, workers, int(hbm_budget_bytes), prec, C.byref(self._h)))
 

@@ -85,3 +85,12 @@ def test_layers_follow_circuit_order(built):
         rid = b.add(S.Request(n=8, chi_max=8, gates=gates, observables=[]))
         layers, nl = b.plan(rid)
     assert list(layers) == [0, 0, 0, 1, 1, 2, 2, 2] and nl == 3
+
+
+def test_unknown_precision_names(built):
+    from qrochet.batch import Batch
+
+    with pytest.raises(_lib.ArgumentError, match="fp64"):
+        Batch(precision="fp32")
+    with pytest.raises(_lib.ArgumentError, match="precision"):
+        S.Server(precision="half")
