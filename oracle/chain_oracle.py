@@ -176,20 +176,29 @@ def _scale_right(a, v):
 # contract!(::Chain, Val(:between)) -- Chain.jl:309-333
 # ---------------------------------------------------------------------------------------------
 def contract_between_(ch: OChain, site1: int, site2: int, direction="left", delete_lambda=True):
-    """Absorb the Lambda of bond (site1, site2) into site2 (``:right``) or site1 (``:left``)."""
-    if site2 != site1 + 1:
-        raise ArgumentError("sites must be adjacent")
-    lm = ch.lam[site1]
+    """Absorb the Lambda of the bond site1 and site2 share into site2 (``:right``) or site1
+    (``:left``) (Chain.jl:309-333).  ``tensors(tn; between)`` (Ansatz.jl:78-89) asserts two
+    different sites of the chain and finds nothing when they share no bond, which leaves the chain
+    as it is; the two sites may come in either order."""
+    if not (0 <= site1 < ch.n and 0 <= site2 < ch.n):
+        raise AssertionError("Site not found")
+    if site1 == site2:
+        raise AssertionError("Sites must be different")
+    if abs(site2 - site1) != 1:
+        return ch
+    b = min(site1, site2)
+    lm = ch.lam[b]
     if lm is None:
         return ch
+    # the bond is site1's right index when site1 is the left site of the pair, else its left index
     if direction == "right":
-        ch.sites[site2] = _scale_left(ch.sites[site2], lm)
+        ch.sites[site2] = (_scale_left if site2 > site1 else _scale_right)(ch.sites[site2], lm)
     elif direction == "left":
-        ch.sites[site1] = _scale_right(ch.sites[site1], lm)
+        ch.sites[site1] = (_scale_right if site2 > site1 else _scale_left)(ch.sites[site1], lm)
     else:
         raise ArgumentError(f"Unknown direction=:{direction}")
     if delete_lambda:
-        ch.lam[site1] = None
+        ch.lam[b] = None
     return ch
 
 

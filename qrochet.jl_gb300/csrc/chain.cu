@@ -1372,14 +1372,17 @@ int qr_normalize(qr_chain* h, int root) try {
 int qr_contract_between(qr_chain* h, int site1, int site2, int direction, int delete_lambda) try {
   QR_TRY(check_site(h, site1));
   QR_TRY(check_site(h, site2));
-  if (site2 != site1 + 1) return fail(QR_EINVAL, "sites must be adjacent");
+  // tensors(tn; between) (Ansatz.jl:78-89): two different sites; none shared bond -> nothing to do
+  if (site1 == site2) return fail(QR_EASSERT, "Sites must be different");
+  if (std::abs(site2 - site1) != 1) return QR_OK;
   QR_TRY(require_nonempty(h));
-  const int b = site1;
+  const int b = std::min(site1, site2);
   if (!h->lam[b]) return QR_OK;
+  const bool fwd = site2 == site1 + 1;  // site1 is the bond's left site: the bond is its r index
   if (direction == QR_DIR_RIGHT) {
-    QR_TRY(scale_site_by_lambda(h, site2, 0, h->lam[b], 0, 0.0));
+    QR_TRY(scale_site_by_lambda(h, site2, fwd ? 0 : 2, h->lam[b], 0, 0.0));
   } else if (direction == QR_DIR_LEFT) {
-    QR_TRY(scale_site_by_lambda(h, site1, 2, h->lam[b], 0, 0.0));
+    QR_TRY(scale_site_by_lambda(h, site1, fwd ? 2 : 0, h->lam[b], 0, 0.0));
   } else {
     return fail(QR_EINVAL, "Unknown direction");
   }
@@ -1392,6 +1395,7 @@ int qr_canonicality_error(const qr_chain* hc, int site, int direction, double* e
   qr_chain* h = const_cast<qr_chain*>(hc);
   QR_TRY(check_site(h, site));
   if (!err) return fail(QR_EINVAL, "null output");
+  if (direction != QR_DIR_LEFT && direction != QR_DIR_RIGHT) return fail(QR_EINVAL, "Unknown direction");
   QR_TRY(require_nonempty(h));
   cudaStream_t s = h->stream;
   const int cl = h->cl(site), d = h->d, cr = h->cr(site);

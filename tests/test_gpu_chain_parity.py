@@ -231,6 +231,17 @@ def test_contract_between():
         assert Q.isleftcanonical(b, i + 1)
     with pytest.raises(Q.ArgumentError):
         Q.contract_between(psi, 1, 2, direction="dummy")
+    # tensors(tn; between) (Ansatz.jl:78-89): the same site twice asserts, sites without a shared
+    # bond leave the chain as it is, a reversed adjacent pair absorbs that bond's Lambda
+    with pytest.raises(AssertionError):
+        Q.contract_between(psi, 2, 2)
+    far = Q.contract_between(psi, 1, 3)
+    assert far.lambda_flags() == psi.lambda_flags()
+    for i in range(1, 5):
+        a = Q.contract_between(psi, i + 1, i, direction="left")
+        r = O.contract_between_(ref.copy(), i, i - 1, direction="left")
+        _check_same(a, r)
+        assert a.lambda_between(i, i + 1) is None
 
 
 def test_evolve_1site_and_2site_exact():

@@ -60,6 +60,28 @@ def test_canonize_contract_between():
         assert np.allclose(b, can.sites[i] * can.lam[i][None, None, :])
 
 
+def test_contract_between_site_pairs():
+    """tensors(tn; between) (Ansatz.jl:78-89) behind contract! (Chain.jl:309-333): the same site
+    twice is an assertion, sites without a shared bond leave the chain as it is, and an adjacent
+    pair in reverse order absorbs the same bond's Lambda into the named site."""
+    can = O.canonize_(O.from_reference_arrays(R.rand_chain_state_arrays(R.rng(5), 5, 20, p=2)))
+    with pytest.raises(AssertionError):
+        O.contract_between_(can.copy(), 2, 2)
+    with pytest.raises(AssertionError):
+        O.contract_between_(can.copy(), 0, 7)
+    far = O.contract_between_(can.copy(), 0, 2)
+    assert all(np.array_equal(x, y) for x, y in zip(far.sites, can.sites))
+    assert all(l is not None for l in far.lam)
+    for i in range(4):
+        fwd = O.contract_between_(can.copy(), i, i + 1, direction="right")
+        rev = O.contract_between_(can.copy(), i + 1, i, direction="left")
+        assert rev.lam[i] is None
+        assert all(np.array_equal(x, y) for x, y in zip(fwd.sites, rev.sites))
+        fwd = O.contract_between_(can.copy(), i, i + 1, direction="left")
+        rev = O.contract_between_(can.copy(), i + 1, i, direction="right")
+        assert all(np.array_equal(x, y) for x, y in zip(fwd.sites, rev.sites))
+
+
 @pytest.mark.parametrize("method", ["qr", "svd"])
 def test_canonize_site(method):
     # Chain_test.jl:268-306
