@@ -116,6 +116,10 @@ int qr_canonize_site(qr_chain* h, int site, int direction, int method);
 int qr_canonize(qr_chain* h);
 int qr_mixed_canonize(qr_chain* h, int center);
 int qr_normalize(qr_chain* h, int root);
+/* contract!(tn, Val(:between), site1, site2; direction, delete_Λ): the Lambda of the bond the two
+   sites share goes into site2 (QR_DIR_RIGHT) or site1 (QR_DIR_LEFT), in either site order; the
+   same site twice is QR_EASSERT, sites that share no bond (or a bond without Lambda) are left
+   as they are (tensors(tn; between) finds nothing, src/Ansatz.jl:78-89). */
 int qr_contract_between(qr_chain* h, int site1, int site2, int direction, int delete_lambda);
 /* ||A^dagger A - I||_F of a site viewed [(l,o) x r] (left) or A A^dagger over [l x (o,r)] */
 int qr_canonicality_error(const qr_chain* h, int site, int direction, double* err);
