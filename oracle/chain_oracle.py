@@ -334,11 +334,13 @@ def mixed_canonize_(ch: OChain, center: int):
     return ch
 
 
-def normalize_(ch: OChain, root: int):
+def normalize_(ch: OChain, root: int, p=2):
+    """``normalize!(tn, root; p)`` (Chain.jl:532-536): mixed-canonical around ``root``, then the
+    Lambda between sites root - 1 and root divided by its p-norm."""
     _require_open(ch)
     mixed_canonize_(ch, root)
     lm = ch.lam[root - 1]
-    ch.lam[root - 1] = lm / np.linalg.norm(lm)
+    ch.lam[root - 1] = lm / np.linalg.norm(lm, p)
     return ch
 
 

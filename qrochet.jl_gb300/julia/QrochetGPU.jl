@@ -223,8 +223,22 @@ Qrochet.canonize(c::GPUChain) = Qrochet.canonize!(copy(c))
 Qrochet.mixed_canonize!(c::GPUChain, center::Site) =
     (check(ccall((:qr_mixed_canonize, libqrochet), Cint, (Ptr{Cvoid}, Cint), c.handle, Qrochet.id(center) - 1)); c)
 
-LinearAlgebra.normalize!(c::GPUChain, root::Site) =
-    (check(ccall((:qr_normalize, libqrochet), Cint, (Ptr{Cvoid}, Cint), c.handle, Qrochet.id(root) - 1)); c)
+# normalize!(tn, root; p) (Chain.jl:532-536): p = 2 on the device; another p re-scales the Lambda
+# between root - 1 and root on the host after the mixed canonization
+function LinearAlgebra.normalize!(c::GPUChain, root::Site; p::Real = 2)
+    if p == 2
+        check(ccall((:qr_normalize, libqrochet), Cint, (Ptr{Cvoid}, Cint), c.handle, Qrochet.id(root) - 1))
+        return c
+    end
+    Qrochet.mixed_canonize!(c, root)
+    r = Qrochet.id(root)
+    λ = spectrum(c, r - 1)
+    λ === nothing && throw(MissingSchmidtCoefficientsException((Site(r - 1), root)))
+    normalize!(λ, p)
+    check(ccall((:qr_chain_set_lambda, libqrochet), Cint, (Ptr{Cvoid}, Cint, Ptr{Float64}, Cint), c.handle, r - 2, λ,
+                length(λ)))
+    return c
+end
 
 # the non-mutating forms (Chain.jl:335, 378, 460, 499)
 Qrochet.canonize_site(c::GPUChain, args...; kwargs...) = Qrochet.canonize_site!(copy(c), args...; kwargs...)

@@ -501,9 +501,17 @@ def mixed_canonize(psi, center):
     return mixed_canonize_(psi.copy(), center)
 
 
-def normalize_(psi: Chain, root):
-    """``normalize!(::Chain, ::Site)`` (Chain.jl:532-536)."""
-    check(lib().qr_normalize(psi._h, _site_id(root) - 1))
+def normalize_(psi: Chain, root, p=2):
+    """``normalize!(::Chain, ::Site; p)`` (Chain.jl:532-536): mixed-canonical around ``root``, then
+    the Lambda between sites root - 1 and root divided by its p-norm (p = 2 on the device; other
+    p re-scale that Lambda on the host)."""
+    if p == 2:
+        check(lib().qr_normalize(psi._h, _site_id(root) - 1))
+        return psi
+    mixed_canonize_(psi, root)
+    r = _site_id(root)
+    lam = psi.lambda_between(r - 1, r)
+    psi.set_lambda(r - 2, lam / np.linalg.norm(lam, p))
     return psi
 
 

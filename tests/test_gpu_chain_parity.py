@@ -158,6 +158,11 @@ def test_mixed_canonize_and_normalize():
         assert Q.isrightcanonical(can, s)
     with pytest.raises(Q.ArgumentError):
         Q.mixed_canonize(psi, 1)
+    for p in (1, np.inf):  # normalize!(tn, root; p): the centre Lambda over its p-norm
+        a = Q.normalize_(psi.copy(), 3, p=p)
+        r = O.normalize_(ref.copy(), 2, p=p)
+        _check_same(a, r)
+        assert np.isclose(np.linalg.norm(a.lambda_between(2, 3), p), 1.0, rtol=1e-12)
     Q.normalize_(psi, 3)
     assert np.isclose(Q.norm(psi), 1.0, rtol=1e-12)
 

@@ -154,6 +154,18 @@ def test_normalize():
     assert np.isclose(O.norm(qtn), 1.0)
 
 
+@pytest.mark.parametrize("p", [1, np.inf, 3])
+def test_normalize_p_norm(p):
+    """normalize!(tn, root; p) divides the centre Lambda by its p-norm (Chain.jl:532-536)."""
+    g = R.rng(17)
+    qtn = _chain(g, [(4, 4), (4, 4, 4), (4, 4, 4), (4, 4, 4), (4, 4)])
+    two = O.normalize_(qtn.copy(), 2)
+    other = O.normalize_(qtn.copy(), 2, p=p)
+    lam2, lamp = two.lam[1], other.lam[1]
+    assert np.isclose(np.linalg.norm(lamp, p), 1.0)
+    assert np.allclose(lamp / lamp[0], lam2 / lam2[0])
+
+
 def test_order_permutation():
     # Chain_test.jl:92-116: custom order (:r, :o, :l) gives the same network
     g = R.rng(19)
