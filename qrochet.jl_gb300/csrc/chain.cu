@@ -1499,6 +1499,8 @@ int qr_evolve_layer(qr_chain* h, int ngates, const int* sites, const double* gat
         rc = evolve2_impl(l, sites[i], gates + (size_t)g4 * i, threshold, maxdim, iscanonical, 0);
     } catch (const std::bad_alloc&) {
       rc = fail(QR_ENOMEM, "host memory allocation failed");
+    } catch (const std::exception& x) {  // nothing may leave a lane's thread
+      rc = fail(QR_EHOST, std::string("host-side failure: ") + x.what());
     }
     if (!rc) rc = cuda_ok(cudaStreamSynchronize(l->stream), "lane synchronisation");
     else cudaStreamSynchronize(l->stream);
