@@ -595,10 +595,15 @@ def evolve_layer_(psi: Chain, gates, threshold=None, maxdim=None, iscanonical=Fa
 
 
 # ---- contractions ---------------------------------------------------------------------------------------
-def overlap(a: Chain, b: Chain):
-    """``overlap(a, b)`` = <b|a> (Chain.jl:740-748)."""
+def overlap(a, b):
+    """``overlap(a, b)`` = <b|a> (Chain.jl:740-748); one side may be a ``Product``, converted to a
+    chain with bonds of size 1 (``overlap(::Product, ::Chain)``, Chain.jl:751-752)."""
+    if isinstance(a, Product) and isinstance(b, Chain):
+        a = a.to_chain()
+    elif isinstance(b, Product) and isinstance(a, Chain):
+        b = b.to_chain()
     if not isinstance(a, Chain) or not isinstance(b, Chain):
-        raise ArgumentError("overlap needs two Chains")
+        raise ArgumentError("overlap needs two Chains, or a Chain and a Product")
     out = np.zeros(2)
     check(lib().qr_overlap(a._h, b._h, dptr(out)))
     return complex(out[0], out[1])
@@ -687,6 +692,26 @@ def zeros_chain(n, d=2):
     from .random import zero_product_arrays
 
     return MPS(zero_product_arrays(n, d))
+
+
+class Product:
+    """``Product(arrays)`` of site vectors, a product state (src/Ansatz/Product.jl:17-31), on the
+    host; ``to_chain()`` is ``convert(Chain, ::Product)`` (Chain.jl:174-183)."""
+
+    def __init__(self, vectors):
+        self.vectors = [np.asarray(v) for v in vectors]
+        from .random import product_arrays
+
+        self._arrays = product_arrays(self.vectors)  # validates
+
+    def sites(self):
+        return [Site(i + 1) for i in range(len(self.vectors))]
+
+    def nsites(self):
+        return len(self.vectors)
+
+    def to_chain(self):
+        return MPS(self._arrays)
 
 
 def ones_chain(n, d=2):

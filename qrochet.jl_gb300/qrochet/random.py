@@ -161,6 +161,20 @@ def one_product_arrays(n, d=2):
     return basis_product_arrays(n, d, 1)
 
 
+def product_arrays(vectors):
+    """``convert(Chain, Product(vectors))`` (Chain.jl:174-183): every site vector becomes a site
+    with bonds of size 1, (o, r) at site 1, (o, l, r) inside, (o, l) at site n."""
+    vs = [np.asarray(v) for v in vectors]
+    if len(vs) < 2 or any(v.ndim != 1 for v in vs) or len({v.shape[0] for v in vs}) != 1:
+        raise ValueError("a product state needs n >= 2 site vectors of one length")
+    n = len(vs)
+    out = []
+    for i, v in enumerate(vs):
+        v = v.astype(np.complex128)
+        out.append(np.asfortranarray(v.reshape(-1, 1) if i in (0, n - 1) else v.reshape(-1, 1, 1)))
+    return out
+
+
 def basis_product_arrays(n, d, level):
     """Every lane in basis state ``level``: arrays as ``MPS(arrays)`` takes them, (o, r) at site 1,
     (o, l, r) inside, (o, l) at site n, all bonds of size 1."""

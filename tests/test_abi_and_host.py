@@ -161,3 +161,23 @@ def test_product_arrays_and_lanes():
     w = MPO.__new__(MPO)
     w.n, w.d = 3, 2
     assert Q.nlanes(w) == 3
+
+
+def test_product_state_arrays():
+    """Product(vectors) (Product.jl:17-31) and its conversion to a chain's arrays with bonds of
+    size 1 (Chain.jl:174-183); bad inputs are rejected on the host."""
+    import qrochet as Q
+    from qrochet import random as R
+
+    vs = [np.array([1, 0]), np.array([0.6, 0.8j]), np.array([0, 1]), np.array([0.5, 0.5])]
+    p = Q.Product(vs)
+    assert Q.socket(p) == Q.State() and Q.nsites(p) == 4
+    arrs = R.product_arrays(vs)
+    assert [a.shape for a in arrs] == [(2, 1), (2, 1, 1), (2, 1, 1), (2, 1)]
+    for v, a in zip(vs, arrs):
+        assert np.array_equal(a.reshape(-1), v.astype(complex))
+    assert all(np.array_equal(a, b) for a, b in zip(R.product_arrays([np.eye(3)[0]] * 3), R.zero_product_arrays(3, 3)))
+    with pytest.raises(ValueError):
+        Q.Product([np.array([1, 0])])
+    with pytest.raises(ValueError):
+        Q.Product([np.array([1, 0]), np.array([1, 0, 0])])

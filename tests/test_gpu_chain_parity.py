@@ -577,6 +577,13 @@ def test_ones_product_chain():
     for i in range(1, n + 1):
         assert abs(Q.expect(psi, [Q.gate_from_matrix(R.PAULI["Z"], [i])]) + 1.0) <= 1e-14
     assert abs(Q.overlap(psi, Q.zeros_chain(n))) <= 1e-15
+    # overlap(::Product, ::Chain) (Chain.jl:751): the product converted to bonds of size 1
+    vs = [np.array([1, 0]), np.array([0.6, 0.8j]), np.array([0, 1]), np.array([1, 1]) / np.sqrt(2), np.array([1, 0])]
+    prod = Q.Product(vs)
+    chain, ref = _pair(5, 3, seed=14)
+    e, e_ref = Q.overlap(prod, chain), O.overlap(O.from_reference_arrays(R.product_arrays(vs)), ref)
+    assert abs(e - e_ref) <= RTOL * max(1.0, abs(e_ref))
+    assert abs(Q.overlap(chain, prod) - np.conj(e_ref)) <= RTOL * max(1.0, abs(e_ref))
 
 
 # Split-precision environment contractions (QR_SPLIT_CONTRACT): ~FP32 accuracy per site step.
