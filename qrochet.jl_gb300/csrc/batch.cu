@@ -622,7 +622,10 @@ void tune_load() {
   if (!fp) return;
   char key[256];
   int v = 0;
-  while (fscanf(fp, "%255s %d", key, &v) == 2) g_tune[key] = v;
+  // keep only choices the autotuner can make itself (4, 8 or 16 warps): the layer kernel's
+  // shape depends on it, so a damaged or hand-edited entry is re-tuned instead of launched
+  while (fscanf(fp, "%255s %d", key, &v) == 2)
+    if (v == 4 || v == 8 || v == 16) g_tune[key] = v;
   fclose(fp);
 }
 
