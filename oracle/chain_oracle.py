@@ -1,6 +1,6 @@
 """CPU oracle for the Chain (MPS/MPO) hot path -- TEST INFRASTRUCTURE ONLY.
 
-This module is the checker, never the product: only ``tests/``, ``__graft_entry__.smoke()``
+This module checks the library and is never part of it: only ``tests/``, ``__graft_entry__.smoke()``
 and the ``cpu_baseline`` / ``--impl reference`` legs of ``bench.py`` may import it.
 
 It restates, in NumPy on LAPACK, the semantics of Qrochet.jl's ``src/Ansatz/Chain.jl`` (v0.1.2)
