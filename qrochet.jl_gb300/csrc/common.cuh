@@ -40,7 +40,7 @@ int cuda_fail(cudaError_t e, const char* what);
 
 // Page-locked host scratch owned by the calling thread, for the small device-to-host reads on the
 // hot path (sweep counters, singular values, a scalar result).  A read into pageable memory goes
-// through the driver's staging buffer after the stream's earlier kernels; with many chains served
+// through the CUDA driver's staging buffer after the stream's earlier kernels; with many chains served
 // by concurrent threads those reads serialise.  Valid until the thread's next call; nullptr if the
 // allocation fails.
 void* host_scratch(size_t bytes);

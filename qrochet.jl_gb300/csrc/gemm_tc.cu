@@ -427,7 +427,7 @@ int encode_fn(EncodeTiled* out) {
     cudaDriverEntryPointQueryResult q;
     cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q);
     if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !p)
-      return fail(QR_ECUDA, "cuTensorMapEncodeTiled is not available from the driver");
+      return fail(QR_ECUDA, "cuTensorMapEncodeTiled is not available from the CUDA driver");
     fn = reinterpret_cast<EncodeTiled>(p);
   }
   *out = fn;
