@@ -221,6 +221,19 @@ def cpu_gate_step(al, ar, lam, u, maxdim):
     return ch
 
 
+def guarded(name, fn, world):
+    """Run a secondary leg; in a single process a failure is reported in the line (an "error"
+    entry) instead of losing the headline measurement.  With several ranks the exception
+    propagates, so that no rank is left waiting in a collective the failed one never joins."""
+    if world > 1:
+        return fn()
+    try:
+        return fn()
+    except Exception as x:  # noqa: BLE001 -- any failure of a secondary leg
+        print(f"bench: the {name} leg failed: {x!r}", file=sys.stderr, flush=True)
+        return {"error": f"{type(x).__name__}: {x}"}
+
+
 def run_batched(args, Q, dist, rank, world):
     """Batched solves/s on requests of the batched distribution (n ~ U[8,96], depth ~ U[4,32],
     cutoff 1e-10) with chi_max log-uniform in {16, 32, 64}: the bond classes the batched engine
@@ -760,13 +773,16 @@ def run_ours(args, chi):
                 accuracy[f"lambda_max_abs_err_{nm}_vs_oracle_over_sigma_max"] = (
                     float(np.max(np.abs(lv - lam_oracle)) / lam_oracle[0]) if lv.size == lam_oracle.size else None)
 
-    batched = run_batched(args, Q, dist, rank, world) if (args.batched > 0 and not args.quick) else None
+    batched = (guarded("batched", lambda: run_batched(args, Q, dist, rank, world), world)
+               if (args.batched > 0 and not args.quick) else None)
     if args.batched_full > 0 and not args.quick:
         batched = batched or {}
-        batched["full_distribution"] = run_batched_full(args, Q, dist, rank, world)
-    serving = run_serving(args, Q, dist, rank, world) if (args.serve > 0 and not args.quick) else None
-    mpo_env = run_mpo_env(args, Q) if (args.mpo_sites > 0 and not args.quick) else None
-    tebd = run_tebd(args, Q, local) if not (args.no_tebd or args.quick) else None
+        batched["full_distribution"] = guarded("batched_full", lambda: run_batched_full(args, Q, dist, rank, world),
+                                               world)
+    serving = (guarded("serving", lambda: run_serving(args, Q, dist, rank, world), world)
+               if (args.serve > 0 and not args.quick) else None)
+    mpo_env = guarded("mpo_env", lambda: run_mpo_env(args, Q), world) if (args.mpo_sites > 0 and not args.quick) else None
+    tebd = guarded("tebd", lambda: run_tebd(args, Q, local), world) if not (args.no_tebd or args.quick) else None
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "gate-steps/s", "n_gpus": world, "steps": args.steps,

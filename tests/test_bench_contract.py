@@ -28,3 +28,23 @@ def test_reference_arm_prints_one_json_line():
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["value"] == d["value"]
     assert d["e2e"] == {"value": d["value"], "unit": "gate-steps/s", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}
+
+
+def test_a_failing_secondary_leg_keeps_the_line():
+    """In a single process a secondary leg that raises is recorded as an error entry, so the
+    headline measurement still prints; with several ranks the failure propagates."""
+    import importlib.util
+
+    import pytest
+
+    spec = importlib.util.spec_from_file_location("bench_mod", os.path.join(ROOT, "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+
+    def boom():
+        raise RuntimeError("planted on the host")
+
+    assert bench.guarded("x", lambda: {"ok": 1}, 1) == {"ok": 1}
+    assert bench.guarded("x", boom, 1) == {"error": "RuntimeError: planted on the host"}
+    with pytest.raises(RuntimeError):
+        bench.guarded("x", boom, 2)
