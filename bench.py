@@ -139,9 +139,11 @@ class DevTimer:
 
 
 # DRAM bytes (read + write) per launch (one Jacobi sweep, or one GEMM) from one ncu capture of each
-# kernel on a 1024 x 1024 mixed SVD.  A sweep's traffic is the first touch of B and V and a GEMM's
-# the first touch of its operands, so it scales with the operand size: (k / 1024)^2 at k columns.
-NCU_TRAFFIC_1024 = {"jacobi_fp32": 16.937472e6 + 15.872e3, "jacobi_df": 33.711360e6 + 28.087296e6,
+# kernel on a 1024 x 1024 mixed SVD: jacobi_block_reg_k for jacobi_fp32, jacobi_block_df_k (the
+# full double-float sweeps) for jacobi_df, zgemm_df_k for zgemm_df.  A sweep's traffic is the first
+# touch of B and V and a GEMM's the first touch of its operands, so it scales with the operand
+# size: (k / 1024)^2 at k columns.
+NCU_TRAFFIC_1024 = {"jacobi_fp32": 16.937472e6 + 15.872e3, "jacobi_df": 34.0e6 + 5.3e6,
                     "zgemm_df": 16.850432e6}
 
 
